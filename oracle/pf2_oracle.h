@@ -1,0 +1,148 @@
+/*
+ * pf2_oracle.h - CPU oracle for the PFEM-2 time-step path (TEST INFRASTRUCTURE ONLY).
+ *
+ * A single-thread FP64 C restatement of the reference gpuPfem2 algorithms on the
+ * PFEM-2 step path.  Only the test suite, the smoke check and the CPU-baseline leg of
+ * the benchmark load it, always as the checker; the product never links it.
+ *
+ * Conventions: 0-based node and cell indices, int32 CSR (row offsets + sorted column
+ * indices), SoA particle arrays, all floating point in double.  Every function names
+ * the reference file:line it restates.  Compiled with -ffp-contract=off: where the
+ * reference's GPU code is contracted into fused multiply-adds by nvcc, the oracle calls
+ * fma() explicitly at the same place (marked "FMA as nvcc contracts"), so results on
+ * x86-64 and aarch64 hosts are identical.
+ */
+#ifndef PF2_ORACLE_H
+#define PF2_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- constants (src/common/constants.h:4-17) ---- */
+#define OR_DOUBLE_MIN 2e-6
+#define OR_MAX_LEVEL 4
+
+/* ---- quadrature (src/integration/quadrature_formula_2d.cu:17-24, _1d.cu:15-18) ---- */
+int or_face_quadrature(int index, double* coords3, double* weights); /* returns #points */
+int or_edge_quadrature(int index, double* coords, double* weights);
+
+/* ---- mesh (src/mesh_2d.cu) ---- */
+void or_mesh_geometry(int nc, const double* xy, const int* tri, double* area, double* invJ);
+int or_node_cells(int nv, int nc, const int* tri, int* offsets, int* cells); /* CSR node->cells, ascending */
+int or_neighbors(int nv, int nc, const int* tri, int* offsets, int* idx);   /* idx may be NULL: count only */
+int or_csr_structure(int nv, int nc, const int* tri, int* rowptr, int* col); /* col may be NULL */
+void or_edge_boundary_ids(int nc, const double* xy, const int* tri, double lx, double ly,
+                          int has_cylinder, double cx, double cy, double r, int* ids3);
+
+/* ---- CSR helpers ---- */
+int or_find_in_row(const int* rowptr, const int* col, int row, int target);
+void or_spmv(int n, const int* rowptr, const int* col, const double* val, const double* x, double* y);
+
+/* ---- assembly ---- */
+enum { OR_RHS_GAUSSIAN = 0, OR_RHS_SINSIN = 1 };
+void or_assemble_poisson(int nc, const double* xy, const int* tri, const double* area, const double* invJ,
+                         int rhs_kind, double lambda, const int* rowptr, const int* col, double* val, double* rhs);
+
+/* ---- Dirichlet BCs (src/Dirichlet_bcs.cu) ---- */
+void or_apply_bcs(int n, const int* rowptr, const int* col, double* val, double* rhs,
+                  int nbc, const int* bc_node, const double* bc_val);
+
+/* ---- solvers (src/linear_algebra/linear_solver.cu, preconditioners.cu) ---- */
+enum { OR_PRECOND_NONE = -1, OR_PRECOND_JACOBI = 0, OR_PRECOND_ILU = 1, OR_PRECOND_IC = 2 };
+typedef struct {
+    int iterations;
+    int converged;
+    double residual; /* sqrt(r^T z) for CG, |beta_k| for GMRES */
+} or_solve_info;
+void or_ilu0(int n, const int* rowptr, const int* col, double* lu);   /* in place on a copy of A */
+void or_ic0(int n, const int* rowptr, const int* col, double* l);     /* lower part holds L */
+void or_precond_apply(int kind, int n, const int* rowptr, const int* col, const double* fact,
+                      const double* invdiag, const double* src, double* dst, double* tmp);
+int or_pcg(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b,
+           double tol, int maxit, int precond, or_solve_info* info);
+int or_gmres(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b,
+             double tol, int maxit, int precond, or_solve_info* info);
+
+/* ---- particles (src/particles/particle_handler_2d.cu) ---- */
+int or_subcell_centers(int level, double* centers3);
+int or_determine_subcell(int level, double step, const double* l3);
+int or_seed(int nc, const double* xy, const int* tri, int level, const double* centers3,
+            double* px, double* py, double* l0, double* l1, double* l2, double* pu, double* pv, int* cell);
+void or_correct_velocity(int np, const int* tri, const int* cell, const double* l0, const double* l1,
+                         const double* l2, const double* ux, const double* uy,
+                         const double* ux_old, const double* uy_old, double* pu, double* pv);
+void or_project(int np, const int* tri, const int* cell, const double* l0, const double* l1, const double* l2,
+                const double* pu, const double* pv, int nv, double* ux, double* uy);
+/* Advection with cell location over `substeps` substeps, then the population check and
+ * reseed; the output is ordered by cell (stable), reseeded particles at the end of each
+ * cell in sub-cell order.  Returns the new particle count, or -1 if cap is too small. */
+int or_advect(int np, int cap, double* px, double* py, double* l0, double* l1, double* l2,
+              double* pu, double* pv, int* cell,
+              int nv, const double* xy, int nc, const int* tri, const double* invJ,
+              const int* nb_off, const int* nb_idx, const double* ux, const double* uy,
+              double dt, int substeps, int level, const double* centers3, int* n_deleted, int* n_added);
+int or_locate(double x, double y, int cell, const double* xy, const int* tri, const double* invJ,
+              const int* nb_off, const int* nb_idx, double* l3);
+
+/* ---- flow (cases/Cylinder2D/main.cu) ---- */
+typedef struct {
+    double rho, mu, dt, tol;
+    int maxit, scheme, substeps, level, n_outer, pressure_precond;
+    int calc_loads, body_id;
+    double thickness, mean_velocity;
+    double lx, ly;
+    int has_cylinder;
+    double cx, cy, radius;
+} or_params;
+
+typedef struct {
+    int particles;
+    int deleted, added;
+    int it_pred[2][8], it_pres[8], it_corr[2][8];
+    int conv_ok;
+    double cx, cy;
+} or_step_info;
+
+typedef struct or_flow or_flow;
+or_flow* or_flow_create(int nv, const double* xy, int nc, const int* tri, const or_params* p,
+                        int nbu, const int* bu_node, const double* bu_val,
+                        int nbv, const int* bv_node, const double* bv_val,
+                        int nbp, const int* bp_node, const double* bp_val, int particle_cap);
+void or_flow_destroy(or_flow* f);
+int or_flow_step(or_flow* f, or_step_info* info);
+int or_flow_particle_count(const or_flow* f);
+/* field ids: 0 ux,1 uy,2 ux_old,3 uy_old,4 pred_x,5 pred_y,6 p,7 p_old */
+void or_flow_get_field(const or_flow* f, int which, double* out);
+void or_flow_set_field(or_flow* f, int which, const double* in);
+void or_flow_get_particles(const or_flow* f, double* px, double* py, double* l0, double* l1, double* l2,
+                           double* pu, double* pv, int* cell);
+void or_flow_set_particles(or_flow* f, int np, const double* px, const double* py, const double* l0,
+                           const double* l1, const double* l2, const double* pu, const double* pv, const int* cell);
+int or_flow_csr_nnz(const or_flow* f);
+/* matrix ids: 0 pred_x, 1 pred_y, 2 pressure, 3 corr_x, 4 corr_y; rhs ids the same */
+void or_flow_get_matrix(const or_flow* f, int which, double* val, double* rhs);
+
+/* The individual flow stages, on explicit arrays (used by the parity tests). */
+void or_assemble_prediction(int nc, const double* xy, const int* tri, const double* area, const double* invJ,
+                            const int* edge_ids, const or_params* p, const double* ux, const double* uy,
+                            const double* ux_old, const double* uy_old, const double* p_old,
+                            const int* rowptr, const int* col, double* val_x, double* val_y,
+                            double* rhs_x, double* rhs_y);
+void or_assemble_pressure(int nc, const int* tri, const double* area, const double* invJ, const or_params* p,
+                          const double* predx, const double* predy, const double* p_old,
+                          const int* rowptr, const int* col, double* val, double* rhs);
+void or_assemble_correction(int nc, const int* tri, const double* area, const double* invJ, const or_params* p,
+                            const double* predx, const double* predy, const double* pres, const double* p_old,
+                            const int* rowptr, const int* col, double* val_x, double* val_y,
+                            double* rhs_x, double* rhs_y);
+void or_prediction_bc(int nc, const int* tri, const double* area, const double* invJ, const or_params* p,
+                      const double* pres, const double* p_old, int nbc, const int* bc_node,
+                      const double* bc_val, const int* node_to_bc, int component, double* out_val);
+int or_body_loads(int nc, const double* xy, const int* tri, const double* invJ, const int* edge_ids,
+                  const or_params* p, const double* ux, const double* uy, const double* pres, double* cxcy);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
