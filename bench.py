@@ -1,0 +1,306 @@
+#!/usr/bin/env python
+"""Benchmark of one PFEM-2 time step (ms per step) on the GB300 engine.
+
+Default workload: the channel-with-cylinder case (2.2 x 0.41 channel, cylinder r=0.05
+at (0.2, 0.2), 994,240 P1 triangles from the committed generator, 16 particles per
+cell, Scheme B, rho=1, mu=1e-3, dt=5e-4, drag/lift each step).  Synthetic input of the
+named shape: the mesh and particles are generated, the flow starts from rest and
+`--warmup` steps run before the timed ones.
+
+Arms:
+  default           the engine (C ABI via ctypes, CUDA kernels for sm_103a)
+  --impl reference  the CPU oracle of the same step (oracle/, single-thread FP64 port of
+                    the reference's algorithm) on a bounded sample, on the host cores
+
+Prints ONE JSON line (rank 0).  `value` is device time per step with all state
+resident in HBM; `e2e` is the same step driven through the C ABI with the inflow
+boundary values uploaded from pinned host memory and the fields (u, v, p) plus the
+step record copied back to pinned host memory every step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+from gpupfem2_gb300 import meshgen as mg  # noqa: E402
+
+WORKLOADS = {
+    # name: (mesh factory, channel length, height, cylinder, params)
+    "cylinder": dict(mesh=lambda: mg.cylinder_channel(), lx=2.2, ly=0.41, cyl=(0.2, 0.2, 0.05),
+                     params=dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3,
+                                 pressure_precond=2, calculate_loads=1, body_boundary_id=3, thickness=0.1,
+                                 mean_velocity=1.0)),
+    "channel": dict(mesh=lambda: mg.channel(), lx=4.0, ly=1.0, cyl=None,
+                    params=dict(rho=1.0, mu=0.01, dt=0.005, scheme=0, level=3, n_outer=2, substeps=3,
+                                pressure_precond=1)),
+    "square": dict(mesh=lambda: mg.unit_square(64), lx=1.0, ly=1.0, cyl=None,
+                   params=dict(rho=1.0, mu=0.01, dt=0.005, scheme=0, level=2, n_outer=2, substeps=3,
+                               pressure_precond=0)),
+}
+PRECOND_NAMES = {-1: "none", 0: "jacobi", 1: "ilu", 2: "ic"}
+PHASES = ["particles", "projection", "prediction_assembly", "prediction_solve", "pressure_assembly",
+          "pressure_solve", "correction_assembly", "correction_solve", "particle_correction"]
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def build_case(name, precond=None):
+    w = WORKLOADS[name]
+    xy, tri = w["mesh"]()
+    bu, bv, bp = mg.channel_boundary_nodes(xy, w["lx"], w["ly"], 1.5, cylinder=w["cyl"])
+    prm = dict(w["params"])
+    if precond is not None:
+        prm["pressure_precond"] = precond
+    return w, xy, tri, bu, bv, bp, prm
+
+
+class ClockSampler:
+    """nvidia-smi clocks during the timed region (200 ms period)."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                          "-i", "0", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(name, precond, max_seconds=25.0):
+    """The oracle's step on a bounded sample of the workload (one host core)."""
+    from oracle import oracle as O
+    w, xy, tri, bu, bv, bp, prm = build_case(name, precond)
+    kw = {k: v for k, v in prm.items() if k not in ("calculate_loads", "body_boundary_id", "mean_velocity",
+                                                    "thickness")}
+    cyl = w["cyl"]
+    op = O.make_params(lx=w["lx"], ly=w["ly"], tol=1e-8, has_cylinder=int(cyl is not None),
+                       cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
+                       calc_loads=prm.get("calculate_loads", 0), body_id=prm.get("body_boundary_id", -1),
+                       thickness=prm.get("thickness", 1.0), **kw)
+    flow = O.Flow(xy, tri, op, bu, bv, bp)
+    times = []
+    t_all = time.perf_counter()
+    while time.perf_counter() - t_all < max_seconds or not times:
+        t0 = time.perf_counter()
+        flow.step()
+        times.append(time.perf_counter() - t0)
+        if len(times) >= 3:
+            break
+    ms = 1000.0 * statistics.median(times)
+    return {"value": ms, "unit": "ms/step", "cores": 1, "kind": "port",
+            "sample": "%d oracle step(s) of the full %s workload (%d triangles, %d particles at the start), "
+                      "median" % (len(times), name, tri.shape[0], tri.shape[0] * prm["level"] ** 2)}
+
+
+def run_reference(args):
+    name, precond = args.workload, args.precond
+    base = cpu_baseline(name, precond, max_seconds=20.0)
+    line = {"metric": "ms per PFEM-2 step", "value": base["value"], "unit": "ms/step", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"], "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": name, "pressure_precond": PRECOND_NAMES[WORKLOADS[name]["params"]
+                                                                            ["pressure_precond"]
+                                                                            if precond is None else precond]},
+            "impl": "reference", "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="cylinder", choices=list(WORKLOADS))
+    ap.add_argument("--precond", type=int, default=None, help="pressure preconditioner override (0 J, 1 ILU, 2 IC)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args)
+        return
+    import torch
+    import gpupfem2_gb300 as g
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond)
+    mesh = g.Mesh2D.from_arrays(xy, tri)
+    mesh.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
+    params = g.default_params(**prm)
+    eng = g.FlowEngine(mesh, params, bu, bv, bp, capacity_factor=2.0)
+    eng.seed()
+    for _ in range(args.warmup):
+        eng.step()
+    info = eng.info()
+    torch.cuda.synchronize()
+    L = g.lib()
+    L.pf2_kernel_launches.restype = __import__("ctypes").c_ulonglong
+    # ---- timed region: K steps, device time with CUDA events on the launching stream
+    g._check(L.pf2_flow_enable_timing(eng.h, args.steps), "enable timing")
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pf2_clocks.csv")
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    n0 = L.pf2_kernel_launches()
+    with clocks:
+        start.record()
+        for _ in range(args.steps):
+            eng.step()
+        end.record()
+        torch.cuda.synchronize()
+    launches = L.pf2_kernel_launches() - n0
+    ms = start.elapsed_time(end) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    info = eng.info()
+    phase = (__import__("ctypes").c_double * 9)()
+    nst = __import__("ctypes").c_int()
+    g._check(L.pf2_flow_phase_times(eng.h, phase, __import__("ctypes").byref(nst)), "phase times")
+    phase_ms = {PHASES[k]: phase[k] / max(nst.value, 1) for k in range(9)}
+    g._check(L.pf2_flow_enable_timing(eng.h, 0), "disable timing")
+    # ---- end to end through the C ABI with host buffers
+    import ctypes as C
+    nv = mesh.nv
+    host_u = torch.empty(3 * nv, dtype=torch.float64, pin_memory=True)
+    inflow = torch.tensor([val for _, val in bu], dtype=torch.float64).pin_memory()
+    dev_inflow = torch.empty_like(inflow, device="cuda")
+    views = [_wrap(eng.field_ptr(n), nv) for n in ("ux", "uy", "p")]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        dev_inflow.copy_(inflow, non_blocking=True)
+        g._check(L.pf2_flow_set_boundary_values(eng.h, 0, g._dev(dev_inflow), g._stream()), "inflow")
+        eng.step()
+        for k, dv in enumerate(views):
+            host_u[k * nv:(k + 1) * nv].copy_(dv, non_blocking=True)
+        eng.info()
+    torch.cuda.synchronize()
+    e2e_ms = 1000.0 * (time.perf_counter() - t0) / args.e2e_steps
+    # ---- roofline of the dominant phase
+    peak, peak_kind = measured_peaks()
+    nnz = g.SparseMatrixCSR(mesh).nnz
+    np_ = info.particles
+    pres_iters = sum(info.it_pressure[k] for k in range(prm["n_outer"]))
+    dominant = max(phase_ms, key=phase_ms.get)
+    n = nv
+    if dominant == "pressure_solve":
+        # per CG iteration: 12 nnz (values + columns) + 4 (n+1) row offsets + x, r, p, q, z
+        # read/written + D^-1: 8 doubles per row
+        algo = pres_iters * (12.0 * nnz + 4.0 * (n + 1) + 64.0 * n)
+        unit_desc = "bytes per CG iteration 12 nnz + 4 (n+1) + 64 n, x %d iterations" % pres_iters
+    elif dominant == "particles":
+        # advect+locate 76 B/particle, scatter 12 B, gather 104 B (SoA 52 B moved in and out)
+        algo = np_ * (76.0 + 12.0 + 104.0)
+        unit_desc = "192 bytes per particle x %d particles" % np_
+    else:
+        algo = None
+        unit_desc = dominant
+    dom_ms = phase_ms[dominant]
+    achieved = (algo / (dom_ms * 1e-3) / 1e9) if algo else None
+    line = {
+        "metric": "ms per PFEM-2 step", "value": ms, "unit": "ms/step", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "triangles": int(tri.shape[0]), "nodes": int(nv), "nnz": int(nnz),
+                   "particles": int(np_), "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
+                   "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
+                   "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),
+                   "iterations_last_step": {"prediction": [list(info.it_prediction[c])[:prm["n_outer"]]
+                                                           for c in range(2)],
+                                            "pressure": list(info.it_pressure)[:prm["n_outer"]],
+                                            "correction": [list(info.it_correction[c])[:prm["n_outer"]]
+                                                           for c in range(2)]},
+                   "phase_ms": {k: round(v, 4) for k, v in phase_ms.items()}, "cx": info.cx, "cy": info.cy},
+        "e2e": {"value": e2e_ms, "unit": "ms/step", "h2d_bytes_per_step": int(inflow.numel() * 8),
+                "d2h_bytes_per_step": int(3 * nv * 8 + 8 * 5 * 8)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind, "algorithmic": unit_desc},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.precond)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def _wrap(ptr, n):
+    """A device tensor view of n doubles at ptr (through the CUDA array interface)."""
+    import torch
+
+    class _A:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False), "version": 3}
+
+    return torch.as_tensor(_A(), device="cuda")
+
+
+if __name__ == "__main__":
+    main()

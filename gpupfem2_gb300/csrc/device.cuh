@@ -1,0 +1,136 @@
+// device.cuh - device helpers shared by the kernels.
+//
+// Arithmetic whose result must match the reference bit for bit (cell geometry,
+// global->local transforms, advection, interpolation) is written with explicit
+// __fma_rn/__dmul_rn/__dadd_rn/__dsub_rn/__ddiv_rn intrinsics, which the compiler never
+// re-associates or fuses, at exactly the places where nvcc contracts the reference's
+// expressions into fused multiply-adds.  The CPU oracle calls fma() at the same places.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace pf2 {
+
+// Row-major invJ {d0, d1, d2, d3}.  shapeFuncGrad(i) mapped by invJ
+// (numerical_integrator_2d.cuh:8-20 with Matrix2x2::operator*, cuda_math.cuh:146-153):
+// grad N0 = (d0, d2), grad N1 = (d1, d3), grad N2 = (-d0 - d1, -d2 - d3).
+__device__ __forceinline__ void shape_grads(const double4_32a J, double2 g[3]) {
+    g[0] = make_double2(J.x, J.z);
+    g[1] = make_double2(J.y, J.w);
+    g[2] = make_double2(__dsub_rn(-J.x, J.y), __dsub_rn(-J.z, J.w));
+}
+
+// GEOMETRY::transformGlobalToLocal (geometry.cuh:14-23)
+__device__ __forceinline__ void global_to_local(double x, double y, const double4_32a J, const double2 v3, double& l0,
+                                                double& l1, double& l2) {
+    const double dx = __dsub_rn(x, v3.x), dy = __dsub_rn(y, v3.y);
+    l0 = __fma_rn(J.x, dx, __dmul_rn(J.z, dy));
+    l1 = __fma_rn(J.y, dx, __dmul_rn(J.w, dy));
+    l2 = __dsub_rn(__dsub_rn(1.0, l0), l1);
+}
+
+// GEOMETRY::isPointInsideUnitTriangle (geometry.cuh:37-46): NaN coordinates count as
+// inside, as with the reference's comparisons.
+__device__ __forceinline__ bool inside_unit(double l0, double l1, double l2) {
+    const double hi = 1.0 + kDoubleMin, lo = -kDoubleMin;
+    if (l0 > hi || l0 < lo) return false;
+    if (l1 > hi || l1 < lo) return false;
+    if (l2 > hi || l2 < lo) return false;
+    return true;
+}
+
+// sum_i L_i u(node_i) accumulated from 0.0 (particle_handler_2d.cu:62-66)
+__device__ __forceinline__ double interp3(double l0, double l1, double l2, double u0, double u1, double u2) {
+    double s = __fma_rn(l0, u0, 0.0);
+    s = __fma_rn(l1, u1, s);
+    return __fma_rn(l2, u2, s);
+}
+
+// transformLocalToGlobal (geometry.cuh:6-8)
+__device__ __forceinline__ double local_to_global(double L0, double L1, double L2, double a, double b, double c) {
+    return __fma_rn(c, L2, __fma_rn(a, L0, __dmul_rn(b, L1)));
+}
+
+// determineSubcell (particle_handler_2d.cu:10-33); may return >= n*n (no clamping)
+__device__ __forceinline__ int determine_subcell(int n, double step, double l0, double l1, double l2) {
+    const int i = (int)__dmul_rn(__dsub_rn(1.0, l1), (double)n);
+    int res = i * i;  // sum_{row<i} (2 row + 1)
+    const int j = (int)__dmul_rn(l0, (double)n);
+    res += 2 * j;
+    if (j != i) {
+        const double x = __dmul_rn(step, (double)(j + 1));
+        const double y = __fma_rn(-step, (double)(i + 1), 1.0);
+        const double z = __dsub_rn(__dsub_rn(1.0, x), y);
+        if (l2 < z) ++res;
+    }
+    return res;
+}
+
+// --------------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum (any blockDim multiple of 32, <= 1024); the result is returned to every
+// thread.  Fixed order, so repeated runs give identical bits.
+__device__ __forceinline__ double block_sum(double v, double* sh /* >= 33 doubles */) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double t = lane < nw ? sh[lane] : 0.0;
+        t = warp_sum(t);
+        if (lane == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+// ------------------------------------------------------------ grid barrier
+// Barrier over all blocks of a cooperative launch (all blocks co-resident).  The wait is
+// bounded: after `limit` polls it records DEV_TIMEOUT in *err and returns, and callers
+// check *err after every barrier, so no block waits forever.
+struct GridBarrier {
+    unsigned int* count;  // zero-initialised
+    unsigned int* gen;
+    int* err;
+};
+
+__device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = b.gen;
+        const unsigned int g = *vgen;
+        __threadfence();
+        if (atomicAdd(b.count, 1u) == nblocks - 1) {
+            *b.count = 0;
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        } else {
+            long long polls = 0;
+            while (*vgen == g) {
+                if (++polls > (1ll << 26)) {  // ~ seconds
+                    atomicExch(b.err, (int)DEV_TIMEOUT);
+                    break;
+                }
+                if (*(volatile int*)b.err != 0) break;
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)b.err == 0;
+}
+
+}  // namespace pf2

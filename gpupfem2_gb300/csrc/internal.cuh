@@ -1,0 +1,46 @@
+// internal.cuh - entry points shared between the translation units of the engine.
+#pragma once
+
+#include "common.cuh"
+
+namespace pf2 {
+
+struct FlowCoef {
+    double rho, mu, dt;
+};
+
+pf2_status launch_prediction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* ux, const double* uy,
+                             const double* uxo, const double* uyo, const double* pold, double* valx, double* valy,
+                             double* rhsx, double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st);
+pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+                           const double* pold, double* val, double* rhs, const pf2_bc* bc, cudaStream_t st);
+pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+                             const double* pres, const double* pold, double* valx, double* valy, double* rhsx,
+                             double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st);
+pf2_status launch_prediction_bc(const pf2_mesh* m, const FlowCoef& P, const pf2_bc* src, pf2_bc* dst,
+                                const double* pres, const double* pold, int comp, cudaStream_t st);
+pf2_status launch_body_loads(const pf2_mesh* m, const FlowCoef& P, int body_id, double thickness, double umean,
+                             double cx, double cy, const double* ux, const double* uy, const double* pres,
+                             double* out_dev, cudaStream_t st);
+
+pf2_status particles_advect(pf2_particles* H, const double* ux, const double* uy, double dt, int substeps,
+                            cudaStream_t st);
+pf2_status particles_project(pf2_particles* H, double* ux, double* uy, double* uxo, double* uyo, cudaStream_t st);
+pf2_status particles_correct(pf2_particles* H, const double* ux, const double* uy, const double* uxo,
+                             const double* uyo, cudaStream_t st);
+pf2_status particles_seed(pf2_particles* H, cudaStream_t st);
+pf2_status particles_status(pf2_particles* H, cudaStream_t st);
+const int* particles_count_ptr(const pf2_particles* H);
+
+// Device-side record of one solve: copies of the solver's result and error word.
+struct SolveRecord {
+    int iterations;
+    int converged;
+    double residual;
+    int status;
+    int err;
+};
+pf2_status solver_solve_async(pf2_solver* s, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
+                              cudaStream_t st);
+
+}  // namespace pf2

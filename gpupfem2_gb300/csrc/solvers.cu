@@ -1,0 +1,790 @@
+// solvers.cu - CSR SpMV, preconditioned CG and GMRES, Jacobi / ILU(0) / IC(0).
+//
+// Reference: src/linear_algebra/linear_solver.cu (CG :301-376, GMRES :378-521),
+// preconditioners.cu (Jacobi :3-46, ILU(0) :48-134, IC(0) :136-213), linear_algebra.h
+// (cuSPARSE SpMV, csrilu02/csric02, SpSV; cuBLAS dot/nrm2/trsv/gemv).
+//
+// Each solve is one cooperative launch: every iteration, its dot products and its
+// convergence test run on the device, with bounded grid barriers between phases, so
+// the host never waits inside a solve (the reference copies the residual to the host
+// every iteration).  Reductions are summed in a fixed order: repeated solves give
+// identical bits.  The ILU(0)/IC(0) factorisation and triangular solves walk the rows
+// in level order; a row waits (bounded) until the rows it depends on are done.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "device.cuh"
+#include "internal.cuh"
+
+namespace pf2 {
+
+constexpr int kSolverThreads = 256;
+constexpr int kGroup = 8;  // lanes per row in SpMV
+constexpr int kMaxGmresSmem = 1024;
+
+struct Csr {
+    int n;
+    const int* rowptr;
+    const int* col;
+    const double* val;
+    const int* diag;  // position of a_ii
+};
+
+// y_i = sum_k a_ik x_k for the rows a group of kGroup lanes handles; x may be written
+// by other blocks during the kernel, so it is read through L2.
+__device__ __forceinline__ double row_times(const Csr& A, int row, const double* x, int lane) {
+    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
+    double sum = 0.0;
+    for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&A.val[k]) * __ldcg(&x[__ldg(&A.col[k])]);
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    return sum;
+}
+
+__global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__ y) {
+    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+    const int lane = threadIdx.x % kGroup;
+    const int ngroups = gridDim.x * blockDim.x / kGroup;
+    for (int row = gid; row < A.n; row += ngroups) {
+        const double v = row_times(A, row, x, lane);
+        if (lane == 0) y[row] = v;
+    }
+}
+
+// ------------------------------------------------------------ triangular data
+struct Tri {
+    int kind;              // PF2_PRECOND_ILU or PF2_PRECOND_IC
+    const int* fwd_order;  // rows in forward level order
+    const int* bwd_order;  // rows in backward level order
+    const int* lt_off;     // IC: rows of L^T (strictly upper), (row k, position of l_ki)
+    const int* lt_row;
+    const int* lt_pos;
+    double* fact;          // factor values on the CSR pattern
+    double* tmp;           // forward result
+    int* done_f;           // per-row epoch flags
+    int* done_b;
+    unsigned* tickets;     // one counter per (apply, direction)
+};
+
+__device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err) {
+    long long polls = 0;
+    while (*(volatile const int*)flag != epoch) {
+        if (++polls > (1ll << 24)) {
+            atomicExch(err, (int)DEV_TIMEOUT);
+            return false;
+        }
+        if (*(volatile int*)err != 0) return false;
+    }
+    __threadfence();
+    return true;
+}
+
+// Sync-free triangular solve: warps take rows in level order from a shared ticket
+// counter, so every row a warp waits on was taken earlier by a running warp.
+// dir 0: forward  y = L^{-1} src (unit diagonal for ILU, l_ii for IC)
+// dir 1: backward dst = U^{-1} y (ILU) or L^{-T} y (IC)
+__device__ void tri_solve(const Csr& A, const Tri& T, int dir, const double* src, double* dst, unsigned* ticket,
+                          int epoch, int* err) {
+    const int lane = threadIdx.x & 31;
+    int* done = dir == 0 ? T.done_f : T.done_b;
+    const int* order = dir == 0 ? T.fwd_order : T.bwd_order;
+    while (true) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= (unsigned)A.n) break;
+        const int i = order[t];
+        double sum = 0.0;
+        bool ok = true;
+        if (dir == 0) {
+            const int s = A.rowptr[i], d = A.diag[i];
+            for (int k = s + lane; k < d; k += 32) {
+                const int j = A.col[k];
+                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
+                sum += __ldcg(&T.fact[k]) * __ldcg(&dst[j]);
+            }
+        } else if (T.kind == PF2_PRECOND_ILU) {
+            const int d = A.diag[i], e = A.rowptr[i + 1];
+            for (int k = d + 1 + lane; k < e; k += 32) {
+                const int j = A.col[k];
+                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
+                sum += __ldcg(&T.fact[k]) * __ldcg(&dst[j]);
+            }
+        } else {
+            const int s = T.lt_off[i], e = T.lt_off[i + 1];
+            for (int k = s + lane; k < e; k += 32) {
+                const int j = T.lt_row[k];
+                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
+                sum += __ldcg(&T.fact[T.lt_pos[k]]) * __ldcg(&dst[j]);
+            }
+        }
+        sum = warp_sum(sum);
+        if (!__all_sync(0xffffffffu, ok)) return;
+        if (lane == 0) {
+            const double in = __ldcg(&src[i]);
+            double v = in - sum;
+            if (dir == 1 || T.kind == PF2_PRECOND_IC) v = v / __ldcg(&T.fact[A.diag[i]]);
+            __stcg(&dst[i], v);
+            __threadfence();
+            atomicExch(&done[i], epoch);
+        }
+    }
+}
+
+// Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
+// per warp in level order, lane 0 working through the row.
+__global__ void k_factor(Csr A, Tri T, const int* __restrict__ order, unsigned* ticket, int epoch, int* err) {
+    const int lane = threadIdx.x & 31;
+    double* a = T.fact;
+    while (true) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= (unsigned)A.n) break;
+        if (lane != 0) continue;
+        const int i = order[t];
+        const int s = A.rowptr[i], d = A.diag[i], e = A.rowptr[i + 1];
+        bool ok = true;
+        if (T.kind == PF2_PRECOND_ILU) {
+            for (int kk = s; kk < d && ok; ++kk) {
+                const int k = A.col[kk];
+                if (!wait_flag(&T.done_f[k], epoch, err)) { ok = false; break; }
+                const double aik = __ldcg(&a[kk]) / __ldcg(&a[A.diag[k]]);
+                __stcg(&a[kk], aik);
+                const int ks = A.diag[k] + 1, ke = A.rowptr[k + 1];
+                int q = ks;
+                for (int jj = kk + 1; jj < e; ++jj) {
+                    const int j = A.col[jj];
+                    while (q < ke && A.col[q] < j) ++q;
+                    if (q < ke && A.col[q] == j) __stcg(&a[jj], __ldcg(&a[jj]) - aik * __ldcg(&a[q]));
+                }
+            }
+        } else {
+            for (int kk = s; kk < d && ok; ++kk) {
+                const int k = A.col[kk];
+                if (!wait_flag(&T.done_f[k], epoch, err)) { ok = false; break; }
+                double sum = __ldcg(&a[kk]);
+                int p = s, q = A.rowptr[k];
+                const int qe = A.diag[k];
+                while (p < kk && q < qe) {
+                    const int cp = A.col[p], cq = A.col[q];
+                    if (cp == cq) { sum -= __ldcg(&a[p]) * __ldcg(&a[q]); ++p; ++q; }
+                    else if (cp < cq) ++p;
+                    else ++q;
+                }
+                __stcg(&a[kk], sum / __ldcg(&a[A.diag[k]]));
+            }
+            if (ok) {
+                double dd = __ldcg(&a[d]);
+                for (int kk = s; kk < d; ++kk) { const double l = __ldcg(&a[kk]); dd -= l * l; }
+                __stcg(&a[d], sqrt(dd));
+            }
+        }
+        if (!ok) return;
+        __threadfence();
+        atomicExch(&T.done_f[i], epoch);
+    }
+}
+
+// ----------------------------------------------------------------- CG / GMRES
+struct SolveOut {
+    int iterations;
+    int converged;
+    double residual;
+    int status;
+    int pad;
+};
+
+struct KArgs {
+    Csr A;
+    int precond;
+    double* x;
+    const double* b;
+    double *r, *z, *p, *q, *invd;
+    double* partial;  // 4 arrays of gridDim doubles
+    GridBarrier bar;
+    Tri T;
+    int epoch_base;
+    double tol;
+    int maxit;
+    int criterion;
+    SolveOut* out;
+    // GMRES
+    double* V;      // (m+1) x n
+    double* H;      // m x m, column-major
+    int m;          // Krylov dimension
+};
+
+__device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
+    const int chunk = (n + gridDim.x - 1) / gridDim.x;
+    r0 = min(n, (int)blockIdx.x * chunk);
+    r1 = min(n, r0 + chunk);
+}
+
+// Fixed-order grid sum of per-block partials `part` (already written) after a barrier.
+__device__ __forceinline__ double grid_total(const double* part, double* sh) {
+    double v = 0.0;
+    if (threadIdx.x < 32) {
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += 32) v += __ldcg(&part[k]);
+        v = warp_sum(v);
+        if (threadIdx.x == 0) sh[32] = v;
+    }
+    __syncthreads();
+    v = sh[32];
+    __syncthreads();
+    return v;
+}
+
+// Preconditioner apply z = M^{-1} r over the rows of this block (Jacobi) or the whole
+// grid (ILU/IC; includes grid barriers).  `apply` counts the applies of this solve.
+__device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply) {
+    if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
+        const int ep = a.epoch_base + 2 * apply;
+        tri_solve(a.A, a.T, 0, src, a.T.tmp, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return false;
+        tri_solve(a.A, a.T, 1, a.T.tmp, dst, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        return grid_sync(a.bar, gridDim.x);
+    }
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        dst[i] = (a.precond == PF2_PRECOND_JACOBI) ? src[i] * a.invd[i] : src[i];
+    return true;
+}
+
+// SolverCG::solve (linear_solver.cu:440-515).
+__global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
+    __shared__ double sh[40];
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    double* P0 = a.partial;
+    double* P1 = a.partial + gridDim.x;
+    double* P2 = a.partial + 2 * gridDim.x;
+    const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
+    // Jacobi: inverse diagonal (PreconditionerJacobi::initialize, preconditioners.cu:3-14)
+    if (a.precond == PF2_PRECOND_JACOBI)
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
+    // r = b - A x
+    for (int i = r0 + grp; i < r1; i += ngrp) {
+        const double v = row_times(a.A, i, a.x, lane);
+        if (lane == 0) a.r[i] = a.b[i] - v;
+    }
+    __syncthreads();
+    int apply = 0;
+    if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+    if (!precond_apply(a, a.r, a.z, r0, r1, apply++)) return;
+    __syncthreads();
+    double g = 0.0, bb = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double zi = __ldcg(&a.z[i]);
+        a.p[i] = zi;
+        g += a.r[i] * zi;
+        bb += a.b[i] * a.b[i];
+    }
+    g = block_sum(g, sh);
+    bb = block_sum(bb, sh);
+    if (threadIdx.x == 0) { P0[blockIdx.x] = g; P2[blockIdx.x] = bb; }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    double gamma = grid_total(P0, sh);
+    const double bnorm = sqrt(grid_total(P2, sh));
+    const double tol2 = a.tol * a.tol;
+    auto done_test = [&](double gm, double rr) {
+        return a.criterion == PF2_CRITERION_ABS ? (gm < tol2) : (sqrt(rr) <= a.tol * bnorm);
+    };
+    double rr = 0.0;
+    if (a.criterion == PF2_CRITERION_REL) {
+        double t = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) t += a.r[i] * a.r[i];
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) P1[blockIdx.x] = t;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        rr = grid_total(P1, sh);
+    }
+    int it = 0;
+    bool conv = done_test(gamma, rr);
+    while (!conv && it < a.maxit) {
+        ++it;
+        double pq = 0.0;
+        for (int i = r0 + grp; i < r1; i += ngrp) {
+            const double v = row_times(a.A, i, a.p, lane);
+            if (lane == 0) { a.q[i] = v; pq += a.p[i] * v; }
+        }
+        pq = block_sum(pq, sh);
+        if (threadIdx.x == 0) P1[blockIdx.x] = pq;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        pq = grid_total(P1, sh);
+        const double alpha = gamma / pq;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            a.x[i] += alpha * a.p[i];
+            a.r[i] -= alpha * a.q[i];
+        }
+        __syncthreads();
+        if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+        if (!precond_apply(a, a.r, a.z, r0, r1, apply++)) return;
+        __syncthreads();
+        double gn = 0.0, rn = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            gn += a.r[i] * __ldcg(&a.z[i]);
+            if (a.criterion == PF2_CRITERION_REL) rn += a.r[i] * a.r[i];
+        }
+        gn = block_sum(gn, sh);
+        if (a.criterion == PF2_CRITERION_REL) rn = block_sum(rn, sh);
+        if (threadIdx.x == 0) { P0[blockIdx.x] = gn; P2[blockIdx.x] = rn; }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        const double gnew = grid_total(P0, sh);
+        if (a.criterion == PF2_CRITERION_REL) rr = grid_total(P2, sh);
+        if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
+        const double beta = gnew / gamma;
+        gamma = gnew;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = __ldcg(&a.z[i]) + beta * a.p[i];
+        if (!grid_sync(a.bar, gridDim.x)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = a.criterion == PF2_CRITERION_ABS ? sqrt(gamma) : sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+// SolverGMRES::solve (linear_solver.cu:560-660): left-preconditioned GMRES, the
+// projections taken one after another on the updated vector, Givens rotations
+// (updateHcolumn :40-66), stop on |beta_k| < tol; x changes only on convergence.  With
+// m < maxit the Krylov space restarts every m iterations.
+__global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
+    __shared__ double sh[40];
+    __shared__ double cs[kMaxGmresSmem], sn[kMaxGmresSmem], beta[kMaxGmresSmem + 1], hcol[kMaxGmresSmem + 1];
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    const int n = a.A.n;
+    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    double* P0 = a.partial;
+    double* P1 = a.partial + gridDim.x;
+    const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
+    if (a.precond == PF2_PRECOND_JACOBI)
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
+    int apply = 0, total_it = 0;
+    bool conv = false;
+    double res = 0.0;
+    const int m = a.m;
+    while (true) {
+        // v0 = M^{-1}(b - A x), beta0 = ||v0||
+        double* v0 = a.V;
+        for (int i = r0 + grp; i < r1; i += ngrp) {
+            const double v = row_times(a.A, i, a.x, lane);
+            if (lane == 0) a.r[i] = a.b[i] - v;
+        }
+        __syncthreads();
+        if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+        if (!precond_apply(a, a.r, v0, r0, r1, apply++)) return;
+        __syncthreads();
+        double s2 = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double vi = __ldcg(&v0[i]);
+            s2 += vi * vi;
+        }
+        s2 = block_sum(s2, sh);
+        if (threadIdx.x == 0) P0[blockIdx.x] = s2;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        const double b0 = sqrt(grid_total(P0, sh));
+        res = b0;
+        if (b0 < a.tol) { conv = true; break; }
+        if (total_it >= a.maxit) break;
+        if (threadIdx.x == 0) beta[0] = b0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) v0[i] = __ldcg(&v0[i]) / b0;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        int k = 0;
+        bool inner_conv = false;
+        while (k < m && total_it < a.maxit) {
+            ++total_it;
+            double* vk = a.V + (size_t)k * n;
+            double* vkp = a.V + (size_t)(k + 1) * n;
+            for (int i = r0 + grp; i < r1; i += ngrp) {
+                const double v = row_times(a.A, i, vk, lane);
+                if (lane == 0) a.q[i] = v;
+            }
+            __syncthreads();
+            if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+            if (!precond_apply(a, a.q, vkp, r0, r1, apply++)) return;
+            __syncthreads();
+            // h_ik = v_{k+1} . v_i, then v_{k+1} -= h_ik v_i, i = 0..k
+            for (int i = 0; i <= k; ++i) {
+                const double* vi = a.V + (size_t)i * n;
+                double d = 0.0;
+                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) d += __ldcg(&vkp[j]) * vi[j];
+                d = block_sum(d, sh);
+                double* P = (i & 1) ? P1 : P0;
+                if (threadIdx.x == 0) P[blockIdx.x] = d;
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                const double h = grid_total(P, sh);
+                if (threadIdx.x == 0) hcol[i] = h;
+                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) - h * vi[j];
+                __syncthreads();
+            }
+            double nn = 0.0;
+            for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) {
+                const double v = __ldcg(&vkp[j]);
+                nn += v * v;
+            }
+            nn = block_sum(nn, sh);
+            double* P = ((k + 1) & 1) ? P1 : P0;
+            if (threadIdx.x == 0) P[blockIdx.x] = nn;
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            const double aux = sqrt(grid_total(P, sh));
+            for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) / aux;
+            if (threadIdx.x == 0) {
+                double* h = hcol;
+                for (int i = 0; i < k; ++i) {
+                    const double tmp = cs[i] * h[i] + sn[i] * h[i + 1];
+                    h[i + 1] = -sn[i] * h[i] + cs[i] * h[i + 1];
+                    h[i] = tmp;
+                }
+                const double coeff = rsqrt(h[k] * h[k] + aux * aux);
+                cs[k] = h[k] * coeff;
+                sn[k] = aux * coeff;
+                h[k] = cs[k] * h[k] + sn[k] * aux;
+                beta[k + 1] = -sn[k] * beta[k];
+                beta[k] *= cs[k];
+                if (blockIdx.x == 0)
+                    for (int i = 0; i <= k; ++i) a.H[(size_t)m * k + i] = h[i];
+            }
+            __syncthreads();
+            res = fabs(beta[k + 1]);
+            ++k;
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            if (res < a.tol) { inner_conv = true; break; }
+        }
+        // y = H^{-1} beta (upper triangular), x += V y (own rows)
+        if (threadIdx.x == 0) {
+            for (int i = k - 1; i >= 0; --i) {
+                double s = beta[i];
+                for (int j = i + 1; j < k; ++j) s -= __ldcg(&a.H[i + (size_t)m * j]) * hcol[j];
+                hcol[i] = s / __ldcg(&a.H[i + (size_t)m * i]);
+            }
+        }
+        __syncthreads();
+        const bool update = inner_conv || (k == m && m < a.maxit);
+        if (update)
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                double s = 0.0;
+                for (int j = 0; j < k; ++j) s += __ldcg(&a.V[(size_t)j * n + i]) * hcol[j];
+                a.x[i] = s + a.x[i];
+            }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        if (inner_conv) { conv = true; break; }
+        if (!update || total_it >= a.maxit) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = total_it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = res;
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+__global__ void k_precond_apply(KArgs a) {
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    precond_apply(a, a.r, a.z, r0, r1, 0);
+}
+
+}  // namespace pf2
+
+using namespace pf2;
+
+struct pf2_solver {
+    pf2_solver_options opt{};
+    const pf2_mesh* mesh = nullptr;
+    int n = 0, nnz = 0, blocks = 0, m = 0;
+    DevBuf<double> r, z, p, q, invd, partial, V, H;
+    DevBuf<unsigned> bar;  // count, gen
+    DevBuf<int> err;
+    DevBuf<SolveOut> out;
+    PinnedBuf<SolveOut> h_out;
+    // ILU / IC
+    DevBuf<double> fact, tmp;
+    DevBuf<int> fwd_order, bwd_order, lt_off, lt_row, lt_pos, done_f, done_b;
+    DevBuf<unsigned> tickets;
+    int epoch = 0;
+    bool factored = false;
+    const pf2_csr* last = nullptr;  // matrix of the last setup / solve
+};
+
+static pf2_status build_tri_plan(pf2_solver* S) {
+    const pf2_mesh* M = S->mesh;
+    const int n = M->nv, nnz = M->nnz;
+    std::vector<int> rp(n + 1), col(nnz), dg(n);
+    PF2_CUDA(cudaMemcpy(rp.data(), M->rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    PF2_CUDA(cudaMemcpy(col.data(), M->col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    PF2_CUDA(cudaMemcpy(dg.data(), M->diag.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    // forward levels: 1 + max over the strictly lower entries
+    std::vector<int> lev(n, 0);
+    int nl = 0;
+    for (int i = 0; i < n; ++i) {
+        int l = 0;
+        for (int k = rp[i]; k < dg[i]; ++k) l = std::max(l, lev[col[k]] + 1);
+        lev[i] = l;
+        nl = std::max(nl, l + 1);
+    }
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
+    PF2_TRY(S->fwd_order.alloc(n));
+    PF2_CUDA(cudaMemcpy(S->fwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    // backward levels: 1 + max over the strictly upper entries (the pattern is symmetric)
+    std::fill(lev.begin(), lev.end(), 0);
+    for (int i = n - 1; i >= 0; --i) {
+        int l = 0;
+        for (int k = dg[i] + 1; k < rp[i + 1]; ++k) l = std::max(l, lev[col[k]] + 1);
+        lev[i] = l;
+    }
+    for (int i = 0; i < n; ++i) order[i] = n - 1 - i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
+    PF2_TRY(S->bwd_order.alloc(n));
+    PF2_CUDA(cudaMemcpy(S->bwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    // rows of L^T: for each k, entries l_ki with i > k ... stored as (row i, position)
+    std::vector<int> off(n + 1, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = rp[i]; k < dg[i]; ++k) off[col[k] + 1]++;
+    for (int i = 0; i < n; ++i) off[i + 1] += off[i];
+    std::vector<int> lrow(std::max(off[n], 1)), lpos(std::max(off[n], 1)), fill(off.begin(), off.end() - 1);
+    for (int i = 0; i < n; ++i)
+        for (int k = rp[i]; k < dg[i]; ++k) {
+            const int c = col[k];
+            lrow[fill[c]] = i;
+            lpos[fill[c]] = k;
+            fill[c]++;
+        }
+    PF2_TRY(S->lt_off.alloc(n + 1));
+    PF2_TRY(S->lt_row.alloc(lrow.size()));
+    PF2_TRY(S->lt_pos.alloc(lpos.size()));
+    PF2_CUDA(cudaMemcpy(S->lt_off.p, off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    PF2_CUDA(cudaMemcpy(S->lt_row.p, lrow.data(), sizeof(int) * lrow.size(), cudaMemcpyHostToDevice));
+    PF2_CUDA(cudaMemcpy(S->lt_pos.p, lpos.data(), sizeof(int) * lpos.size(), cudaMemcpyHostToDevice));
+    PF2_TRY(S->fact.alloc(nnz));
+    PF2_TRY(S->tmp.alloc(n));
+    PF2_TRY(S->done_f.alloc(n));
+    PF2_TRY(S->done_b.alloc(n));
+    PF2_CUDA(cudaMemset(S->done_f.p, 0, sizeof(int) * n));
+    PF2_CUDA(cudaMemset(S->done_b.p, 0, sizeof(int) * n));
+    return PF2_OK;
+}
+
+static Csr csr_of(const pf2_csr* A) {
+    return Csr{ A->n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, A->mesh->diag.p };
+}
+
+static Tri tri_of(pf2_solver* S) {
+    return Tri{ S->opt.precond, S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p,
+                S->fact.p, S->tmp.p, S->done_f.p, S->done_b.p, S->tickets.p };
+}
+
+static bool uses_tri(const pf2_solver* S) {
+    return S->opt.precond == PF2_PRECOND_ILU || S->opt.precond == PF2_PRECOND_IC;
+}
+
+// Preconditioner::initialize(A): ILU/IC factorise a copy of A's values.
+__global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __restrict__ diag, double* invd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) invd[i] = 1.0 / val[diag[i]];
+}
+
+static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
+    S->last = A;
+    if (S->opt.precond == PF2_PRECOND_JACOBI) {
+        k_inv_diag<<<blocks_for(S->n), kThreads, 0, st>>>(S->n, A->val.p, A->mesh->diag.p, S->invd.p);
+        PF2_LAUNCH_CHECK();
+        return PF2_OK;
+    }
+    if (!uses_tri(S)) return PF2_OK;
+    PF2_CUDA(cudaMemcpyAsync(S->fact.p, A->val.p, sizeof(double) * S->nnz, cudaMemcpyDeviceToDevice, st));
+    PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned), st));
+    S->epoch += 1;
+    Tri T = tri_of(S);
+    const int nb = std::min(num_sms() * 8, (int)blocks_for(S->n, kSolverThreads / 32));
+    k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(csr_of(A), T, S->fwd_order.p, S->tickets.p, S->epoch,
+                                                          S->err.p);
+    PF2_LAUNCH_CHECK();
+    S->factored = true;
+    return PF2_OK;
+}
+
+static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, const double* b, cudaStream_t st,
+                                bool precond_only = false) {
+    KArgs a{};
+    a.A = csr_of(A ? A : S->last);
+    a.precond = S->opt.precond;
+    a.x = x;
+    a.b = b;
+    a.r = S->r.p;
+    a.z = S->z.p;
+    a.p = S->p.p;
+    a.q = S->q.p;
+    a.invd = S->invd.p;
+    a.partial = S->partial.p;
+    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p };
+    a.T = tri_of(S);
+    a.tol = S->opt.tolerance;
+    a.maxit = S->opt.max_iterations;
+    a.criterion = S->opt.criterion;
+    a.out = S->out.p;
+    a.V = S->V.p;
+    a.H = S->H.p;
+    a.m = S->m;
+    const int applies = (S->opt.kind == PF2_SOLVER_GMRES) ? (S->opt.max_iterations + 2 * (S->opt.max_iterations / std::max(S->m, 1)) + 4)
+                                                           : (S->opt.max_iterations + 2);
+    if (uses_tri(S)) {
+        PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
+        a.epoch_base = S->epoch;
+        S->epoch += 2 * applies + 2;
+    }
+    PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
+    PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
+    void* args[] = { &a };
+    if (precond_only) {
+        PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, st);
+        return PF2_OK;
+    }
+    void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (void*)k_pcg;
+    PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, st);
+    (void)applies;
+    return PF2_OK;
+}
+
+extern "C" {
+
+pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf2_solver** out) {
+    PF2_REQUIRE(A && opt && out, PF2_BAD_INPUT, "null argument");
+    *out = nullptr;
+    PF2_REQUIRE(opt->kind == PF2_SOLVER_CG || opt->kind == PF2_SOLVER_GMRES, PF2_BAD_INPUT, "unknown solver kind %d",
+                opt->kind);
+    PF2_REQUIRE(opt->precond >= PF2_PRECOND_NONE && opt->precond <= PF2_PRECOND_IC, PF2_BAD_INPUT,
+                "unknown preconditioner %d", opt->precond);
+    PF2_REQUIRE(opt->max_iterations >= 0 && opt->tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
+    PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
+                PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
+    PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64, PF2_BAD_INPUT, "mixed precision is built by pf2_solver_create_mixed");
+    pf2_solver* S = new pf2_solver();
+    S->opt = *opt;
+    S->mesh = A->mesh;
+    S->n = A->n;
+    S->nnz = A->nnz;
+    auto fail = [&](pf2_status s) { delete S; return s; };
+    // SolverGMRES::init clamps the iteration limit to the matrix size (linear_solver.cu:396-399)
+    if (opt->kind == PF2_SOLVER_GMRES && S->opt.max_iterations > S->n) S->opt.max_iterations = S->n;
+    int occ = 0;
+    void* fn = (opt->kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (void*)k_pcg;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolverThreads, 0) != cudaSuccess || occ < 1)
+        return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
+    const int maxb = occ * num_sms();
+    // at least ~512 rows per block keeps the barrier count per unit of work low
+    S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
+    pf2_status s;
+    if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
+        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
+        (s = S->err.alloc(1)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
+        return fail(s);
+    if (opt->kind == PF2_SOLVER_GMRES) {
+        int m = opt->restart > 0 ? opt->restart : S->opt.max_iterations;
+        m = std::max(1, std::min(m, std::min(S->opt.max_iterations, kMaxGmresSmem - 1)));
+        S->m = m;
+        if ((s = S->V.alloc((size_t)(m + 1) * S->n)) || (s = S->H.alloc((size_t)m * m))) return fail(s);
+    }
+    if (uses_tri(S)) {
+        if ((s = build_tri_plan(S))) return fail(s);
+        const int applies = S->opt.max_iterations + 2 * (S->opt.max_iterations / std::max(S->m, 1)) + 4;
+        if ((s = S->tickets.alloc(2 * (size_t)applies + 2))) return fail(s);
+    }
+    *out = S;
+    return PF2_OK;
+}
+
+pf2_status pf2_solver_destroy(pf2_solver* s) {
+    delete s;
+    return PF2_OK;
+}
+
+pf2_status pf2_solver_setup(pf2_solver* S, const pf2_csr* A, void* stream) {
+    PF2_REQUIRE(S && A, PF2_BAD_INPUT, "null argument");
+    PF2_REQUIRE(A->mesh == S->mesh, PF2_BAD_INPUT, "matrix pattern differs from the solver's");
+    return factorize(S, A, as_stream(stream));
+}
+
+}  // extern "C"
+
+namespace pf2 {
+
+__global__ void k_record(const SolveOut* out, const int* err, SolveRecord* rec) {
+    rec->iterations = out->iterations;
+    rec->converged = out->converged;
+    rec->residual = out->residual;
+    rec->status = out->status;
+    rec->err = *err;
+}
+
+pf2_status solver_solve_async(pf2_solver* S, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
+                              cudaStream_t st) {
+    PF2_TRY(factorize(S, A, st));
+    PF2_TRY(launch_solver(S, A, x, b, st));
+    if (rec) {
+        k_record<<<1, 1, 0, st>>>(S->out.p, S->err.p, rec);
+        PF2_LAUNCH_CHECK();
+    }
+    return PF2_OK;
+}
+
+}  // namespace pf2
+
+extern "C" {
+
+pf2_status pf2_solver_solve(pf2_solver* S, const pf2_csr* A, double* x, const double* b, pf2_solve_info* info,
+                            void* stream) {
+    PF2_REQUIRE(S && A && x && b, PF2_BAD_INPUT, "null argument");
+    PF2_REQUIRE(A->mesh == S->mesh, PF2_BAD_INPUT, "matrix pattern differs from the solver's");
+    cudaStream_t st = as_stream(stream);
+    PF2_TRY(factorize(S, A, st));
+    PF2_TRY(launch_solver(S, A, x, b, st));
+    if (!info) return PF2_OK;
+    int err = 0;
+    PF2_CUDA(cudaMemcpyAsync(S->h_out.p, S->out.p, sizeof(SolveOut), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(&err, S->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaStreamSynchronize(st));
+    info->iterations = S->h_out.p->iterations;
+    info->converged = S->h_out.p->converged;
+    info->residual = S->h_out.p->residual;
+    info->outer_iterations = 1;
+    info->status = err ? err : S->h_out.p->status;
+    PF2_REQUIRE(err == 0, (pf2_status)err, "device-side wait timed out in the solver");
+    if (!info->converged) {
+        set_error("solver did not converge in %d iterations (residual %g)", info->iterations, info->residual);
+        return PF2_NOT_CONVERGED;
+    }
+    return PF2_OK;
+}
+
+pf2_status pf2_precond_apply(pf2_solver* S, double* dst, const double* src, void* stream) {
+    PF2_REQUIRE(S && dst && src, PF2_BAD_INPUT, "null argument");
+    cudaStream_t st = as_stream(stream);
+    if (S->opt.precond == PF2_PRECOND_NONE) {
+        PF2_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * S->n, cudaMemcpyDeviceToDevice, st));
+        return PF2_OK;
+    }
+    PF2_REQUIRE(S->last && (S->factored || S->opt.precond == PF2_PRECOND_JACOBI), PF2_BAD_INPUT,
+                "preconditioner not initialised: call pf2_solver_setup or pf2_solver_solve first");
+    PF2_CUDA(cudaMemcpyAsync(S->r.p, src, sizeof(double) * S->n, cudaMemcpyDeviceToDevice, st));
+    PF2_TRY(launch_solver(S, nullptr, nullptr, nullptr, st, true));
+    PF2_CUDA(cudaMemcpyAsync(dst, S->z.p, sizeof(double) * S->n, cudaMemcpyDeviceToDevice, st));
+    return PF2_OK;
+}
+
+pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream) {
+    PF2_REQUIRE(A && x && y, PF2_BAD_INPUT, "null argument");
+    const int blocks = std::min((int)blocks_for((long long)A->n * kGroup), num_sms() * 16);
+    k_spmv<<<std::max(blocks, 1), kThreads, 0, as_stream(stream)>>>(csr_of(A), x, y);
+    PF2_LAUNCH_CHECK();
+    return PF2_OK;
+}
+
+}  // extern "C"

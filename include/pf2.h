@@ -1,0 +1,333 @@
+/*
+ * pf2.h - C ABI of the GB300-native PFEM-2 time-step engine.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and returns a
+ * pf2_status; none allocates or frees user memory.  Objects (mesh, CSR matrix,
+ * Dirichlet set, solver, particle set, flow engine) own their device memory; device
+ * pointers handed out by the *_view functions stay valid until the object is destroyed
+ * (particle arrays until the next call that changes the particle count).  `stream` is
+ * a cudaStream_t (NULL = the legacy default stream); work is enqueued on it and the
+ * call returns without waiting unless its comment says "synchronises".
+ *
+ * Each declaration names the reference interface it replaces (andreyypopov/gpuPfem2,
+ * paths relative to its source tree).  The reference reports failures by exit()
+ * (src/common/cuda_helper.cuh:32-94) or by a bool plus printf; here they come back as a
+ * status, and pf2_last_error() holds the message of the calling thread's last failure.
+ */
+#ifndef PF2_H
+#define PF2_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF2_ABI_VERSION 1
+
+typedef enum pf2_status {
+    PF2_OK = 0,
+    PF2_NOT_CONVERGED = 1, /* solver hit maxit (reference: solve() returns false) */
+    PF2_BAD_INPUT = 2,     /* invalid argument, mesh or size                      */
+    PF2_OVERFLOW = 3,      /* a fixed-capacity buffer (particles) would overflow  */
+    PF2_CUDA_ERROR = 4,    /* a CUDA runtime call failed                          */
+    PF2_TIMEOUT = 5,       /* a bounded device-side wait gave up                  */
+    PF2_IO_ERROR = 6       /* file could not be read                              */
+} pf2_status;
+
+typedef struct pf2_mesh pf2_mesh;
+typedef struct pf2_csr pf2_csr;
+typedef struct pf2_bc pf2_bc;
+typedef struct pf2_solver pf2_solver;
+typedef struct pf2_particles pf2_particles;
+typedef struct pf2_flow pf2_flow;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* pf2_last_error(void);
+const char* pf2_status_string(pf2_status s);
+int pf2_abi_version(void);
+/* Number of kernels the engine has launched in this process (diagnostics; no
+ * reference counterpart). */
+unsigned long long pf2_kernel_launches(void);
+
+/* ------------------------------------------------------------------ Mesh2D
+ * Replaces Mesh2D (src/mesh_2d.cuh:11-69). */
+
+/* Mesh2D::loadMeshFromFile(filename, fillNeighborLists, scale), src/mesh_2d.cu:36-96:
+ * SALOME DAT, triangles (type 203) kept, other entities skipped, 1-based ids.
+ * Builds cell areas and inverse Jacobians (mesh_2d.cu:10-34, :98-105), the
+ * vertex-sharing neighbour lists (mesh_2d.cu:107-139) when fill_neighbors != 0, and the
+ * node incidence and CSR pattern the assembly uses.  Synchronises. */
+pf2_status pf2_mesh_load_dat(const char* path, int fill_neighbors, double scale, void* stream, pf2_mesh** out);
+
+/* The same mesh from host arrays: xy[2*nv] (x,y pairs), tri[3*nc] (0-based). Synchronises. */
+pf2_status pf2_mesh_create(int nv, const double* xy, int nc, const int* tri, int fill_neighbors,
+                           void* stream, pf2_mesh** out);
+pf2_status pf2_mesh_destroy(pf2_mesh* mesh);
+pf2_status pf2_mesh_sizes(const pf2_mesh* mesh, int* nv, int* nc, int* n_neighbor_entries);
+
+/* Device arrays of the mesh (Mesh2D::getVertices/getCells/getCellArea/getInvJacobi/
+ * getCellNeighborsOffsets/getCellNeighborIndices/getEdgeBoundaryIDs, mesh_2d.cuh:18-44).
+ * xy: double2[nv]; tri: int[3*nc]; area: double[nc]; inv_jacobi: double[4*nc] row-major;
+ * neighbor_offsets: int[nc+1]; neighbor_indices: int[n]; edge_ids: int[3*nc]. */
+typedef struct pf2_mesh_view {
+    int nv, nc, n_neighbor_entries;
+    const double* xy;
+    const int* tri;
+    const double* area;
+    const double* inv_jacobi;
+    const int* neighbor_offsets;
+    const int* neighbor_indices;
+    const int* edge_boundary_ids;
+} pf2_mesh_view;
+pf2_status pf2_mesh_view_get(const pf2_mesh* mesh, pf2_mesh_view* out);
+
+enum { PF2_MESH_XY = 0, PF2_MESH_TRI = 1, PF2_MESH_AREA = 2, PF2_MESH_INV_JACOBI = 3,
+       PF2_MESH_NEIGHBOR_OFFSETS = 4, PF2_MESH_NEIGHBOR_INDICES = 5, PF2_MESH_EDGE_IDS = 6 };
+/* Copies one mesh array to host memory (sizes as in pf2_mesh_view). Synchronises. */
+pf2_status pf2_mesh_download(const pf2_mesh* mesh, int field, void* host_dst);
+
+/* kSetEdgeBoundaryIDs of the channel drivers (cases/Cylinder2D/main.cu:35-70): edge i of
+ * a cell (vertex i -> vertex (i+1)%3) gets 0 inlet x=0, 1 outlet x=lx, 2 walls y=0 or
+ * y=ly, 3 cylinder (|midpoint - c| - r| < 0.001 when has_cylinder), else -1. */
+pf2_status pf2_mesh_set_channel_boundary_ids(pf2_mesh* mesh, double lx, double ly, int has_cylinder,
+                                             double cx, double cy, double r, void* stream);
+/* Edge boundary ids from host memory, int[3*nc]. */
+pf2_status pf2_mesh_set_edge_boundary_ids(pf2_mesh* mesh, const int* ids_host);
+
+/* --------------------------------------------------------- SparseMatrixCSR
+ * Replaces SparseMatrixCSR (src/linear_algebra/sparse_matrix.cuh:9-58). */
+
+/* SparseMatrixCSR(const Mesh2D&), sparse_matrix.cu:8-54: rows = nodes, columns =
+ * {i} U edge neighbours, ascending, int32 offsets/indices, double values (zeroed).  All
+ * matrices of one mesh share the mesh's pattern arrays. */
+pf2_status pf2_csr_create(const pf2_mesh* mesh, pf2_csr** out);
+pf2_status pf2_csr_destroy(pf2_csr* A);
+/* getRows(), getTotalElements() */
+pf2_status pf2_csr_sizes(const pf2_csr* A, int* rows, int* nnz);
+/* getRowOffset(), getColIndices(), getMatrixValues(): device pointers */
+pf2_status pf2_csr_view(const pf2_csr* A, const int** row_offsets, const int** col_indices, double** values);
+/* clearValues(), sparse_matrix.cuh:50-52 */
+pf2_status pf2_csr_clear_values(pf2_csr* A, void* stream);
+/* Copies pattern and/or values to host (NULL skips). Synchronises. */
+pf2_status pf2_csr_download(const pf2_csr* A, int* row_offsets, int* col_indices, double* values);
+pf2_status pf2_csr_upload_values(pf2_csr* A, const double* values_host);
+
+/* ------------------------------------------------------------ DirichletBCs
+ * Replaces DirichletBCs (src/Dirichlet_bcs.cuh:14-29).  pf2_dirichlet_node has the
+ * layout of the reference's DirichletNode {unsigned nodeIdx; double bcValue}. */
+typedef struct pf2_dirichlet_node {
+    unsigned int node;
+    double value;
+} pf2_dirichlet_node;
+
+/* setupDirichletBCs + setupNodeMap (Dirichlet_bcs.cu:53-71). */
+pf2_status pf2_bc_create(int n_nodes, int n_bc, const pf2_dirichlet_node* nodes_host, pf2_bc** out);
+pf2_status pf2_bc_destroy(pf2_bc* bc);
+pf2_status pf2_bc_size(const pf2_bc* bc, int* n_bc);
+/* Replaces the boundary values (device double[n_bc]). */
+pf2_status pf2_bc_set_values(pf2_bc* bc, const double* values_dev, void* stream);
+/* Copies the current boundary values to device memory double[n_bc]. */
+pf2_status pf2_bc_get_values(const pf2_bc* bc, double* values_dev, void* stream);
+/* DirichletBCs::applyBCs(matrix, rhs), Dirichlet_bcs.cu:73-86: boundary rows -> e_i with
+ * rhs g; other rows lose their boundary columns (rhs_r -= a_rd g_d), unless the row's
+ * first off-diagonal value, read before elimination, is below 2e-6 in magnitude. */
+pf2_status pf2_bc_apply(const pf2_bc* bc, pf2_csr* A, double* rhs_dev, void* stream);
+
+/* ------------------------------------------------------ Assembly (integrators)
+ * The reference's assembly entry points live in its case drivers; each function below
+ * assembles matrix values and rhs (overwriting them: clearValues + assemble), and with
+ * a non-NULL bc applies the Dirichlet rule of pf2_bc_apply in the same pass. */
+
+enum { PF2_RHS_GAUSSIAN = 0, /* exp(-(x^2+10y^2)), cases/Poisson2D/main.cu:24-26 */
+       PF2_RHS_SINSIN = 1 /* 2 pi^2 sin(pi x) sin(pi y) */ };
+
+/* PoissonIntegrator::assembleSystem, cases/Poisson2D/main.cu:28-85 (lambda = 0.5 in the
+ * shipped case): A_ij = lambda int grad N_i . grad N_j, b_i = int f N_i, 3-point rule. */
+pf2_status pf2_assemble_poisson(const pf2_mesh* mesh, pf2_csr* A, double* rhs_dev, int rhs_kind, double lambda,
+                                const pf2_bc* bc, void* stream);
+
+/* SimulationParameters, src/parameters.cuh:6-51 (the fields the step uses). */
+typedef struct pf2_params {
+    double rho, mu, dt, tolerance;
+    int max_iterations;
+    int scheme;            /* 0 = Scheme A, 1 = Scheme B (pressure increment) */
+    int substeps;          /* particleAdvectionSubsteps */
+    int level;             /* cellDivisionLevel: level^2 particles per cell, 1..4 */
+    int n_outer;           /* outer iterations of the step (2 in Cylinder2D, 1 in PoiseuilleFlow2D) */
+    int pressure_precond;  /* PF2_PRECOND_* for the pressure solve */
+    int calculate_loads, body_boundary_id;
+    double thickness, mean_velocity;
+    double body_cx, body_cy; /* body centre for the load normals (0.2, 0.2 in Cylinder2D/main.cu:344) */
+    int pressure_precision;  /* PF2_PRECISION_* for the pressure solve */
+    int pressure_x0;         /* PF2_X0_* for the pressure solve */
+    int gmres_restart;       /* Krylov dimension of the prediction GMRES, 0 = no restart */
+} pf2_params;
+/* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
+pf2_status pf2_params_default(pf2_params* p);
+
+/* kIntegrateVelocityPrediction (cases/Cylinder2D/main.cu:72-167): rho M + mu dt K_visc
+ * with the outlet edge term on boundary id 1; rhs from u_old, u and (Scheme B) p_old.
+ * ux/uy: current velocity, ux_old/uy_old: projected velocity, p_old may be NULL. */
+pf2_status pf2_assemble_velocity_prediction(const pf2_mesh* mesh, const pf2_params* p,
+                                            const double* ux, const double* uy,
+                                            const double* ux_old, const double* uy_old, const double* p_old,
+                                            pf2_csr* Ax, pf2_csr* Ay, double* rhs_x, double* rhs_y,
+                                            const pf2_bc* bc_x, const pf2_bc* bc_y, void* stream);
+/* kIntegratePressureEquation (:169-211). */
+pf2_status pf2_assemble_pressure(const pf2_mesh* mesh, const pf2_params* p, const double* pred_x,
+                                 const double* pred_y, const double* p_old, pf2_csr* A, double* rhs,
+                                 const pf2_bc* bc, void* stream);
+/* kIntegrateVelocityCorrection (:213-259). */
+pf2_status pf2_assemble_velocity_correction(const pf2_mesh* mesh, const pf2_params* p, const double* pred_x,
+                                            const double* pred_y, const double* pressure, const double* p_old,
+                                            pf2_csr* Ax, pf2_csr* Ay, double* rhs_x, double* rhs_y,
+                                            const pf2_bc* bc_x, const pf2_bc* bc_y, void* stream);
+/* VelocityDirichletBCs::setDirichletValues (:467-479, kernels :261-297): writes into
+ * `target` the values of `source` plus dt/rho * area-weighted pressure gradient
+ * (component 0/1) at each boundary node.  source and target share the node list. */
+pf2_status pf2_prediction_bc_values(const pf2_mesh* mesh, const pf2_params* p, const pf2_bc* source,
+                                    pf2_bc* target, const double* pressure, const double* p_old, int component,
+                                    void* stream);
+/* boundaryLoadsCalculator::calculateLoads (:414-428, kernels :299-376): drag and lift
+ * coefficients on the edges with body_boundary_id; cxcy_host[2]. The body centre is
+ * (cx, cy).  Synchronises. */
+pf2_status pf2_body_loads(const pf2_mesh* mesh, const pf2_params* p, double cx, double cy, const double* ux,
+                          const double* uy, const double* pressure, double* cxcy_host, void* stream);
+
+/* ---------------------------------------------------------------- Solvers
+ * Replaces LinearSolver/SolverCG/SolverGMRES (src/linear_algebra/linear_solver.cuh:15-137)
+ * and Preconditioner{Jacobi,ILU,IC} (src/linear_algebra/preconditioners.cuh:9-106). */
+enum { PF2_SOLVER_CG = 0, PF2_SOLVER_GMRES = 1 };
+enum { PF2_PRECOND_NONE = -1, PF2_PRECOND_JACOBI = 0, PF2_PRECOND_ILU = 1, PF2_PRECOND_IC = 2 };
+enum { PF2_CRITERION_ABS = 0,   /* CG: r^T z < tol^2; GMRES: |beta_k| < tol (the reference's) */
+       PF2_CRITERION_REL = 1 }; /* ||b - A x|| <= tol ||b|| */
+enum { PF2_PRECISION_FP64 = 0, PF2_PRECISION_MIXED = 1 };
+enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
+
+typedef struct pf2_solver_options {
+    int kind;          /* PF2_SOLVER_* */
+    int precond;       /* PF2_PRECOND_* */
+    double tolerance;
+    int max_iterations;
+    int criterion;     /* PF2_CRITERION_* */
+    int precision;     /* PF2_PRECISION_* (CG only) */
+    int restart;       /* GMRES Krylov dimension; 0 = max_iterations (no restart, as the reference) */
+} pf2_solver_options;
+
+typedef struct pf2_solve_info {
+    int iterations;      /* total inner iterations */
+    int converged;
+    double residual;     /* sqrt(r^T z) (CG, ABS), |beta| (GMRES), or ||r||/||b|| (REL) */
+    int outer_iterations; /* refinement sweeps (mixed precision) */
+    int status;          /* pf2_status of the device-side run */
+} pf2_solve_info;
+
+/* SolverCG/SolverGMRES(tol, maxIt, LA, precond) + init(A): allocates the work vectors
+ * for A's size (and the factor storage of ILU/IC). */
+pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf2_solver** out);
+pf2_status pf2_solver_destroy(pf2_solver* s);
+/* solve(A, x, b) -> bool: x (device, in/out: initial guess in, solution out), b device.
+ * Preconditioner::initialize(A) runs inside, as in the reference (ILU/IC factorise A).
+ * Returns PF2_NOT_CONVERGED when maxit is reached.  info may be NULL; when non-NULL the
+ * call synchronises to fill it. */
+pf2_status pf2_solver_solve(pf2_solver* s, const pf2_csr* A, double* x, const double* b, pf2_solve_info* info,
+                            void* stream);
+/* Preconditioner::applyPreconditioner(dest, src) with the factors of the last solve or
+ * pf2_solver_setup(). */
+pf2_status pf2_solver_setup(pf2_solver* s, const pf2_csr* A, void* stream);
+pf2_status pf2_precond_apply(pf2_solver* s, double* dst, const double* src, void* stream);
+
+/* y = A x (device vectors); the cusparseSpMV call of LinearAlgebra::sparseMV
+ * (src/linear_algebra/linear_algebra.h:56-80). */
+pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream);
+
+/* ------------------------------------------------------ ParticleHandler2D
+ * Replaces ParticleHandler2D (src/particles/particle_handler_2d.cuh:9-54).  Velocity
+ * fields are two device arrays (the reference passes a device array of two device
+ * pointers, deviceVector<double*>). */
+
+/* ParticleHandler2D(mesh, cellDivisionLevel): level clamped to [1,4]; capacity =
+ * capacity_factor * level^2 * nc particles (>= 1.1, the reference's resize margin). */
+pf2_status pf2_particles_create(const pf2_mesh* mesh, int level, double capacity_factor, pf2_particles** out);
+pf2_status pf2_particles_destroy(pf2_particles* ph);
+/* seedParticles(), particle_handler_2d.cu:304-320: level^2 particles per cell at the
+ * sub-triangle centroids, zero velocity, ordered by cell. */
+pf2_status pf2_particles_seed(pf2_particles* ph, void* stream);
+/* initParticleVelocity(u), :322-326 */
+pf2_status pf2_particles_init_velocity(pf2_particles* ph, const double* ux, const double* uy, void* stream);
+/* advectParticles(u, dt, substeps), :328-342: advection, cell location (own cell, then
+ * vertex-sharing neighbours in ascending order), deletion of particles not found, then
+ * the sub-cell population check and reseed.  Particles end up ordered by cell. */
+pf2_status pf2_particles_advect(pf2_particles* ph, const double* ux, const double* uy, double dt, int substeps,
+                                void* stream);
+/* correctParticleVelocity(u, u_old), :344-348 */
+pf2_status pf2_particles_correct(pf2_particles* ph, const double* ux, const double* uy, const double* ux_old,
+                                 const double* uy_old, void* stream);
+/* projectVelocityOntoGrid(u), :350-361: u_node = sum L_i v_p / sum L_i. */
+pf2_status pf2_particles_project(pf2_particles* ph, double* ux, double* uy, void* stream);
+/* getParticleCount(). Synchronises. */
+pf2_status pf2_particles_count(const pf2_particles* ph, int* count);
+/* getParticles(): copies the particle state to host arrays (NULL skips a field); l2 is
+ * the third barycentric coordinate; cell is the containing cell. Synchronises. */
+pf2_status pf2_particles_download(const pf2_particles* ph, double* x, double* y, double* l0, double* l1,
+                                  double* l2, double* u, double* v, int* cell);
+/* Replaces the particle state from host arrays (l2 taken as 1 - l0 - l1 unless it
+ * differs, in which case the particle keeps it until it is next located).  Particles
+ * are reordered by cell.  Synchronises. */
+pf2_status pf2_particles_upload(pf2_particles* ph, int n, const double* x, const double* y, const double* l0,
+                                const double* l1, const double* l2, const double* u, const double* v,
+                                const int* cell);
+
+/* ------------------------------------------------------------- Flow engine
+ * One PFEM-2 time step of the channel drivers (cases/Cylinder2D/main.cu:793-880): the
+ * state (particles, velocity, prediction, pressure, matrices, solvers) lives on the
+ * device; pf2_flow_step enqueues the whole step without host round trips. */
+pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p,
+                           int n_bc_x, const pf2_dirichlet_node* bc_x,
+                           int n_bc_y, const pf2_dirichlet_node* bc_y,
+                           int n_bc_p, const pf2_dirichlet_node* bc_p, double particle_capacity_factor,
+                           pf2_flow** out);
+pf2_status pf2_flow_destroy(pf2_flow* f);
+/* seedParticles + initParticleVelocity of the zero initial field. */
+pf2_status pf2_flow_seed(pf2_flow* f, void* stream);
+pf2_status pf2_flow_step(pf2_flow* f, void* stream);
+enum { PF2_FIELD_UX = 0, PF2_FIELD_UY = 1, PF2_FIELD_UX_OLD = 2, PF2_FIELD_UY_OLD = 3, PF2_FIELD_PRED_X = 4,
+       PF2_FIELD_PRED_Y = 5, PF2_FIELD_P = 6, PF2_FIELD_P_OLD = 7 };
+pf2_status pf2_flow_field(pf2_flow* f, int which, double** device_ptr);
+/* Host copies of a node field (double[nv]). Synchronise. */
+pf2_status pf2_flow_download_field(pf2_flow* f, int which, double* host_dst);
+pf2_status pf2_flow_upload_field(pf2_flow* f, int which, const double* host_src);
+pf2_status pf2_flow_particles(pf2_flow* f, pf2_particles** ph);
+/* New values for a Dirichlet set of the flow (0 velocity x, 1 velocity y, 2 pressure),
+ * device double[n_bc] in the order the set was created with (a time-dependent inflow). */
+pf2_status pf2_flow_set_boundary_values(pf2_flow* f, int which, const double* values_dev, void* stream);
+
+typedef struct pf2_step_info {
+    int particles;
+    int it_prediction[2][8];
+    int it_pressure[8];
+    int it_correction[2][8];
+    int converged;       /* all solves converged */
+    int status;          /* first device-side error (pf2_status) */
+    double cx, cy;       /* loads, when calculate_loads */
+} pf2_step_info;
+/* Statistics of the last completed step. Synchronises. */
+pf2_status pf2_flow_step_info(pf2_flow* f, pf2_step_info* info);
+
+/* Per-phase device time of the steps (the reference prints per-phase ms with its
+ * GpuTimer and NVTX scopes, src/common/gpu_timer.cuh, Cylinder2D/main.cu:795-879).
+ * pf2_flow_enable_timing records CUDA events around each phase of the next max_steps
+ * steps (0 disables); pf2_flow_phase_times sums them per phase (ms) over the recorded
+ * steps and synchronises. */
+enum { PF2_PHASE_PARTICLES = 0, PF2_PHASE_PROJECTION = 1, PF2_PHASE_PREDICTION_ASSEMBLY = 2,
+       PF2_PHASE_PREDICTION_SOLVE = 3, PF2_PHASE_PRESSURE_ASSEMBLY = 4, PF2_PHASE_PRESSURE_SOLVE = 5,
+       PF2_PHASE_CORRECTION_ASSEMBLY = 6, PF2_PHASE_CORRECTION_SOLVE = 7, PF2_PHASE_PARTICLE_CORRECTION = 8,
+       PF2_PHASES = 9 };
+pf2_status pf2_flow_enable_timing(pf2_flow* f, int max_steps);
+pf2_status pf2_flow_phase_times(pf2_flow* f, double* ms_per_phase, int* steps);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PF2_H */

@@ -1,0 +1,77 @@
+"""CG / GMRES with Jacobi, ILU(0), IC(0) on a jittered-channel SPD system against the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import gpupfem2_gb300 as g
+from gpupfem2_gb300 import meshgen as mg
+from oracle import oracle as O
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(nx=64, ny=16):
+    xy, tri = mg.channel(nx, ny, 4.0, 1.0)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    A = g.SparseMatrixCSR(m)
+    area, invJ = O.mesh_geometry(xy, tri)
+    rp, col = O.csr_structure(xy.shape[0], tri)
+    val, rhs = O.assemble_poisson(xy, tri, area, invJ, rp, col, 1, 1.0)
+    diag = np.array([rp[i] + np.searchsorted(col[rp[i]:rp[i + 1]], i) for i in range(rp.size - 1)])
+    val[diag] += 1e-2
+    A.upload_values(val)
+    return m, A, rp, col, val, rhs
+
+
+@pytest.mark.parametrize("kind,pc", [("cg", "none"), ("cg", "jacobi"), ("cg", "ilu"), ("cg", "ic"),
+                                     ("gmres", "jacobi"), ("gmres", "ilu"), ("gmres", "none")])
+def test_solver_matches_oracle(cuda, kind, pc):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    s = g.LinearSolver(A, kind, pc, tol=1e-8, maxit=1000)
+    info = s.solve(A, x, b)
+    fn = O.pcg if kind == "cg" else O.gmres
+    ox, oinfo = fn(rp, col, val, rhs, tol=1e-8, maxit=1000, precond=pc)
+    assert info.converged == 1 and oinfo.converged == 1
+    assert abs(info.iterations - oinfo.iterations) <= 2
+    # both stop at an absolute 1e-8 criterion; the solutions agree to the solve tolerance
+    assert rel_err(x.cpu().numpy(), ox) < 1e-6
+
+
+@pytest.mark.parametrize("pc", ["ilu", "ic"])
+def test_preconditioner_apply_matches_oracle(cuda, pc):
+    m, A, rp, col, val, rhs = _system(32, 8)
+    s = g.LinearSolver(A, "cg", pc)
+    s.setup(A)
+    src = torch.tensor(rhs, device="cuda")
+    dst = torch.empty_like(src)
+    s.apply_preconditioner(dst, src)
+    f = O.ilu0(rp, col, val) if pc == "ilu" else O.ic0(rp, col, val)
+    ref = np.empty_like(rhs)
+    tmp = np.empty_like(rhs)
+    src_h = np.ascontiguousarray(rhs)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    O.lib().or_precond_apply.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 7
+    O.lib().or_precond_apply(O.PRECOND[pc], rp.size - 1, p(rp), p(col), p(f), None, p(src_h), p(ref), p(tmp))
+    assert rel_err(dst.cpu().numpy(), ref) < 1e-12
+
+
+def test_gmres_restart_converges(cuda):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "gmres", "jacobi", tol=1e-8, maxit=2000, restart=20).solve(A, x, b)
+    ox, _ = O.pcg(rp, col, val, rhs, tol=1e-10, maxit=2000, precond="jacobi")
+    assert info.converged == 1 and rel_err(x.cpu().numpy(), ox) < 1e-6
+
+
+def test_spmv(cuda):
+    m, A, rp, col, val, rhs = _system()
+    x = np.random.default_rng(0).uniform(-1, 1, m.nv)
+    y = torch.empty(m.nv, dtype=torch.float64, device="cuda")
+    g.spmv(A, torch.tensor(x, device="cuda"), y)
+    assert rel_err(y.cpu().numpy(), O.spmv(rp, col, val, x)) < 1e-14
