@@ -216,6 +216,11 @@ struct KArgs {
     double* V;      // (m+1) x n
     double* H;      // m x m, column-major
     int m;          // Krylov dimension
+    // mixed precision
+    const float* val32;   // FP32 copy of the matrix values
+    float *d32, *r32, *p32, *q32, *z32, *invd32;
+    double inner_eta;     // inner solves stop at ||r_inner|| <= eta ||r_outer||
+    int max_outer;
 };
 
 __device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
@@ -484,6 +489,130 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     }
 }
 
+// FP32 SpMV row (FP32 products summed in FP32 within the row; values read through L2
+// only where other blocks write them during the kernel).
+__device__ __forceinline__ float row_times32(const Csr& A, const float* __restrict__ val32, int row, const float* x,
+                                             int lane) {
+    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
+    float sum = 0.0f;
+    for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&val32[k]) * __ldcg(&x[__ldg(&A.col[k])]);
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    return sum;
+}
+
+// Mixed-precision iterative refinement (no reference counterpart): the outer loop keeps
+// x, r = b - A x (FP64 SpMV), the update x += d and the test ||r|| <= tol ||b|| in FP64;
+// each inner solve A d = r is a Jacobi-preconditioned CG whose SpMV, preconditioner
+// and vector updates are FP32 and whose dot products accumulate FP32 products in FP64.
+__global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
+    __shared__ double sh[40];
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    double* P0 = a.partial;
+    double* P1 = a.partial + gridDim.x;
+    double* P2 = a.partial + 2 * gridDim.x;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+        a.invd32[i] = (a.precond == PF2_PRECOND_JACOBI) ? (float)(1.0 / a.A.val[a.A.diag[i]]) : 1.0f;
+    double bb = 0.0;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) bb += a.b[i] * a.b[i];
+    bb = block_sum(bb, sh);
+    if (threadIdx.x == 0) P2[blockIdx.x] = bb;
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    const double bnorm = sqrt(grid_total(P2, sh));
+    int total = 0, outer = 0;
+    bool conv = false;
+    double rnorm = 0.0;
+    while (true) {
+        // r = b - A x in FP64
+        double rr = 0.0;
+        for (int i = r0 + grp; i < r1; i += ngrp) {
+            const double v = row_times(a.A, i, a.x, lane);
+            if (lane == 0) {
+                const double ri = a.b[i] - v;
+                a.r[i] = ri;
+                rr += ri * ri;
+            }
+        }
+        rr = block_sum(rr, sh);
+        if (threadIdx.x == 0) P0[blockIdx.x] = rr;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        rnorm = sqrt(grid_total(P0, sh));
+        if (rnorm <= a.tol * bnorm) { conv = true; break; }
+        if (outer >= a.max_outer || total >= a.maxit) break;
+        ++outer;
+        // inner CG in FP32
+        double g = 0.0;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const float ri = (float)a.r[i];
+            const float zi = ri * a.invd32[i];
+            a.r32[i] = ri;
+            a.d32[i] = 0.0f;
+            a.z32[i] = zi;
+            a.p32[i] = zi;
+            g += (double)ri * (double)zi;
+        }
+        g = block_sum(g, sh);
+        if (threadIdx.x == 0) P1[blockIdx.x] = g;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        double gamma = grid_total(P1, sh);
+        const double target = a.inner_eta * rnorm;
+        while (total < a.maxit) {
+            ++total;
+            double pq = 0.0;
+            for (int i = r0 + grp; i < r1; i += ngrp) {
+                const float v = row_times32(a.A, a.val32, i, a.p32, lane);
+                if (lane == 0) {
+                    a.q32[i] = v;
+                    pq += (double)a.p32[i] * (double)v;
+                }
+            }
+            pq = block_sum(pq, sh);
+            if (threadIdx.x == 0) P0[blockIdx.x] = pq;
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            pq = grid_total(P0, sh);
+            const float alpha = (float)(gamma / pq);
+            double gn = 0.0, rn = 0.0;
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                a.d32[i] += alpha * a.p32[i];
+                const float ri = a.r32[i] - alpha * a.q32[i];
+                const float zi = ri * a.invd32[i];
+                a.r32[i] = ri;
+                a.z32[i] = zi;
+                gn += (double)ri * (double)zi;
+                rn += (double)ri * (double)ri;
+            }
+            gn = block_sum(gn, sh);
+            rn = block_sum(rn, sh);
+            if (threadIdx.x == 0) { P1[blockIdx.x] = gn; P2[blockIdx.x] = rn; }
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            const double gnew = grid_total(P1, sh);
+            const double rin = sqrt(grid_total(P2, sh));
+            if (rin <= target) break;
+            const float beta = (float)(gnew / gamma);
+            gamma = gnew;
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p32[i] = a.z32[i] + beta * a.p32[i];
+            if (!grid_sync(a.bar, gridDim.x)) return;
+        }
+        // x += d in FP64
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[i] += (double)a.d32[i];
+        if (!grid_sync(a.bar, gridDim.x)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = total;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+        a.out->pad = outer;
+    }
+}
+
+__global__ void k_to_float(long long n, const double* __restrict__ a, float* __restrict__ b) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
 __global__ void k_precond_apply(KArgs a) {
     int r0, r1;
     row_range(a.A.n, r0, r1);
@@ -505,6 +634,8 @@ struct pf2_solver {
     PinnedBuf<SolveOut> h_out;
     // ILU / IC
     DevBuf<double> fact, tmp;
+    // mixed precision
+    DevBuf<float> val32, d32, r32, p32, q32, z32, invd32;
     DevBuf<int> fwd_order, bwd_order, lt_off, lt_row, lt_pos, done_f, done_b;
     DevBuf<unsigned> tickets;
     int epoch = 0;
@@ -633,6 +764,20 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.V = S->V.p;
     a.H = S->H.p;
     a.m = S->m;
+    const bool mixed = S->opt.precision == PF2_PRECISION_MIXED && !precond_only;
+    if (mixed) {
+        k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, a.A.val, S->val32.p);
+        PF2_LAUNCH_CHECK();
+        a.val32 = S->val32.p;
+        a.d32 = S->d32.p;
+        a.r32 = S->r32.p;
+        a.p32 = S->p32.p;
+        a.q32 = S->q32.p;
+        a.z32 = S->z32.p;
+        a.invd32 = S->invd32.p;
+        a.inner_eta = 1e-4;
+        a.max_outer = 40;
+    }
     const int applies = (S->opt.kind == PF2_SOLVER_GMRES) ? (S->opt.max_iterations + 2 * (S->opt.max_iterations / std::max(S->m, 1)) + 4)
                                                            : (S->opt.max_iterations + 2);
     if (uses_tri(S)) {
@@ -647,7 +792,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, st);
         return PF2_OK;
     }
-    void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (void*)k_pcg;
+    void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
     PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, st);
     (void)applies;
     return PF2_OK;
@@ -665,7 +810,9 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     PF2_REQUIRE(opt->max_iterations >= 0 && opt->tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
-    PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64, PF2_BAD_INPUT, "mixed precision is built by pf2_solver_create_mixed");
+    PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || opt->precond == PF2_PRECOND_JACOBI ||
+                    opt->precond == PF2_PRECOND_NONE,
+                PF2_BAD_INPUT, "the mixed-precision solver takes Jacobi or no preconditioner");
     pf2_solver* S = new pf2_solver();
     S->opt = *opt;
     S->mesh = A->mesh;
@@ -675,7 +822,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // SolverGMRES::init clamps the iteration limit to the matrix size (linear_solver.cu:396-399)
     if (opt->kind == PF2_SOLVER_GMRES && S->opt.max_iterations > S->n) S->opt.max_iterations = S->n;
     int occ = 0;
-    void* fn = (opt->kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (void*)k_pcg;
+    const bool mixed = opt->precision == PF2_PRECISION_MIXED;
+    void* fn = (opt->kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolverThreads, 0) != cudaSuccess || occ < 1)
         return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
     const int maxb = occ * num_sms();
@@ -685,6 +833,10 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
+        return fail(s);
+    if (mixed && ((s = S->val32.alloc(S->nnz)) || (s = S->d32.alloc(S->n)) || (s = S->r32.alloc(S->n)) ||
+                  (s = S->p32.alloc(S->n)) || (s = S->q32.alloc(S->n)) || (s = S->z32.alloc(S->n)) ||
+                  (s = S->invd32.alloc(S->n))))
         return fail(s);
     if (opt->kind == PF2_SOLVER_GMRES) {
         int m = opt->restart > 0 ? opt->restart : S->opt.max_iterations;
@@ -754,7 +906,7 @@ pf2_status pf2_solver_solve(pf2_solver* S, const pf2_csr* A, double* x, const do
     info->iterations = S->h_out.p->iterations;
     info->converged = S->h_out.p->converged;
     info->residual = S->h_out.p->residual;
-    info->outer_iterations = 1;
+    info->outer_iterations = S->opt.precision == PF2_PRECISION_MIXED ? S->h_out.p->pad : 1;
     info->status = err ? err : S->h_out.p->status;
     PF2_REQUIRE(err == 0, (pf2_status)err, "device-side wait timed out in the solver");
     if (!info->converged) {

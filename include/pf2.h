@@ -211,7 +211,8 @@ typedef struct pf2_solver_options {
     double tolerance;
     int max_iterations;
     int criterion;     /* PF2_CRITERION_* */
-    int precision;     /* PF2_PRECISION_* (CG only) */
+    int precision;     /* PF2_PRECISION_* (CG only; MIXED takes Jacobi or no preconditioner and
+                          always stops on ||b - A x|| <= tol ||b||) */
     int restart;       /* GMRES Krylov dimension; 0 = max_iterations (no restart, as the reference) */
 } pf2_solver_options;
 

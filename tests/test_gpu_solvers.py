@@ -75,3 +75,22 @@ def test_spmv(cuda):
     y = torch.empty(m.nv, dtype=torch.float64, device="cuda")
     g.spmv(A, torch.tensor(x, device="cuda"), y)
     assert rel_err(y.cpu().numpy(), O.spmv(rp, col, val, x)) < 1e-14
+
+
+def test_mixed_precision_refinement_reaches_fp64_residual(cuda):
+    """FP32 inner CG inside FP64 iterative refinement reaches ||b - A x|| <= 1e-8 ||b||,
+    with the residual checked by the oracle's FP64 SpMV."""
+    m, A, rp, col, val, rhs = _system(128, 32)
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    s = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL,
+                       precision=g.PRECISION_MIXED)
+    info = s.solve(A, x, b)
+    assert info.converged == 1 and info.outer_iterations >= 2
+    xs = x.cpu().numpy()
+    res = np.linalg.norm(rhs - O.spmv(rp, col, val, xs)) / np.linalg.norm(rhs)
+    assert res <= 1e-8
+    x64 = torch.zeros_like(b)
+    info64 = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL).solve(A, x64, b)
+    assert info64.converged == 1
+    assert rel_err(xs, x64.cpu().numpy()) < 1e-6
