@@ -46,7 +46,8 @@ class Params(C.Structure):
                 ("calculate_loads", C.c_int), ("body_boundary_id", C.c_int),
                 ("thickness", C.c_double), ("mean_velocity", C.c_double),
                 ("body_cx", C.c_double), ("body_cy", C.c_double),
-                ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int)]
+                ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int),
+                ("pressure_criterion", C.c_int), ("learn_steps", C.c_int), ("learn_rate", C.c_float)]
 
 
 class MeshView(C.Structure):
@@ -73,7 +74,8 @@ class SolveInfo(C.Structure):
 class StepInfo(C.Structure):
     _fields_ = [("particles", C.c_int), ("it_prediction", (C.c_int * 8) * 2), ("it_pressure", C.c_int * 8),
                 ("it_correction", (C.c_int * 8) * 2), ("converged", C.c_int), ("status", C.c_int),
-                ("cx", C.c_double), ("cy", C.c_double)]
+                ("cx", C.c_double), ("cy", C.c_double), ("guess_used", C.c_int),
+                ("guess_residual", C.c_double * 2)]
 
 
 def lib():
@@ -418,3 +420,43 @@ class FlowEngine:
         a = np.ascontiguousarray(values, dtype=np.float64)
         _check(lib().pf2_flow_upload_field(self.h, FIELDS[name], a.ctypes.data_as(C.c_void_p)),
                "pf2_flow_upload_field")
+
+
+class LearnedGuess:
+    """The message-passing network of the learned initial guess (pf2_mpnn_*)."""
+
+    IN, H, LAYERS = 5, 64, 3
+
+    def __init__(self, mesh: Mesh2D, seed=0):
+        self.mesh = mesh
+        self.h = C.c_void_p()
+        _check(lib().pf2_mpnn_create(mesh.h, C.c_ulonglong(seed), C.byref(self.h)), "pf2_mpnn_create")
+        self.n_params = lib().pf2_mpnn_param_count()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.pf2_mpnn_destroy(self.h)
+            self.h = None
+
+    def params(self):
+        p = np.empty(self.n_params, np.float32)
+        _check(lib().pf2_mpnn_get_params(self.h, p.ctypes.data_as(C.c_void_p), None), "pf2_mpnn_get_params")
+        return p
+
+    def grad(self):
+        g = np.empty(self.n_params, np.float32)
+        _check(lib().pf2_mpnn_get_params(self.h, None, g.ctypes.data_as(C.c_void_p)), "pf2_mpnn_get_params")
+        return g
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().pf2_mpnn_set_params(self.h, p.ctypes.data_as(C.c_void_p)), "pf2_mpnn_set_params")
+
+    def forward(self, feat, y):
+        _check(lib().pf2_mpnn_forward(self.h, _dev(feat), _dev(y), _stream()), "pf2_mpnn_forward")
+
+    def train_step(self, feat, target, lr=1e-3, apply=True):
+        loss = C.c_double()
+        _check(lib().pf2_mpnn_train_step(self.h, _dev(feat), _dev(target), C.c_float(lr), int(apply),
+                                         C.byref(loss), _stream()), "pf2_mpnn_train_step")
+        return loss.value

@@ -482,6 +482,9 @@ pf2_status pf2_params_default(pf2_params* p) {
     p->pressure_precision = PF2_PRECISION_FP64;
     p->pressure_x0 = PF2_X0_GIVEN;
     p->gmres_restart = 0;
+    p->pressure_criterion = PF2_CRITERION_ABS;
+    p->learn_steps = 500;
+    p->learn_rate = 1e-3f;
     return PF2_OK;
 }
 

@@ -31,6 +31,12 @@ struct pf2_flow {
     pf2_solver* gmres = nullptr;
     pf2_solver* cg_p = nullptr;
     pf2_solver* cg_c = nullptr;
+    Guess* guess = nullptr;
+    long long steps_done = 0;
+    DevBuf<double> guess_res;
+    DevBuf<int> guess_used;
+    PinnedBuf<double> h_guess_res;
+    PinnedBuf<int> h_guess_used;
     DevBuf<SolveRecord> rec;
     DevBuf<double> loads;
     PinnedBuf<SolveRecord> h_rec;
@@ -62,6 +68,7 @@ struct pf2_flow {
         pf2_solver_destroy(gmres);
         pf2_solver_destroy(cg_p);
         pf2_solver_destroy(cg_c);
+        guess_destroy(guess);
         pf2_particles_destroy(ph);
     }
 };
@@ -110,7 +117,11 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.kind = PF2_SOLVER_CG;
     o.restart = 0;
     o.precond = p->pressure_precond;
+    o.precision = p->pressure_precision;
+    o.criterion = p->pressure_criterion;
     if ((s = pf2_solver_create(F->A[2], &o, &F->cg_p))) return fail(s);
+    o.precision = PF2_PRECISION_FP64;
+    o.criterion = PF2_CRITERION_ABS;
     o.precond = PF2_PRECOND_JACOBI;
     if ((s = pf2_solver_create(F->A[3], &o, &F->cg_c))) return fail(s);
     if ((s = F->rec.alloc(kRecords)) || (s = F->h_rec.alloc(kRecords)) || (s = F->loads.alloc(2)) ||
@@ -120,6 +131,13 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
         cudaMemset(F->loads.p, 0, sizeof(double) * 2) != cudaSuccess)
         return fail(PF2_CUDA_ERROR);
     if (cudaEventCreateWithFlags(&F->done, cudaEventDisableTiming) != cudaSuccess) return fail(PF2_CUDA_ERROR);
+    if ((s = F->guess_res.alloc(2)) || (s = F->guess_used.alloc(1)) || (s = F->h_guess_res.alloc(2)) ||
+        (s = F->h_guess_used.alloc(1)))
+        return fail(s);
+    if (cudaMemset(F->guess_res.p, 0, 2 * sizeof(double)) != cudaSuccess ||
+        cudaMemset(F->guess_used.p, 0, sizeof(int)) != cudaSuccess)
+        return fail(PF2_CUDA_ERROR);
+    if (p->pressure_x0 == PF2_X0_LEARNED && (s = guess_create(mesh, &F->guess))) return fail(s);
     *out = F;
     return PF2_OK;
 }
@@ -166,6 +184,8 @@ pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
         // pressure (:831-842)
         PF2_TRY(launch_pressure(F->mesh, K, px, py, pold, F->A[2]->val.p, F->b[2].p, F->bc[2], st));
         F->mark(st, PF2_PHASE_PRESSURE_ASSEMBLY);
+        if (F->guess && it == 0)
+            PF2_TRY(guess_apply(F->guess, F->A[2], F->b[2].p, pr, nullptr, F->guess_res.p, F->guess_used.p, st));
         PF2_TRY(solver_solve_async(F->cg_p, F->A[2], pr, F->b[2].p, &R[5 * it + 2], st));
         F->mark(st, PF2_PHASE_PRESSURE_SOLVE);
         // velocity correction (:845-860)
@@ -182,10 +202,15 @@ pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
         PF2_TRY(launch_body_loads(F->mesh, K, P.body_boundary_id, P.thickness, P.mean_velocity, P.body_cx, P.body_cy,
                                   ux, uy, pr, F->loads.p, st));
     F->mark(st, PF2_PHASE_PARTICLE_CORRECTION);
+    if (F->guess)
+        PF2_TRY(guess_train(F->guess, pr, F->steps_done < P.learn_steps ? P.learn_rate : 0.0f, st));
+    ++F->steps_done;
     if (F->tmax && F->tsteps < F->tmax) ++F->tsteps;
     PF2_CUDA(cudaMemcpyAsync(F->h_rec.p, F->rec.p, sizeof(SolveRecord) * kRecords, cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(F->h_loads.p, F->loads.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(F->h_np.p, particles_count_ptr(F->ph), sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(F->h_guess_res.p, F->guess_res.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(F->h_guess_used.p, F->guess_used.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaEventRecord(F->done, st));
     F->stepped = true;
     return PF2_OK;
@@ -275,6 +300,9 @@ pf2_status pf2_flow_step_info(pf2_flow* F, pf2_step_info* info) {
     }
     info->cx = F->h_loads.p[0];
     info->cy = F->h_loads.p[1];
+    info->guess_used = F->guess ? F->h_guess_used.p[0] : 0;
+    info->guess_residual[0] = F->h_guess_res.p[0];
+    info->guess_residual[1] = F->h_guess_res.p[1];
     PF2_REQUIRE(info->status == PF2_OK, (pf2_status)info->status, "a device-side wait timed out during the step");
     return PF2_OK;
 }

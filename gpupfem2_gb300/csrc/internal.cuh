@@ -43,4 +43,16 @@ struct SolveRecord {
 pf2_status solver_solve_async(pf2_solver* s, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
                               cudaStream_t st);
 
+// Learned initial guess of the pressure solve (guess.cu).
+struct Guess;
+pf2_status guess_create(const pf2_mesh* m, Guess** out);
+void guess_destroy(Guess* g);
+// Before the first pressure solve of a step: features from (x, y, b, p, p_prev), the
+// network's candidate x0, and x <- the candidate if its residual ||b - A x0|| is smaller
+// than that of x (the previous-step pressure).  Residuals go to res_out[2].
+pf2_status guess_apply(Guess* g, const pf2_csr* A, const double* b, double* x, const double* p_prev,
+                       double* res_out, int* used_out, cudaStream_t st);
+// After the step: one AdamW step on the target (p_new - p) of the features of guess_apply.
+pf2_status guess_train(Guess* g, const double* p_new, float lr, cudaStream_t st);
+
 }  // namespace pf2

@@ -1,0 +1,586 @@
+// mpnn.cu - the learned initial guess of the pressure solve (no reference counterpart).
+//
+// A message-passing network over the mesh graph (nodes; edges = off-diagonal CSR
+// entries, symmetric) with 5 input features, 64 hidden units and 3 layers:
+//   h0 = relu(W0 f + c0)
+//   l = 1..3:  m_i = mean_{j in N(i)} h_j ;  h = h + relu(W_l [h ; m] + c_l)
+//   y  = w4 . h + c4
+// Master parameters are FP32; the per-node MLPs run on the tensor cores with BF16
+// weights and activations and FP32 accumulation (mma.sync m16n8k16).  Training
+// (backward and AdamW) runs on the device; gradients are summed in a fixed order.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "device.cuh"
+#include "internal.cuh"
+
+namespace pf2 {
+
+constexpr int MH = 64;      // hidden width
+constexpr int MIN = 5;      // input features
+constexpr int ML = 3;       // message-passing layers
+constexpr int MK = 2 * MH;  // layer input width [h ; m]
+constexpr int kTile = 64;   // nodes per CTA tile
+constexpr int kMpnnThreads = 128;
+constexpr int kPad = 8;     // bf16 row padding against bank conflicts
+
+constexpr int kParamW0 = 0;
+constexpr int kParamC0 = kParamW0 + MH * MIN;
+constexpr int kParamLayer0 = kParamC0 + MH;
+constexpr int kLayerSize = MH * MK + MH;
+constexpr int kParamW4 = kParamLayer0 + ML * kLayerSize;
+constexpr int kParamC4 = kParamW4 + MH;
+constexpr int kParams = kParamC4 + 1;
+
+__device__ __forceinline__ unsigned pack_bf16(float a, float b) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<unsigned*>(&v);
+}
+
+// D = A(16x16, row) * B(16x8, col) + D, bf16 inputs, f32 accumulate
+__device__ __forceinline__ void mma16816(float d[4], const unsigned a[4], const unsigned b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// One warp: acc[16 x 8NT] += A[16 x 16KT] (smem row-major, stride sa) * B, with B given as
+// rows of n (smem [n][k], stride sb).
+template <int KT, int NT>
+__device__ __forceinline__ void warp_gemm(const __nv_bfloat16* A, int sa, const __nv_bfloat16* B, int sb,
+                                          float acc[NT][4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt) {
+        const int k0 = kt * 16 + 2 * t;
+        unsigned a[4];
+        a[0] = *reinterpret_cast<const unsigned*>(A + g * sa + k0);
+        a[1] = *reinterpret_cast<const unsigned*>(A + (g + 8) * sa + k0);
+        a[2] = *reinterpret_cast<const unsigned*>(A + g * sa + k0 + 8);
+        a[3] = *reinterpret_cast<const unsigned*>(A + (g + 8) * sa + k0 + 8);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const __nv_bfloat16* Bn = B + (nt * 8 + g) * sb + k0;
+            unsigned b[2];
+            b[0] = *reinterpret_cast<const unsigned*>(Bn);
+            b[1] = *reinterpret_cast<const unsigned*>(Bn + 8);
+            mma16816(acc[nt], a, b);
+        }
+    }
+}
+
+struct Graph {
+    int n;
+    const int* rowptr;
+    const int* col;
+    const float* deg_inv;  // 1 / #neighbours (0 for an isolated node)
+};
+
+// ---------------------------------------------------------------- forward
+__global__ void k_mpnn_encoder(Graph G, const float* __restrict__ feat, const float* __restrict__ P, float* H0,
+                               unsigned long long* mask0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= G.n) return;
+    float f[MIN];
+#pragma unroll
+    for (int k = 0; k < MIN; ++k) f[k] = feat[(size_t)i * MIN + k];
+    unsigned long long mk = 0ull;
+    for (int o = 0; o < MH; ++o) {
+        float s = P[kParamC0 + o];
+#pragma unroll
+        for (int k = 0; k < MIN; ++k) s += P[kParamW0 + o * MIN + k] * f[k];
+        if (s > 0.0f) mk |= 1ull << o;
+        H0[(size_t)i * MH + o] = s > 0.0f ? s : 0.0f;
+    }
+    mask0[i] = mk;
+}
+
+// mean of the neighbours' h (fixed order: ascending column)
+__device__ __forceinline__ void gather_mean(const Graph& G, const float* __restrict__ H, int i, int o, float& out) {
+    float s = 0.0f;
+    for (int k = G.rowptr[i]; k < G.rowptr[i + 1]; ++k) {
+        const int j = G.col[k];
+        if (j != i) s += H[(size_t)j * MH + o];
+    }
+    out = s * G.deg_inv[i];
+}
+
+// One layer: h_out = h_in + relu(W [h_in ; m] + c); stores m (for the backward pass)
+// and the relu mask.  CTA = 4 warps x 16 nodes.
+__global__ void __launch_bounds__(kMpnnThreads) k_mpnn_layer(Graph G, const float* __restrict__ Hin,
+                                                             const __nv_bfloat16* __restrict__ Wb,
+                                                             const float* __restrict__ c, float* Hout, float* M,
+                                                             unsigned long long* mask) {
+    __shared__ __align__(16) __nv_bfloat16 sA[kTile][MK + kPad];
+    __shared__ __align__(16) __nv_bfloat16 sW[MH][MK + kPad];
+    const int base = blockIdx.x * kTile;
+    for (int q = threadIdx.x; q < MH * MK; q += blockDim.x) sW[q / MK][q % MK] = Wb[q];
+    for (int q = threadIdx.x; q < kTile * MH; q += blockDim.x) {
+        const int r = q / MH, o = q % MH, i = base + r;
+        float h = 0.0f, m = 0.0f;
+        if (i < G.n) {
+            h = Hin[(size_t)i * MH + o];
+            gather_mean(G, Hin, i, o, m);
+            M[(size_t)i * MH + o] = m;
+        }
+        sA[r][o] = __float2bfloat16_rn(h);
+        sA[r][MH + o] = __float2bfloat16_rn(m);
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[MH / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < MH / 8; ++nt)
+        for (int k = 0; k < 4; ++k) acc[nt][k] = 0.0f;
+    warp_gemm<MK / 16, MH / 8>(&sA[w * 16][0], MK + kPad, &sW[0][0], MK + kPad, acc);
+    // epilogue: rows g, g+8 of this warp's 16 nodes; columns nt*8 + 2t, +1
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int i = base + w * 16 + g + 8 * half;
+        const bool valid = i < G.n;
+        unsigned long long bits = 0ull;
+#pragma unroll
+        for (int nt = 0; nt < MH / 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int o = nt * 8 + 2 * t + e;
+                const float z = acc[nt][2 * half + e] + c[o];
+                if (z > 0.0f) bits |= 1ull << o;
+                if (valid) Hout[(size_t)i * MH + o] = Hin[(size_t)i * MH + o] + (z > 0.0f ? z : 0.0f);
+            }
+        // the four threads of a quad own disjoint columns of the row: combine their bits
+        // (every lane takes part in the shuffles; only the store is guarded)
+        bits |= __shfl_xor_sync(0xffffffffu, bits, 1);
+        bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
+        if (valid && t == 0) mask[i] = bits;
+    }
+}
+
+// y = w4 . h + c4; optionally loss partials and dy = 2 (y - t) / n
+__global__ void k_mpnn_decoder(int n, const float* __restrict__ H, const float* __restrict__ P, float* y,
+                               const float* __restrict__ target, float* dy, double* loss_part) {
+    __shared__ double sh[40];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double l = 0.0;
+    if (i < n) {
+        float s = P[kParamC4];
+        for (int o = 0; o < MH; ++o) s += P[kParamW4 + o] * H[(size_t)i * MH + o];
+        y[i] = s;
+        if (target) {
+            const float r = s - target[i];
+            dy[i] = 2.0f * r / (float)n;
+            l = (double)r * r;
+        }
+    }
+    if (target) {
+        l = block_sum(l, sh);
+        if (threadIdx.x == 0) loss_part[blockIdx.x] = l;
+    }
+}
+
+// ---------------------------------------------------------------- backward
+// dh = dy w4, and per-block partials of (dw4, dc4)
+__global__ void k_mpnn_decoder_back(int n, const float* __restrict__ H, const float* __restrict__ P,
+                                    const float* __restrict__ dy, float* dH, float* part /* [grid][MH+1] */) {
+    __shared__ float sp[MH + 1][kMpnnThreads / 32];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const float d = (i < n) ? dy[i] : 0.0f;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 0; o <= MH; ++o) {
+        float v = 0.0f;
+        if (i < n) {
+            if (o < MH) {
+                v = d * H[(size_t)i * MH + o];
+                dH[(size_t)i * MH + o] = d * P[kParamW4 + o];
+            } else {
+                v = d;
+            }
+        }
+        v = warp_sumf(v);
+        if (lane == 0) sp[o][w] = v;
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o <= MH; o += blockDim.x) {
+        float s = 0.0f;
+        for (int k = 0; k < kMpnnThreads / 32; ++k) s += sp[o][k];
+        part[(size_t)blockIdx.x * (MH + 1) + o] = s;
+    }
+}
+
+// One layer backward, node part: dz = dh * mask; [dself ; dm] = dz W (tensor cores);
+// writes dself and dm / d_i.
+__global__ void __launch_bounds__(kMpnnThreads) k_mpnn_layer_back_nodes(Graph G, const float* __restrict__ dH,
+                                                                        const unsigned long long* __restrict__ mask,
+                                                                        const __nv_bfloat16* __restrict__ Wb,
+                                                                        float* dSelf, float* dMs) {
+    __shared__ __align__(16) __nv_bfloat16 sZ[kTile][MH + kPad];
+    __shared__ __align__(16) __nv_bfloat16 sWT[MK][MH + kPad];  // W^T: [in][out]
+    const int base = blockIdx.x * kTile;
+    for (int q = threadIdx.x; q < MH * MK; q += blockDim.x) {
+        const int o = q / MK, k = q % MK;
+        sWT[k][o] = Wb[q];
+    }
+    for (int q = threadIdx.x; q < kTile * MH; q += blockDim.x) {
+        const int r = q / MH, o = q % MH, i = base + r;
+        float v = 0.0f;
+        if (i < G.n && ((mask[i] >> o) & 1ull)) v = dH[(size_t)i * MH + o];
+        sZ[r][o] = __float2bfloat16_rn(v);
+    }
+    __syncthreads();
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float acc[MK / 8][4];
+#pragma unroll
+    for (int nt = 0; nt < MK / 8; ++nt)
+        for (int k = 0; k < 4; ++k) acc[nt][k] = 0.0f;
+    warp_gemm<MH / 16, MK / 8>(&sZ[w * 16][0], MH + kPad, &sWT[0][0], MH + kPad, acc);
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int i = base + w * 16 + g + 8 * half;
+        if (i >= G.n) continue;
+        const float di = G.deg_inv[i];
+#pragma unroll
+        for (int nt = 0; nt < MK / 8; ++nt)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int k = nt * 8 + 2 * t + e;
+                const float v = acc[nt][2 * half + e];
+                if (k < MH) dSelf[(size_t)i * MH + k] = v;
+                else dMs[(size_t)i * MH + (k - MH)] = v * di;
+            }
+    }
+}
+
+// dh_prev_i = dh_i + dself_i + sum_{k in N(i)} dm_k / d_k (the graph is symmetric)
+__global__ void k_mpnn_agg_back(Graph G, const float* __restrict__ dH, const float* __restrict__ dSelf,
+                                const float* __restrict__ dMs, float* dHprev) {
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)G.n * MH) return;
+    const int i = (int)(q / MH), o = (int)(q % MH);
+    float s = dH[q] + dSelf[q];
+    for (int k = G.rowptr[i]; k < G.rowptr[i + 1]; ++k) {
+        const int j = G.col[k];
+        if (j != i) s += dMs[(size_t)j * MH + o];
+    }
+    dHprev[q] = s;
+}
+
+// One layer backward, weight part: per-CTA partial dW (= [h ; m]^T dz, tensor cores) and
+// dc, over the node tiles this CTA visits.
+__global__ void __launch_bounds__(kMpnnThreads) k_mpnn_layer_back_weights(Graph G, const float* __restrict__ Hin,
+                                                                          const float* __restrict__ M,
+                                                                          const float* __restrict__ dH,
+                                                                          const unsigned long long* __restrict__ mask,
+                                                                          float* part /* [grid][MH*MK + MH] */) {
+    __shared__ __align__(16) __nv_bfloat16 sAT[MK][kTile + kPad];  // [in][node]
+    __shared__ __align__(16) __nv_bfloat16 sZT[MH][kTile + kPad];  // [out][node]
+    __shared__ float sC[MH];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    // warp w owns rows (inputs) w*32 .. w*32+31: two m tiles
+    float acc[2][MH / 8][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < MH / 8; ++nt)
+            for (int k = 0; k < 4; ++k) acc[mt][nt][k] = 0.0f;
+    for (int o = threadIdx.x; o < MH; o += blockDim.x) sC[o] = 0.0f;
+    const int ntiles = (G.n + kTile - 1) / kTile;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int base = tile * kTile;
+        __syncthreads();
+        for (int q = threadIdx.x; q < kTile * MH; q += blockDim.x) {
+            const int r = q / MH, o = q % MH, i = base + r;
+            float h = 0.0f, m = 0.0f, z = 0.0f;
+            if (i < G.n) {
+                h = Hin[(size_t)i * MH + o];
+                m = M[(size_t)i * MH + o];
+                if ((mask[i] >> o) & 1ull) z = dH[(size_t)i * MH + o];
+            }
+            sAT[o][r] = __float2bfloat16_rn(h);
+            sAT[MH + o][r] = __float2bfloat16_rn(m);
+            sZT[o][r] = __float2bfloat16_rn(z);
+        }
+        __syncthreads();
+        for (int o = threadIdx.x; o < MH; o += blockDim.x) {
+            float s = 0.0f;
+            for (int r = 0; r < kTile; ++r) s += __bfloat162float(sZT[o][r]);
+            sC[o] += s;
+        }
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt)
+            warp_gemm<kTile / 16, MH / 8>(&sAT[w * 32 + mt * 16][0], kTile + kPad, &sZT[0][0], kTile + kPad, acc[mt]);
+    }
+    __syncthreads();
+    // dW[out][in] = acc[in][out]
+    float* P = part + (size_t)blockIdx.x * (MH * MK + MH);
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int in = w * 32 + mt * 16 + g + 8 * half;
+#pragma unroll
+            for (int nt = 0; nt < MH / 8; ++nt)
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int o = nt * 8 + 2 * t + e;
+                    P[o * MK + in] = acc[mt][nt][2 * half + e];
+                }
+        }
+    for (int o = threadIdx.x; o < MH; o += blockDim.x) P[MH * MK + o] = sC[o];
+}
+
+// Encoder backward: per-block partials of (dW0, dc0)
+__global__ void k_mpnn_encoder_back(int n, const float* __restrict__ feat, const float* __restrict__ dH,
+                                    const unsigned long long* __restrict__ mask0, float* part /* [grid][MH*MIN+MH] */) {
+    __shared__ float sp[MH * (MIN + 1)];
+    for (int q = threadIdx.x; q < MH * (MIN + 1); q += blockDim.x) sp[q] = 0.0f;
+    __syncthreads();
+    const int nper = (n + gridDim.x - 1) / gridDim.x;
+    const int i0 = blockIdx.x * nper, i1 = min(n, i0 + nper);
+    // thread (o, k): sums dz_o * f_k (k < MIN) or dz_o (k == MIN) over this block's nodes
+    for (int q = threadIdx.x; q < MH * (MIN + 1); q += blockDim.x) {
+        const int o = q / (MIN + 1), k = q % (MIN + 1);
+        float s = 0.0f;
+        for (int i = i0; i < i1; ++i) {
+            if (!((mask0[i] >> o) & 1ull)) continue;
+            const float dz = dH[(size_t)i * MH + o];
+            s += (k < MIN) ? dz * feat[(size_t)i * MIN + k] : dz;
+        }
+        sp[q] = s;
+    }
+    __syncthreads();
+    float* P = part + (size_t)blockIdx.x * (MH * MIN + MH);
+    for (int q = threadIdx.x; q < MH * (MIN + 1); q += blockDim.x) {
+        const int o = q / (MIN + 1), k = q % (MIN + 1);
+        if (k < MIN) P[o * MIN + k] = sp[q];
+        else P[MH * MIN + o] = sp[q];
+    }
+}
+
+// grad[off + j] = sum_b part[b * width + j], fixed order, FP64 accumulation
+__global__ void k_reduce_cols(const float* __restrict__ part, int nb, int width, float* grad, int off) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= width) return;
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)b * width + j];
+    grad[off + j] = (float)s;
+}
+
+__global__ void k_adamw(int np, float* P, const float* __restrict__ g, float* m, float* v, float c1, float c2,
+                        float lr, float b1, float b2, float eps, float wd) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    const float gk = g[k];
+    const float mk = b1 * m[k] + (1.0f - b1) * gk;
+    const float vk = b2 * v[k] + (1.0f - b2) * gk * gk;
+    m[k] = mk;
+    v[k] = vk;
+    P[k] -= lr * (mk / c1 / (sqrtf(vk / c2) + eps) + wd * P[k]);
+}
+
+__global__ void k_weights_bf16(const float* __restrict__ P, __nv_bfloat16* Wb) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ML * MH * MK) return;
+    const int l = q / (MH * MK), r = q % (MH * MK);
+    Wb[q] = __float2bfloat16_rn(P[kParamLayer0 + l * kLayerSize + r]);
+}
+
+__global__ void k_deg_inv(int n, const int* __restrict__ rowptr, const int* __restrict__ col, float* dinv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int d = 0;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) d += (col[k] != i);
+    dinv[i] = d ? 1.0f / (float)d : 0.0f;
+}
+
+}  // namespace pf2
+
+using namespace pf2;
+
+struct pf2_mpnn {
+    int n = 0;
+    const pf2_mesh* mesh = nullptr;
+    DevBuf<float> P, grad, am, av, dinv, feat, y, dy, H, M, dH, dH2, dSelf, dMs, part, target;
+    DevBuf<unsigned long long> mask;
+    DevBuf<__nv_bfloat16> Wb;
+    DevBuf<double> loss_part;
+    int step = 0;
+    int wgrid = 0;
+    Graph graph() const { return Graph{ n, mesh->rowptr.p, mesh->col.p, dinv.p }; }
+    float* Hl(int l) { return H.p + (size_t)l * n * MH; }
+    float* Ml(int l) { return M.p + (size_t)l * n * MH; }
+    unsigned long long* maskl(int l) { return mask.p + (size_t)l * n; }
+};
+
+namespace pf2 {
+
+static pf2_status mpnn_forward(pf2_mpnn* N, cudaStream_t st) {
+    const Graph G = N->graph();
+    k_mpnn_encoder<<<blocks_for(N->n), kThreads, 0, st>>>(G, N->feat.p, N->P.p, N->Hl(0), N->maskl(0));
+    PF2_LAUNCH_CHECK();
+    const unsigned tiles = blocks_for(N->n, kTile);
+    for (int l = 0; l < ML; ++l) {
+        k_mpnn_layer<<<tiles, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Wb.p + (size_t)l * MH * MK,
+                                                     N->P.p + kParamLayer0 + l * kLayerSize + MH * MK, N->Hl(l + 1),
+                                                     N->Ml(l), N->maskl(l + 1));
+        PF2_LAUNCH_CHECK();
+    }
+    return PF2_OK;
+}
+
+static pf2_status mpnn_backward(pf2_mpnn* N, cudaStream_t st) {
+    const Graph G = N->graph();
+    const unsigned nb = blocks_for(N->n, kMpnnThreads);
+    k_mpnn_decoder_back<<<nb, kMpnnThreads, 0, st>>>(N->n, N->Hl(ML), N->P.p, N->dy.p, N->dH.p, N->part.p);
+    PF2_LAUNCH_CHECK();
+    k_reduce_cols<<<blocks_for(MH + 1), kThreads, 0, st>>>(N->part.p, (int)nb, MH + 1, N->grad.p, kParamW4);
+    PF2_LAUNCH_CHECK();
+    const unsigned tiles = blocks_for(N->n, kTile);
+    float* dh = N->dH.p;
+    float* dh2 = N->dH2.p;
+    for (int l = ML - 1; l >= 0; --l) {
+        const __nv_bfloat16* W = N->Wb.p + (size_t)l * MH * MK;
+        k_mpnn_layer_back_weights<<<N->wgrid, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Ml(l), dh, N->maskl(l + 1),
+                                                                     N->part.p);
+        PF2_LAUNCH_CHECK();
+        k_reduce_cols<<<blocks_for(kLayerSize), kThreads, 0, st>>>(N->part.p, N->wgrid, kLayerSize, N->grad.p,
+                                                                   kParamLayer0 + l * kLayerSize);
+        PF2_LAUNCH_CHECK();
+        k_mpnn_layer_back_nodes<<<tiles, kMpnnThreads, 0, st>>>(G, dh, N->maskl(l + 1), W, N->dSelf.p, N->dMs.p);
+        PF2_LAUNCH_CHECK();
+        k_mpnn_agg_back<<<blocks_for((long long)N->n * MH), kThreads, 0, st>>>(G, dh, N->dSelf.p, N->dMs.p, dh2);
+        PF2_LAUNCH_CHECK();
+        std::swap(dh, dh2);
+    }
+    k_mpnn_encoder_back<<<N->wgrid, kThreads, 0, st>>>(N->n, N->feat.p, dh, N->maskl(0), N->part.p);
+    PF2_LAUNCH_CHECK();
+    k_reduce_cols<<<blocks_for(MH * MIN + MH), kThreads, 0, st>>>(N->part.p, N->wgrid, MH * MIN + MH, N->grad.p,
+                                                                  kParamW0);
+    PF2_LAUNCH_CHECK();
+    return PF2_OK;
+}
+
+}  // namespace pf2
+
+extern "C" {
+
+pf2_status pf2_mpnn_create(const pf2_mesh* mesh, unsigned long long seed, pf2_mpnn** out) {
+    PF2_REQUIRE(mesh && out, PF2_BAD_INPUT, "null argument");
+    *out = nullptr;
+    pf2_mpnn* N = new pf2_mpnn();
+    N->mesh = mesh;
+    N->n = mesh->nv;
+    const size_t n = N->n;
+    auto fail = [&](pf2_status s) { delete N; return s; };
+    N->wgrid = std::max(1, std::min((int)blocks_for(N->n, kTile), num_sms() * 2));
+    const size_t part = std::max<size_t>((size_t)N->wgrid * (MH * MK + MH),
+                                         (size_t)blocks_for(N->n, kMpnnThreads) * (MH + 1));
+    pf2_status s;
+    if ((s = N->P.alloc(kParams)) || (s = N->grad.alloc(kParams)) || (s = N->am.alloc(kParams)) ||
+        (s = N->av.alloc(kParams)) || (s = N->dinv.alloc(n)) || (s = N->feat.alloc(n * MIN)) ||
+        (s = N->y.alloc(n)) || (s = N->dy.alloc(n)) || (s = N->target.alloc(n)) ||
+        (s = N->H.alloc((ML + 1) * n * MH)) || (s = N->M.alloc(ML * n * MH)) || (s = N->dH.alloc(n * MH)) ||
+        (s = N->dH2.alloc(n * MH)) || (s = N->dSelf.alloc(n * MH)) || (s = N->dMs.alloc(n * MH)) ||
+        (s = N->part.alloc(part)) || (s = N->mask.alloc((ML + 1) * n)) || (s = N->Wb.alloc(ML * MH * MK)) ||
+        (s = N->loss_part.alloc(blocks_for(N->n))))
+        return fail(s);
+    // He-style initialisation from a splitmix64 stream (deterministic for a seed);
+    // the output layer starts at zero so the untrained guess is the extrapolation alone
+    std::vector<float> h(kParams, 0.0f);
+    unsigned long long st = seed;
+    auto next = [&]() {
+        st += 0x9E3779B97F4A7C15ull;
+        unsigned long long z = st;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    for (int k = 0; k < MH * MIN; ++k) h[kParamW0 + k] = (float)(next() * std::sqrt(6.0 / MIN));
+    for (int l = 0; l < ML; ++l)
+        for (int k = 0; k < MH * MK; ++k)
+            h[kParamLayer0 + l * kLayerSize + k] = (float)(next() * std::sqrt(6.0 / MK) * 0.5);
+    if (cudaMemcpy(N->P.p, h.data(), sizeof(float) * kParams, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(N->am.p, 0, sizeof(float) * kParams) != cudaSuccess ||
+        cudaMemset(N->av.p, 0, sizeof(float) * kParams) != cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "mpnn init", __FILE__, __LINE__));
+    k_deg_inv<<<blocks_for(N->n), kThreads>>>(N->n, mesh->rowptr.p, mesh->col.p, N->dinv.p);
+    k_weights_bf16<<<blocks_for(ML * MH * MK), kThreads>>>(N->P.p, N->Wb.p);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(cuda_fail(cudaGetLastError(), "mpnn init", __FILE__, __LINE__));
+    *out = N;
+    return PF2_OK;
+}
+
+pf2_status pf2_mpnn_destroy(pf2_mpnn* N) {
+    delete N;
+    return PF2_OK;
+}
+
+int pf2_mpnn_param_count(void) { return kParams; }
+
+pf2_status pf2_mpnn_set_params(pf2_mpnn* N, const float* params_host) {
+    PF2_REQUIRE(N && params_host, PF2_BAD_INPUT, "null argument");
+    PF2_CUDA(cudaMemcpy(N->P.p, params_host, sizeof(float) * kParams, cudaMemcpyHostToDevice));
+    k_weights_bf16<<<blocks_for(ML * MH * MK), kThreads>>>(N->P.p, N->Wb.p);
+    PF2_LAUNCH_CHECK();
+    PF2_CUDA(cudaDeviceSynchronize());
+    return PF2_OK;
+}
+
+pf2_status pf2_mpnn_get_params(const pf2_mpnn* N, float* params_host, float* grad_host) {
+    PF2_REQUIRE(N, PF2_BAD_INPUT, "null argument");
+    PF2_CUDA(cudaDeviceSynchronize());
+    if (params_host) PF2_CUDA(cudaMemcpy(params_host, N->P.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
+    if (grad_host) PF2_CUDA(cudaMemcpy(grad_host, N->grad.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
+    return PF2_OK;
+}
+
+pf2_status pf2_mpnn_forward(pf2_mpnn* N, const float* feat_dev, float* y_dev, void* stream) {
+    PF2_REQUIRE(N && feat_dev && y_dev, PF2_BAD_INPUT, "null argument");
+    cudaStream_t st = as_stream(stream);
+    PF2_CUDA(cudaMemcpyAsync(N->feat.p, feat_dev, sizeof(float) * MIN * (size_t)N->n, cudaMemcpyDeviceToDevice, st));
+    PF2_TRY(mpnn_forward(N, st));
+    k_mpnn_decoder<<<blocks_for(N->n), kThreads, 0, st>>>(N->n, N->Hl(ML), N->P.p, y_dev, nullptr, nullptr, nullptr);
+    PF2_LAUNCH_CHECK();
+    return PF2_OK;
+}
+
+pf2_status pf2_mpnn_train_step(pf2_mpnn* N, const float* feat_dev, const float* target_dev, float lr, int apply,
+                               double* loss_host, void* stream) {
+    PF2_REQUIRE(N && feat_dev && target_dev, PF2_BAD_INPUT, "null argument");
+    cudaStream_t st = as_stream(stream);
+    PF2_CUDA(cudaMemcpyAsync(N->feat.p, feat_dev, sizeof(float) * MIN * (size_t)N->n, cudaMemcpyDeviceToDevice, st));
+    PF2_CUDA(cudaMemcpyAsync(N->target.p, target_dev, sizeof(float) * (size_t)N->n, cudaMemcpyDeviceToDevice, st));
+    PF2_TRY(mpnn_forward(N, st));
+    k_mpnn_decoder<<<blocks_for(N->n), kThreads, 0, st>>>(N->n, N->Hl(ML), N->P.p, N->y.p, N->target.p, N->dy.p,
+                                                         N->loss_part.p);
+    PF2_LAUNCH_CHECK();
+    PF2_TRY(mpnn_backward(N, st));
+    if (apply) {
+        ++N->step;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.0f - std::pow(b1, (float)N->step), c2 = 1.0f - std::pow(b2, (float)N->step);
+        k_adamw<<<blocks_for(kParams), kThreads, 0, st>>>(kParams, N->P.p, N->grad.p, N->am.p, N->av.p, c1, c2, lr,
+                                                          b1, b2, 1e-8f, 0.01f);
+        PF2_LAUNCH_CHECK();
+        k_weights_bf16<<<blocks_for(ML * MH * MK), kThreads, 0, st>>>(N->P.p, N->Wb.p);
+        PF2_LAUNCH_CHECK();
+    }
+    if (loss_host) {
+        std::vector<double> lp(blocks_for(N->n));
+        PF2_CUDA(cudaMemcpyAsync(lp.data(), N->loss_part.p, sizeof(double) * lp.size(), cudaMemcpyDeviceToHost, st));
+        PF2_CUDA(cudaStreamSynchronize(st));
+        double s = 0.0;
+        for (double v : lp) s += v;
+        *loss_host = s / N->n;
+    }
+    return PF2_OK;
+}
+
+}  // extern "C"

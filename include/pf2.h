@@ -162,6 +162,9 @@ typedef struct pf2_params {
     int pressure_precision;  /* PF2_PRECISION_* for the pressure solve */
     int pressure_x0;         /* PF2_X0_* for the pressure solve */
     int gmres_restart;       /* Krylov dimension of the prediction GMRES, 0 = no restart */
+    int pressure_criterion;  /* PF2_CRITERION_* of the pressure solve */
+    int learn_steps;         /* PF2_X0_LEARNED: train the network on the first learn_steps steps */
+    float learn_rate;        /* AdamW learning rate of that training */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -312,6 +315,8 @@ typedef struct pf2_step_info {
     int converged;       /* all solves converged */
     int status;          /* first device-side error (pf2_status) */
     double cx, cy;       /* loads, when calculate_loads */
+    int guess_used;      /* PF2_X0_LEARNED: 1 if the network's guess started the pressure solve */
+    double guess_residual[2]; /* ||b - A x0|| of the previous-step guess and of the network's */
 } pf2_step_info;
 /* Statistics of the last completed step. Synchronises. */
 pf2_status pf2_flow_step_info(pf2_flow* f, pf2_step_info* info);
@@ -327,6 +332,28 @@ enum { PF2_PHASE_PARTICLES = 0, PF2_PHASE_PROJECTION = 1, PF2_PHASE_PREDICTION_A
        PF2_PHASES = 9 };
 pf2_status pf2_flow_enable_timing(pf2_flow* f, int max_steps);
 pf2_status pf2_flow_phase_times(pf2_flow* f, double* ms_per_phase, int* steps);
+
+/* ------------------------------------------------- Learned initial guess
+ * No reference counterpart.  A message-passing network over the mesh graph (nodes;
+ * edges = off-diagonal CSR entries): 5 input features per node, 64 hidden units, 3
+ * layers (h0 = relu(W0 f + c0); h += relu(Wl [h ; mean of neighbours' h] + cl);
+ * y = w4 . h + c4), FP32 master parameters, BF16 tensor-core MLPs with FP32
+ * accumulation, training by AdamW (beta 0.9/0.999, eps 1e-8, weight decay 0.01) on the
+ * device.  Parameter order: W0[64x5], c0, (Wl[64x128], cl) x 3, w4[64], c4. */
+typedef struct pf2_mpnn pf2_mpnn;
+pf2_status pf2_mpnn_create(const pf2_mesh* mesh, unsigned long long seed, pf2_mpnn** out);
+pf2_status pf2_mpnn_destroy(pf2_mpnn* net);
+int pf2_mpnn_param_count(void);
+/* Host copies of the parameters / of the last gradient (NULL skips). Synchronise. */
+pf2_status pf2_mpnn_set_params(pf2_mpnn* net, const float* params_host);
+pf2_status pf2_mpnn_get_params(const pf2_mpnn* net, float* params_host, float* grad_host);
+/* y = network(features); feat: device float[nv*5] node-major, y: device float[nv]. */
+pf2_status pf2_mpnn_forward(pf2_mpnn* net, const float* feat, float* y, void* stream);
+/* One training step on L = mean (y - target)^2: forward, backward (gradient kept for
+ * pf2_mpnn_get_params) and, if apply != 0, an AdamW update with rate lr.  loss_host may
+ * be NULL; when not, the call synchronises to fill it. */
+pf2_status pf2_mpnn_train_step(pf2_mpnn* net, const float* feat, const float* target, float lr, int apply,
+                               double* loss_host, void* stream);
 
 #ifdef __cplusplus
 }

@@ -349,3 +349,44 @@ class Flow:
         val, rhs = np.empty(nnz, D), np.empty(self.nv, D)
         lib().or_flow_get_matrix(self.h, which, val, rhs)
         return val, rhs
+
+
+# ---- learned initial guess (message-passing network) -----------------------------
+MPNN_H, MPNN_IN, MPNN_LAYERS = 64, 5, 3
+
+
+def _declare_mpnn(L):
+    L.or_mpnn_param_count.restype = C.c_int
+    L.or_mpnn_forward.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_void_p]
+    L.or_mpnn_forward.restype = C.c_double
+    L.or_mpnn_backward.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, _dp]
+    L.or_mpnn_backward.restype = C.c_double
+    L.or_adamw.argtypes = [C.c_int, _dp, _dp, _dp, _dp, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
+                           C.c_double]
+
+
+def mpnn_param_count():
+    _declare_mpnn(lib())
+    return lib().or_mpnn_param_count()
+
+
+def mpnn_forward(rowptr, col, feat, theta, t=None):
+    _declare_mpnn(lib())
+    n = rowptr.size - 1
+    y = np.empty(n, D)
+    tt = None if t is None else _c(t, D)
+    loss = lib().or_mpnn_forward(n, _c(rowptr, I), _c(col, I), _c(feat, D), _c(theta, D), y,
+                                 None if tt is None else tt.ctypes.data_as(C.c_void_p))
+    return y, loss
+
+
+def mpnn_backward(rowptr, col, feat, theta, t):
+    _declare_mpnn(lib())
+    g = np.empty(mpnn_param_count(), D)
+    loss = lib().or_mpnn_backward(rowptr.size - 1, _c(rowptr, I), _c(col, I), _c(feat, D), _c(theta, D), _c(t, D), g)
+    return g, loss
+
+
+def adamw(theta, grad, m, v, step, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8, wd=0.01):
+    _declare_mpnn(lib())
+    lib().or_adamw(theta.size, theta, _c(grad, D), m, v, step, lr, b1, b2, eps, wd)

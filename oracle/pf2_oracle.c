@@ -1251,3 +1251,180 @@ void or_flow_get_matrix(const or_flow* f, int which, double* val, double* rhs)
     if (val) memcpy(val, f->A[which], sizeof(double) * f->nnz);
     if (rhs) memcpy(rhs, f->b[which], sizeof(double) * f->nv);
 }
+
+/* ------------------------------------------------------------------------- */
+/* Learned initial guess: the network of pf2_oracle.h (no reference counterpart). */
+#define MH OR_MPNN_H
+int or_mpnn_param_count(void) { return MH * OR_MPNN_IN + MH + OR_MPNN_LAYERS * (MH * 2 * MH + MH) + MH + 1; }
+
+typedef struct {
+    const double *W0, *c0, *W[OR_MPNN_LAYERS], *c[OR_MPNN_LAYERS], *w4, *c4;
+} mpnn_view;
+
+static mpnn_view mpnn_split(const double* th)
+{
+    mpnn_view v;
+    v.W0 = th; th += MH * OR_MPNN_IN;
+    v.c0 = th; th += MH;
+    for (int l = 0; l < OR_MPNN_LAYERS; ++l) { v.W[l] = th; th += MH * 2 * MH; v.c[l] = th; th += MH; }
+    v.w4 = th; th += MH;
+    v.c4 = th;
+    return v;
+}
+
+/* h[(l+1)][n][MH] for l = 0..LAYERS (h[0] after the encoder), m[l][n][MH], z0 and z[l] kept */
+typedef struct { double *h, *m, *z; } mpnn_acts;
+
+static void mpnn_fwd(int n, const int* rp, const int* col, const double* f, mpnn_view P, mpnn_acts* A, double* y)
+{
+    const int L = OR_MPNN_LAYERS;
+    double* h0 = A->h;
+    for (int i = 0; i < n; ++i)
+        for (int o = 0; o < MH; ++o) {
+            double s = P.c0[o];
+            for (int k = 0; k < OR_MPNN_IN; ++k) s += P.W0[o * OR_MPNN_IN + k] * f[i * OR_MPNN_IN + k];
+            A->z[i * MH + o] = s;
+            h0[i * MH + o] = s > 0 ? s : 0;
+        }
+    for (int l = 0; l < L; ++l) {
+        const double* hp = A->h + (size_t)l * n * MH;
+        double* hn = A->h + (size_t)(l + 1) * n * MH;
+        double* m = A->m + (size_t)l * n * MH;
+        double* z = A->z + (size_t)(l + 1) * n * MH;
+        for (int i = 0; i < n; ++i) {
+            int d = 0;
+            for (int o = 0; o < MH; ++o) m[i * MH + o] = 0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                if (col[k] == i) continue;
+                ++d;
+                for (int o = 0; o < MH; ++o) m[i * MH + o] += hp[col[k] * MH + o];
+            }
+            for (int o = 0; o < MH; ++o) m[i * MH + o] = d ? m[i * MH + o] / d : 0.0;
+        }
+        for (int i = 0; i < n; ++i)
+            for (int o = 0; o < MH; ++o) {
+                double s = P.c[l][o];
+                const double* w = P.W[l] + o * 2 * MH;
+                for (int k = 0; k < MH; ++k) s += w[k] * hp[i * MH + k] + w[MH + k] * m[i * MH + k];
+                z[i * MH + o] = s;
+                hn[i * MH + o] = hp[i * MH + o] + (s > 0 ? s : 0);
+            }
+    }
+    const double* hl = A->h + (size_t)L * n * MH;
+    for (int i = 0; i < n; ++i) {
+        double s = P.c4[0];
+        for (int o = 0; o < MH; ++o) s += P.w4[o] * hl[i * MH + o];
+        y[i] = s;
+    }
+}
+
+static mpnn_acts mpnn_alloc(int n)
+{
+    mpnn_acts A;
+    A.h = (double*)calloc((size_t)(OR_MPNN_LAYERS + 1) * n * MH, sizeof(double));
+    A.m = (double*)calloc((size_t)OR_MPNN_LAYERS * n * MH, sizeof(double));
+    A.z = (double*)calloc((size_t)(OR_MPNN_LAYERS + 1) * n * MH, sizeof(double));
+    return A;
+}
+
+static void mpnn_free(mpnn_acts* A) { free(A->h); free(A->m); free(A->z); }
+
+double or_mpnn_forward(int n, const int* rp, const int* col, const double* f, const double* th, double* y,
+                       const double* t)
+{
+    mpnn_acts A = mpnn_alloc(n);
+    mpnn_fwd(n, rp, col, f, mpnn_split(th), &A, y);
+    mpnn_free(&A);
+    double loss = 0.0;
+    if (t) {
+        for (int i = 0; i < n; ++i) loss += (y[i] - t[i]) * (y[i] - t[i]);
+        loss /= n;
+    }
+    return loss;
+}
+
+double or_mpnn_backward(int n, const int* rp, const int* col, const double* f, const double* th, const double* t,
+                        double* grad)
+{
+    const int L = OR_MPNN_LAYERS;
+    const mpnn_view P = mpnn_split(th);
+    memset(grad, 0, sizeof(double) * or_mpnn_param_count());
+    double* gW0 = grad;
+    double* gc0 = gW0 + MH * OR_MPNN_IN;
+    double* gW[OR_MPNN_LAYERS];
+    double* gc[OR_MPNN_LAYERS];
+    double* g = gc0 + MH;
+    for (int l = 0; l < L; ++l) { gW[l] = g; g += MH * 2 * MH; gc[l] = g; g += MH; }
+    double* gw4 = g;
+    double* gc4 = g + MH;
+    mpnn_acts A = mpnn_alloc(n);
+    double* y = (double*)malloc(sizeof(double) * n);
+    mpnn_fwd(n, rp, col, f, P, &A, y);
+    double loss = 0.0;
+    double* dh = (double*)calloc((size_t)n * MH, sizeof(double));
+    double* dm = (double*)calloc((size_t)n * MH, sizeof(double));
+    const double* hl = A.h + (size_t)L * n * MH;
+    for (int i = 0; i < n; ++i) {
+        const double r = y[i] - t[i];
+        loss += r * r;
+        const double dy = 2.0 * r / n;
+        gc4[0] += dy;
+        for (int o = 0; o < MH; ++o) { gw4[o] += dy * hl[i * MH + o]; dh[i * MH + o] = dy * P.w4[o]; }
+    }
+    for (int l = L - 1; l >= 0; --l) {
+        const double* hp = A.h + (size_t)l * n * MH;
+        const double* m = A.m + (size_t)l * n * MH;
+        const double* z = A.z + (size_t)(l + 1) * n * MH;
+        for (int i = 0; i < n; ++i)
+            for (int o = 0; o < MH; ++o) dm[i * MH + o] = 0.0;
+        /* dz = dh * [z > 0]; dW += dz [h; m]^T; [dh_self; dm] = W^T dz; dh (residual) stays */
+        double* dself = (double*)calloc((size_t)n * MH, sizeof(double));
+        for (int i = 0; i < n; ++i)
+            for (int o = 0; o < MH; ++o) {
+                const double dz = z[i * MH + o] > 0 ? dh[i * MH + o] : 0.0;
+                if (dz == 0.0) continue;
+                gc[l][o] += dz;
+                double* gw = gW[l] + o * 2 * MH;
+                const double* w = P.W[l] + o * 2 * MH;
+                for (int k = 0; k < MH; ++k) {
+                    gw[k] += dz * hp[i * MH + k];
+                    gw[MH + k] += dz * m[i * MH + k];
+                    dself[i * MH + k] += w[k] * dz;
+                    dm[i * MH + k] += w[MH + k] * dz;
+                }
+            }
+        /* m_i = mean_j h_j: h_j receives dm_i / d_i from each neighbour i */
+        for (int i = 0; i < n; ++i) {
+            int d = 0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) d += (col[k] != i);
+            if (!d) continue;
+            for (int k = rp[i]; k < rp[i + 1]; ++k) {
+                if (col[k] == i) continue;
+                for (int o = 0; o < MH; ++o) dself[col[k] * MH + o] += dm[i * MH + o] / d;
+            }
+        }
+        for (size_t q = 0; q < (size_t)n * MH; ++q) dh[q] += dself[q];
+        free(dself);
+    }
+    for (int i = 0; i < n; ++i)
+        for (int o = 0; o < MH; ++o) {
+            const double dz = A.z[i * MH + o] > 0 ? dh[i * MH + o] : 0.0;
+            gc0[o] += dz;
+            for (int k = 0; k < OR_MPNN_IN; ++k) gW0[o * OR_MPNN_IN + k] += dz * f[i * OR_MPNN_IN + k];
+        }
+    free(dh); free(dm); free(y);
+    mpnn_free(&A);
+    return loss / n;
+}
+
+/* AdamW (decoupled weight decay), bias-corrected; `step` counts from 1. */
+void or_adamw(int np, double* th, const double* g, double* m, double* v, int step, double lr, double b1, double b2,
+              double eps, double wd)
+{
+    const double c1 = 1.0 - pow(b1, step), c2 = 1.0 - pow(b2, step);
+    for (int k = 0; k < np; ++k) {
+        m[k] = b1 * m[k] + (1.0 - b1) * g[k];
+        v[k] = b2 * v[k] + (1.0 - b2) * g[k] * g[k];
+        th[k] -= lr * (m[k] / c1 / (sqrt(v[k] / c2) + eps) + wd * th[k]);
+    }
+}

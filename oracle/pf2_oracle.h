@@ -142,6 +142,27 @@ void or_prediction_bc(int nc, const int* tri, const double* area, const double* 
 int or_body_loads(int nc, const double* xy, const int* tri, const double* invJ, const int* edge_ids,
                   const or_params* p, const double* ux, const double* uy, const double* pres, double* cxcy);
 
+/* ---- learned initial guess: message-passing network (no reference counterpart) ----
+ * Graph: mesh nodes, edges = off-diagonal CSR entries (symmetric), d_i = #neighbours.
+ * features f_i (5): x, y, b, p^n, p^{n-1}, each already scaled by the caller.
+ *   h0 = relu(W0 f + c0)                       W0: 64x5   (row-major, [out][in])
+ *   l = 1..3: m_i = mean_{j in N(i)} h_j
+ *             h  = h + relu(Wl [h ; m] + cl)   Wl: 64x128
+ *   y_i = w4 . h_i + c4                        w4: 64
+ * Parameter vector order: W0, c0, (W1, c1), (W2, c2), (W3, c3), w4, c4.
+ * Loss L = (1/N) sum_i (y_i - t_i)^2.  or_mpnn_forward returns L (t may be NULL: y only);
+ * or_mpnn_backward writes dL/dtheta. */
+#define OR_MPNN_H 64
+#define OR_MPNN_IN 5
+#define OR_MPNN_LAYERS 3
+int or_mpnn_param_count(void);
+double or_mpnn_forward(int n, const int* rowptr, const int* col, const double* feat, const double* theta,
+                       double* y, const double* t);
+double or_mpnn_backward(int n, const int* rowptr, const int* col, const double* feat, const double* theta,
+                        const double* t, double* grad);
+void or_adamw(int np, double* theta, const double* grad, double* m, double* v, int step, double lr, double b1,
+              double b2, double eps, double wd);
+
 #ifdef __cplusplus
 }
 #endif
