@@ -67,6 +67,17 @@ __device__ __forceinline__ void eliminate_row(int i, int s, int len, const int* 
     }
 }
 
+// True when some column of row i (other than i) is a boundary node of bc: only such rows
+// need their matrix values in a right-hand-side-only assembly (for the elimination).
+__device__ __forceinline__ bool has_bc_column(int i, int s, int len, const int* __restrict__ col, const BcView& bc) {
+    if (!bc.node_to_bc) return false;
+    for (int k = 0; k < len; ++k) {
+        const int j = col[s + k];
+        if (j != i && bc.node_to_bc[j] >= 0) return true;
+    }
+    return false;
+}
+
 __device__ __forceinline__ bool boundary_row(int i, int s, int len, const int* __restrict__ col, double* __restrict__ val,
                                              double* __restrict__ rhs, const BcView& bc, bool matrix = true) {
     if (!bc.node_to_bc) return false;
@@ -145,8 +156,11 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
     const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, MATRIX);
     const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, MATRIX);
     if (bx && by) return;
+    // the matrix rows are needed when written, or for the elimination of boundary columns
+    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
     double v0[kMaxRow], v1[kMaxRow];
-    for (int k = 0; k < len; ++k) { v0[k] = 0.0; v1[k] = 0.0; }
+    if (need)
+        for (int k = 0; k < len; ++k) { v0[k] = 0.0; v1[k] = 0.0; }
     double r0 = 0.0, r1 = 0.0;
     const double visc = P.mu * P.dt;
     const double third = 1.0 / 3.0;
@@ -163,8 +177,10 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
             const double mass = P.rho * ((j == m) ? (1.0 / 6.0) : (1.0 / 12.0));
             const double xx = g[m].x * g[j].x, yy = g[m].y * g[j].y;
             const double xy_ = g[m].y * g[j].x, yx = g[m].x * g[j].y;
-            v0[p] += (mass + visc * (yy + 4.0 / 3.0 * xx)) * A;
-            v1[p] += (mass + visc * (xx + 4.0 / 3.0 * yy)) * A;
+            if (need) {
+                v0[p] += (mass + visc * (yy + 4.0 / 3.0 * xx)) * A;
+                v1[p] += (mass + visc * (xx + 4.0 / 3.0 * yy)) * A;
+            }
             c0 += mass * uxo[nj] - visc * (xy_ - 2.0 / 3.0 * yx) * uy[nj];
             c1 += mass * uyo[nj] - visc * (yx - 2.0 / 3.0 * xy_) * ux[nj];
             if (pold) {
@@ -187,8 +203,10 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 const int nj = vtx(t, j), p = (pos >> (10 * j)) & 1023;
-                v0[p] -= w * ((4.0 / 3.0) * g[j].x * nx + g[j].y * ny) * A;
-                v1[p] -= w * (g[j].x * nx + (4.0 / 3.0) * g[j].y * ny) * A;
+                if (need) {
+                    v0[p] -= w * ((4.0 / 3.0) * g[j].x * nx + g[j].y * ny) * A;
+                    v1[p] -= w * (g[j].x * nx + (4.0 / 3.0) * g[j].y * ny) * A;
+                }
                 c0 += w * uy[nj] * ((-2.0 / 3.0) * g[j].y * nx + g[j].x * ny);
                 c1 += w * ux[nj] * (g[j].y * nx + (-2.0 / 3.0) * g[j].x * ny);
             }
@@ -197,13 +215,13 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
         r1 += c1 * A;
     }
     if (!bx) {
-        eliminate_row(i, s, len, M.col, v0, r0, bcx);
+        if (need) eliminate_row(i, s, len, M.col, v0, r0, bcx);
         if (MATRIX)
             for (int k = 0; k < len; ++k) valx[s + k] = v0[k];
         rhsx[i] = r0;
     }
     if (!by) {
-        eliminate_row(i, s, len, M.col, v1, r1, bcy);
+        if (need) eliminate_row(i, s, len, M.col, v1, r1, bcy);
         if (MATRIX)
             for (int k = 0; k < len; ++k) valy[s + k] = v1[k];
         rhsy[i] = r1;
@@ -211,15 +229,18 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
 }
 
 // kIntegratePressureEquation, cases/Cylinder2D/main.cu:169-211
+template <bool MATRIX>
 __global__ void k_pressure(int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
                            const double* __restrict__ py, const double* __restrict__ pold, double* __restrict__ val,
                            double* __restrict__ rhs, BcView bc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const int s = M.rowptr[i], len = M.rowptr[i + 1] - s;
-    if (boundary_row(i, s, len, M.col, val, rhs, bc)) return;
+    if (boundary_row(i, s, len, M.col, val, rhs, bc, MATRIX)) return;
+    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bc);
     double v[kMaxRow];
-    for (int k = 0; k < len; ++k) v[k] = 0.0;
+    if (need)
+        for (int k = 0; k < len; ++k) v[k] = 0.0;
     double r = 0.0;
     const double fdiv = -P.rho / P.dt / 3.0;
     for (int q = M.inc_off[i]; q < M.inc_off[i + 1]; ++q) {
@@ -233,18 +254,20 @@ __global__ void k_pressure(int nv, RowMesh M, FlowCoef P, const double* __restri
         for (int j = 0; j < 3; ++j) {
             const int nj = vtx(t, j), p = (pos >> (10 * j)) & 1023;
             const double K = g[m].x * g[j].x + g[m].y * g[j].y;
-            v[p] += K * A;
+            if (need) v[p] += K * A;
             if (pold) cr += K * pold[nj];
             div += g[j].x * px[nj] + g[j].y * py[nj];
         }
         r += (cr + fdiv * div) * A;
     }
-    eliminate_row(i, s, len, M.col, v, r, bc);
-    for (int k = 0; k < len; ++k) val[s + k] = v[k];
+    if (need) eliminate_row(i, s, len, M.col, v, r, bc);
+    if (MATRIX)
+        for (int k = 0; k < len; ++k) val[s + k] = v[k];
     rhs[i] = r;
 }
 
 // kIntegrateVelocityCorrection, cases/Cylinder2D/main.cu:213-259
+template <bool MATRIX>
 __global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
                              const double* __restrict__ py, const double* __restrict__ pres,
                              const double* __restrict__ pold, double* __restrict__ valx, double* __restrict__ valy,
@@ -252,11 +275,13 @@ __global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __rest
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const int s = M.rowptr[i], len = M.rowptr[i + 1] - s;
-    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx);
-    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy);
+    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, MATRIX);
+    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, MATRIX);
     if (bx && by) return;
+    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
     double v[kMaxRow];
-    for (int k = 0; k < len; ++k) v[k] = 0.0;
+    if (need)
+        for (int k = 0; k < len; ++k) v[k] = 0.0;
     double r0 = 0.0, r1 = 0.0;
     const double gdt = P.dt / 3.0;
     for (int q = M.inc_off[i]; q < M.inc_off[i + 1]; ++q) {
@@ -270,7 +295,7 @@ __global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __rest
         for (int j = 0; j < 3; ++j) {
             const int nj = vtx(t, j), p = (pos >> (10 * j)) & 1023;
             const double mass = P.rho * ((j == m) ? (1.0 / 6.0) : (1.0 / 12.0));
-            v[p] += mass * A;
+            if (need) v[p] += mass * A;
             const double dp = pold ? (pres[nj] - pold[nj]) : pres[nj];
             c0 += mass * px[nj] - gdt * g[j].x * dp;
             c1 += mass * py[nj] - gdt * g[j].y * dp;
@@ -279,15 +304,18 @@ __global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __rest
         r1 += c1 * A;
     }
     double w[kMaxRow];
-    for (int k = 0; k < len; ++k) w[k] = v[k];
+    if (need)
+        for (int k = 0; k < len; ++k) w[k] = v[k];
     if (!bx) {
-        eliminate_row(i, s, len, M.col, v, r0, bcx);
-        for (int k = 0; k < len; ++k) valx[s + k] = v[k];
+        if (need) eliminate_row(i, s, len, M.col, v, r0, bcx);
+        if (MATRIX)
+            for (int k = 0; k < len; ++k) valx[s + k] = v[k];
         rhsx[i] = r0;
     }
     if (!by) {
-        eliminate_row(i, s, len, M.col, w, r1, bcy);
-        for (int k = 0; k < len; ++k) valy[s + k] = w[k];
+        if (need) eliminate_row(i, s, len, M.col, w, r1, bcy);
+        if (MATRIX)
+            for (int k = 0; k < len; ++k) valy[s + k] = w[k];
         rhsy[i] = r1;
     }
 }
@@ -408,18 +436,27 @@ pf2_status launch_prediction(const pf2_mesh* m, const FlowCoef& P, bool matrix, 
     return PF2_OK;
 }
 
-pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                            const double* pold, double* val, double* rhs, const pf2_bc* bc, cudaStream_t st) {
-    k_pressure<<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pold, val, rhs, bc_view(bc));
+    if (matrix)
+        k_pressure<true><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pold, val, rhs,
+                                                                   bc_view(bc));
+    else
+        k_pressure<false><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pold, val, rhs,
+                                                                    bc_view(bc));
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }
 
-pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                              const double* pres, const double* pold, double* valx, double* valy, double* rhsx,
                              double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st) {
-    k_correction<<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pres, pold, valx, valy,
-                                                          rhsx, rhsy, bc_view(bcx), bc_view(bcy));
+    if (matrix)
+        k_correction<true><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pres, pold, valx,
+                                                                     valy, rhsx, rhsy, bc_view(bcx), bc_view(bcy));
+    else
+        k_correction<false><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pres, pold, valx,
+                                                                      valy, rhsx, rhsy, bc_view(bcx), bc_view(bcy));
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }
@@ -517,7 +554,8 @@ pf2_status pf2_assemble_pressure(const pf2_mesh* m, const pf2_params* p, const d
     PF2_TRY(check_csr(m, A));
     PF2_TRY(check_bc(m, bc));
     PF2_REQUIRE(p && px && py && rhs, PF2_BAD_INPUT, "null argument");
-    return launch_pressure(m, FlowCoef{ p->rho, p->mu, p->dt }, px, py, pold, A->val.p, rhs, bc, as_stream(stream));
+    return launch_pressure(m, FlowCoef{ p->rho, p->mu, p->dt }, true, px, py, pold, A->val.p, rhs, bc,
+                           as_stream(stream));
 }
 
 pf2_status pf2_assemble_velocity_correction(const pf2_mesh* m, const pf2_params* p, const double* px,
@@ -529,8 +567,8 @@ pf2_status pf2_assemble_velocity_correction(const pf2_mesh* m, const pf2_params*
     PF2_TRY(check_bc(m, bcx));
     PF2_TRY(check_bc(m, bcy));
     PF2_REQUIRE(p && px && py && pres && rx && ry, PF2_BAD_INPUT, "null argument");
-    return launch_correction(m, FlowCoef{ p->rho, p->mu, p->dt }, px, py, pres, pold, Ax->val.p, Ay->val.p, rx, ry,
-                             bcx, bcy, as_stream(stream));
+    return launch_correction(m, FlowCoef{ p->rho, p->mu, p->dt }, true, px, py, pres, pold, Ax->val.p, Ay->val.p, rx,
+                             ry, bcx, bcy, as_stream(stream));
 }
 
 pf2_status pf2_prediction_bc_values(const pf2_mesh* m, const pf2_params* p, const pf2_bc* src, pf2_bc* dst,

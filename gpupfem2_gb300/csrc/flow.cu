@@ -33,6 +33,9 @@ struct pf2_flow {
     pf2_solver* cg_c = nullptr;
     Guess* guess = nullptr;
     long long steps_done = 0;
+    // the five matrices (and the pressure factors) do not change between steps: after
+    // the first step only the right-hand sides are assembled
+    bool assembled = false;
     DevBuf<double> guess_res;
     DevBuf<int> guess_used;
     PinnedBuf<double> h_guess_res;
@@ -175,25 +178,26 @@ pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
         // velocity prediction (:812-828): boundary values from the pressure gradient,
         // assembly with the Dirichlet rule, GMRES per component
         for (int k = 0; k < 2; ++k) PF2_TRY(launch_prediction_bc(F->mesh, K, F->bc[k], F->pbc[k], pr, pold, k, st));
-        PF2_TRY(launch_prediction(F->mesh, K, true, ux, uy, uxo, uyo, pold, F->A[0]->val.p, F->A[1]->val.p, F->b[0].p,
+        const bool mat = !F->assembled && it == 0;
+        PF2_TRY(launch_prediction(F->mesh, K, mat, ux, uy, uxo, uyo, pold, F->A[0]->val.p, F->A[1]->val.p, F->b[0].p,
                                   F->b[1].p, F->pbc[0], F->pbc[1], st));
         F->mark(st, PF2_PHASE_PREDICTION_ASSEMBLY);
-        PF2_TRY(solver_solve_async(F->gmres, F->A[0], px, F->b[0].p, &R[5 * it + 0], st));
-        PF2_TRY(solver_solve_async(F->gmres, F->A[1], py, F->b[1].p, &R[5 * it + 1], st));
+        PF2_TRY(solver_solve_async(F->gmres, F->A[0], px, F->b[0].p, &R[5 * it + 0], st, mat));
+        PF2_TRY(solver_solve_async(F->gmres, F->A[1], py, F->b[1].p, &R[5 * it + 1], st, true));
         F->mark(st, PF2_PHASE_PREDICTION_SOLVE);
         // pressure (:831-842)
-        PF2_TRY(launch_pressure(F->mesh, K, px, py, pold, F->A[2]->val.p, F->b[2].p, F->bc[2], st));
+        PF2_TRY(launch_pressure(F->mesh, K, mat, px, py, pold, F->A[2]->val.p, F->b[2].p, F->bc[2], st));
         F->mark(st, PF2_PHASE_PRESSURE_ASSEMBLY);
         if (F->guess && it == 0)
             PF2_TRY(guess_apply(F->guess, F->A[2], F->b[2].p, pr, nullptr, F->guess_res.p, F->guess_used.p, st));
-        PF2_TRY(solver_solve_async(F->cg_p, F->A[2], pr, F->b[2].p, &R[5 * it + 2], st));
+        PF2_TRY(solver_solve_async(F->cg_p, F->A[2], pr, F->b[2].p, &R[5 * it + 2], st, mat));
         F->mark(st, PF2_PHASE_PRESSURE_SOLVE);
         // velocity correction (:845-860)
-        PF2_TRY(launch_correction(F->mesh, K, px, py, pr, pold, F->A[3]->val.p, F->A[4]->val.p, F->b[3].p, F->b[4].p,
-                                  F->bc[0], F->bc[1], st));
+        PF2_TRY(launch_correction(F->mesh, K, mat, px, py, pr, pold, F->A[3]->val.p, F->A[4]->val.p, F->b[3].p,
+                                  F->b[4].p, F->bc[0], F->bc[1], st));
         F->mark(st, PF2_PHASE_CORRECTION_ASSEMBLY);
-        PF2_TRY(solver_solve_async(F->cg_c, F->A[3], ux, F->b[3].p, &R[5 * it + 3], st));
-        PF2_TRY(solver_solve_async(F->cg_c, F->A[4], uy, F->b[4].p, &R[5 * it + 4], st));
+        PF2_TRY(solver_solve_async(F->cg_c, F->A[3], ux, F->b[3].p, &R[5 * it + 3], st, true));
+        PF2_TRY(solver_solve_async(F->cg_c, F->A[4], uy, F->b[4].p, &R[5 * it + 4], st, true));
         F->mark(st, PF2_PHASE_CORRECTION_SOLVE);
     }
     // particle velocity correction (:863-865) and loads (:874-876)
@@ -205,6 +209,7 @@ pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
     if (F->guess)
         PF2_TRY(guess_train(F->guess, pr, F->steps_done < P.learn_steps ? P.learn_rate : 0.0f, st));
     ++F->steps_done;
+    F->assembled = true;
     if (F->tmax && F->tsteps < F->tmax) ++F->tsteps;
     PF2_CUDA(cudaMemcpyAsync(F->h_rec.p, F->rec.p, sizeof(SolveRecord) * kRecords, cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(F->h_loads.p, F->loads.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));

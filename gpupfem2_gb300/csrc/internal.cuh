@@ -12,9 +12,9 @@ struct FlowCoef {
 pf2_status launch_prediction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* ux, const double* uy,
                              const double* uxo, const double* uyo, const double* pold, double* valx, double* valy,
                              double* rhsx, double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st);
-pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                            const double* pold, double* val, double* rhs, const pf2_bc* bc, cudaStream_t st);
-pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, const double* px, const double* py,
+pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                              const double* pres, const double* pold, double* valx, double* valy, double* rhsx,
                              double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st);
 pf2_status launch_prediction_bc(const pf2_mesh* m, const FlowCoef& P, const pf2_bc* src, pf2_bc* dst,
@@ -40,8 +40,9 @@ struct SolveRecord {
     int status;
     int err;
 };
+// refactor = false reuses the preconditioner of the previous solve (same matrix values)
 pf2_status solver_solve_async(pf2_solver* s, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
-                              cudaStream_t st);
+                              cudaStream_t st, bool refactor = true);
 
 // Learned initial guess of the pressure solve (guess.cu).
 struct Guess;

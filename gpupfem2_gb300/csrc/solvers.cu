@@ -877,8 +877,8 @@ __global__ void k_record(const SolveOut* out, const int* err, SolveRecord* rec) 
 }
 
 pf2_status solver_solve_async(pf2_solver* S, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
-                              cudaStream_t st) {
-    PF2_TRY(factorize(S, A, st));
+                              cudaStream_t st, bool refactor) {
+    if (refactor || S->last != A) PF2_TRY(factorize(S, A, st));
     PF2_TRY(launch_solver(S, A, x, b, st));
     if (rec) {
         k_record<<<1, 1, 0, st>>>(S->out.p, S->err.p, rec);
