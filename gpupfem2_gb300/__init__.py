@@ -399,6 +399,9 @@ class FlowEngine:
     def step(self):
         _check(lib().pf2_flow_step(self.h, _stream()), "pf2_flow_step")
 
+    def set_graphs(self, enable):
+        _check(lib().pf2_flow_set_graphs(self.h, int(enable)), "pf2_flow_set_graphs")
+
     def info(self):
         info = StepInfo()
         _check(lib().pf2_flow_step_info(self.h, C.byref(info)), "pf2_flow_step_info")

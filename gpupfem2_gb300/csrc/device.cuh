@@ -31,14 +31,36 @@ __device__ __forceinline__ void global_to_local(double x, double y, const double
     l2 = __dsub_rn(__dsub_rn(1.0, l0), l1);
 }
 
-// GEOMETRY::isPointInsideUnitTriangle (geometry.cuh:37-46): NaN coordinates count as
-// inside, as with the reference's comparisons.
+// GEOMETRY::isPointInsideUnitTriangle (geometry.cuh:37-46): every coordinate in
+// [-2e-6, 1 + 2e-6].  The comparisons run on the IEEE bit patterns with integer
+// instructions (GB300 issues FP64 compares on its small FP64 pipe): for a double v,
+// v > hi (hi > 0) iff bits(v) > bits(hi) as signed 64-bit integers, and v < lo (lo < 0)
+// iff v is negative with |v| > |lo|, i.e. bits(v) < 0 and (bits(v) & ~sign) >
+// bits(|lo|).  Same result as the floating-point test for every non-NaN v (a NaN
+// coordinate, which only a degenerate cell produces, counts as outside here).
+__device__ __forceinline__ bool in_band(double v) {
+    const long long b = __double_as_longlong(v);
+    const long long hi = __double_as_longlong(1.0 + kDoubleMin);
+    const long long lo_mag = __double_as_longlong(kDoubleMin);
+    if (b >= 0) return b <= hi;
+    return (b & 0x7fffffffffffffffll) <= lo_mag;
+}
+
 __device__ __forceinline__ bool inside_unit(double l0, double l1, double l2) {
-    const double hi = 1.0 + kDoubleMin, lo = -kDoubleMin;
-    if (l0 > hi || l0 < lo) return false;
-    if (l1 > hi || l1 < lo) return false;
-    if (l2 > hi || l2 < lo) return false;
-    return true;
+    return in_band(l0) && in_band(l1) && in_band(l2);
+}
+
+// Conservative single-precision test used to skip cells: false only when the point is
+// outside the cell by more than 0.01 in some barycentric coordinate, far beyond the
+// FP32 rounding of these O(10) quantities, so it never rejects a cell the exact FP64
+// test would accept.
+__device__ __forceinline__ bool maybe_inside_f32(double x, double y, const double4_32a J, const double2 v3) {
+    const float dx = (float)(x - v3.x), dy = (float)(y - v3.y);
+    const float l0 = (float)J.x * dx + (float)J.z * dy;
+    const float l1 = (float)J.y * dx + (float)J.w * dy;
+    const float l2 = 1.0f - l0 - l1;
+    const float m = 0.01f;
+    return l0 > -m && l0 < 1.0f + m && l1 > -m && l1 < 1.0f + m && l2 > -m && l2 < 1.0f + m;
 }
 
 // sum_i L_i u(node_i) accumulated from 0.0 (particle_handler_2d.cu:62-66)

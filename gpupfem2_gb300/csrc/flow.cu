@@ -36,6 +36,12 @@ struct pf2_flow {
     // the five matrices (and the pressure factors) do not change between steps: after
     // the first step only the right-hand sides are assembled
     bool assembled = false;
+    // CUDA graphs of the step body, one per particle-buffer parity (the cell sort
+    // alternates two buffers); captured on the engine's own stream
+    bool use_graph = true;
+    cudaStream_t cs = nullptr;
+    cudaGraphExec_t gexec[2] = { nullptr, nullptr };
+    int glr[2] = { -1, -1 };
     DevBuf<double> guess_res;
     DevBuf<int> guess_used;
     PinnedBuf<double> h_guess_res;
@@ -63,6 +69,9 @@ struct pf2_flow {
     }
 
     ~pf2_flow() {
+        for (auto g : gexec)
+            if (g) cudaGraphExecDestroy(g);
+        if (cs) cudaStreamDestroy(cs);
         for (auto e : tev) cudaEventDestroy(e);
         if (done) cudaEventDestroy(done);
         for (auto* a : A) pf2_csr_destroy(a);
@@ -141,6 +150,7 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
         cudaMemset(F->guess_used.p, 0, sizeof(int)) != cudaSuccess)
         return fail(PF2_CUDA_ERROR);
     if (p->pressure_x0 == PF2_X0_LEARNED && (s = guess_create(mesh, &F->guess))) return fail(s);
+    if (cudaStreamCreateWithFlags(&F->cs, cudaStreamNonBlocking) != cudaSuccess) return fail(PF2_CUDA_ERROR);
     *out = F;
     return PF2_OK;
 }
@@ -157,9 +167,10 @@ pf2_status pf2_flow_seed(pf2_flow* F, void* stream) {
     return particles_correct(F->ph, F->f[0].p, F->f[1].p, nullptr, nullptr, st);
 }
 
-pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
-    PF2_REQUIRE(F, PF2_BAD_INPUT, "null flow");
-    cudaStream_t st = as_stream(stream);
+}  // extern "C"
+
+// The work of one step, enqueued on st (also what a graph capture records).
+static pf2_status step_body(pf2_flow* F, cudaStream_t st) {
     const pf2_params& P = F->P;
     const FlowCoef K{ P.rho, P.mu, P.dt };
     double *ux = F->f[0].p, *uy = F->f[1].p, *uxo = F->f[2].p, *uyo = F->f[3].p;
@@ -216,8 +227,59 @@ pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
     PF2_CUDA(cudaMemcpyAsync(F->h_np.p, particles_count_ptr(F->ph), sizeof(int), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(F->h_guess_res.p, F->guess_res.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(F->h_guess_used.p, F->guess_used.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    return PF2_OK;
+}
+
+extern "C" {
+
+pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
+    PF2_REQUIRE(F, PF2_BAD_INPUT, "null flow");
+    cudaStream_t st = as_stream(stream);
+    const bool learning = F->guess && F->steps_done < F->P.learn_steps;
+    // graphs replay identical work: from the second step on (matrices assembled), and
+    // not while phase timing records events
+    if (F->use_graph && F->assembled && F->tmax == 0) {
+        const int par = particles_parity(F->ph);
+        const long long steps0 = F->steps_done;
+        if (!F->gexec[par] || F->glr[par] != (int)learning) {
+            if (F->gexec[par]) cudaGraphExecDestroy(F->gexec[par]);
+            F->gexec[par] = nullptr;
+            PF2_CUDA(cudaStreamBeginCapture(F->cs, cudaStreamCaptureModeThreadLocal));
+            const pf2_status sb = step_body(F, F->cs);
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ec = cudaStreamEndCapture(F->cs, &graph);
+            cudaGetLastError();
+            F->steps_done = steps0;  // the capture did not run the step
+            particles_set_parity(F->ph, par);
+            cudaGraphExec_t ex = nullptr;
+            if (sb == PF2_OK && ec == cudaSuccess && graph &&
+                cudaGraphInstantiate(&ex, graph, 0) == cudaSuccess) {
+                F->gexec[par] = ex;
+                F->glr[par] = (int)learning;
+            } else {
+                cudaGetLastError();
+                F->use_graph = false;  // capture refused: launch eagerly from now on
+            }
+            if (graph) cudaGraphDestroy(graph);
+        }
+        if (F->gexec[par]) {
+            PF2_CUDA(cudaGraphLaunch(F->gexec[par], st));
+            particles_set_parity(F->ph, 1 - par);
+            ++F->steps_done;
+            PF2_CUDA(cudaEventRecord(F->done, st));
+            F->stepped = true;
+            return PF2_OK;
+        }
+    }
+    PF2_TRY(step_body(F, st));
     PF2_CUDA(cudaEventRecord(F->done, st));
     F->stepped = true;
+    return PF2_OK;
+}
+
+pf2_status pf2_flow_set_graphs(pf2_flow* F, int enable) {
+    PF2_REQUIRE(F, PF2_BAD_INPUT, "null flow");
+    F->use_graph = enable != 0;
     return PF2_OK;
 }
 

@@ -31,6 +31,9 @@ pf2_status particles_correct(pf2_particles* H, const double* ux, const double* u
 pf2_status particles_seed(pf2_particles* H, cudaStream_t st);
 pf2_status particles_status(pf2_particles* H, cudaStream_t st);
 const int* particles_count_ptr(const pf2_particles* H);
+// which of the two particle buffers holds the state (the cell sort alternates them)
+int particles_parity(const pf2_particles* H);
+void particles_set_parity(pf2_particles* H, int parity);
 
 // Device-side record of one solve: copies of the solver's result and error word.
 struct SolveRecord {

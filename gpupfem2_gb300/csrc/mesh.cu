@@ -129,10 +129,15 @@ __global__ void k_diag_and_pos(int nv, const int* __restrict__ rowptr, const int
         }
         return 1023;
     };
-    diag[i] = rs + find(i);
+    const int d = find(i);
+    diag[i] = rs + (d < kMaxRow ? d : 0);
+    if (d >= kMaxRow) atomicExch(err, (int)DEV_BAD_INPUT);
     for (int q = off[i]; q < off[i + 1]; ++q) {
         const int4 t = tri[inc[q] >> 2];
-        inc_pos[q] = find(t.x) | (find(t.y) << 10) | (find(t.z) << 20);
+        const int a = find(t.x), b = find(t.y), c = find(t.z);
+        // the assembly kernels index a per-thread row buffer with these positions
+        if (a >= kMaxRow || b >= kMaxRow || c >= kMaxRow) atomicExch(err, (int)DEV_BAD_INPUT);
+        inc_pos[q] = (a & 1023) | ((b & 1023) << 10) | ((c & 1023) << 20);
     }
 }
 

@@ -96,7 +96,10 @@ __global__ void __launch_bounds__(256) k_advect(const int* __restrict__ np_ptr, 
                 int found = -1;
                 for (int k = o; k < e; ++k) {
                     const int nb = M.nb_idx[k];
-                    global_to_local(x, y, M.invJ[nb], M.v3[nb], n0, n1, n2);
+                    const double4_32a J = M.invJ[nb];
+                    const double2 V = M.v3[nb];
+                    if (!maybe_inside_f32(x, y, J, V)) continue;
+                    global_to_local(x, y, J, V, n0, n1, n2);
                     if (inside_unit(n0, n1, n2)) { found = nb; break; }
                 }
                 if (found < 0) { lost = true; break; }
@@ -430,6 +433,8 @@ pf2_status particles_status(pf2_particles* H, cudaStream_t st) {
 }
 
 const int* particles_count_ptr(const pf2_particles* H) { return H->cnt.p; }
+int particles_parity(const pf2_particles* H) { return H->cur; }
+void particles_set_parity(pf2_particles* H, int parity) { H->cur = parity; }
 
 }  // namespace pf2
 

@@ -136,8 +136,10 @@ __device__ void tri_solve(const Csr& A, const Tri& T, int dir, const double* src
 
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
 // per warp in level order, lane 0 working through the row.
-__global__ void k_factor(Csr A, Tri T, const int* __restrict__ order, unsigned* ticket, int epoch, int* err) {
+__global__ void k_factor(Csr A, Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr,
+                         int* err) {
     const int lane = threadIdx.x & 31;
+    const int epoch = *epoch_ptr + 1;
     double* a = T.fact;
     while (true) {
         unsigned t = 0;
@@ -207,7 +209,7 @@ struct KArgs {
     double* partial;  // 4 arrays of gridDim doubles
     GridBarrier bar;
     Tri T;
-    int epoch_base;
+    const int* epoch;  // device counter: this launch uses epochs *epoch + 1 ..
     double tol;
     int maxit;
     int criterion;
@@ -245,9 +247,10 @@ __device__ __forceinline__ double grid_total(const double* part, double* sh) {
 
 // Preconditioner apply z = M^{-1} r over the rows of this block (Jacobi) or the whole
 // grid (ILU/IC; includes grid barriers).  `apply` counts the applies of this solve.
-__device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply) {
+__device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply,
+                              int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
-        const int ep = a.epoch_base + 2 * apply;
+        const int ep = ep_base + 2 * apply;
         tri_solve(a.A, a.T, 0, src, a.T.tmp, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
         tri_solve(a.A, a.T, 1, a.T.tmp, dst, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
@@ -260,6 +263,8 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
 
 // SolverCG::solve (linear_solver.cu:440-515).
 __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
+    // read before the first barrier, so before the counter can advance
+    const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[40];
     int r0, r1;
     row_range(a.A.n, r0, r1);
@@ -279,7 +284,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     __syncthreads();
     int apply = 0;
     if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
-    if (!precond_apply(a, a.r, a.z, r0, r1, apply++)) return;
+    if (!precond_apply(a, a.r, a.z, r0, r1, apply++, ep_base)) return;
     __syncthreads();
     double g = 0.0, bb = 0.0;
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
         }
         __syncthreads();
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
-        if (!precond_apply(a, a.r, a.z, r0, r1, apply++)) return;
+        if (!precond_apply(a, a.r, a.z, r0, r1, apply++, ep_base)) return;
         __syncthreads();
         double gn = 0.0, rn = 0.0;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -359,6 +364,8 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
 // (updateHcolumn :40-66), stop on |beta_k| < tol; x changes only on convergence.  With
 // m < maxit the Krylov space restarts every m iterations.
 __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
+    // read before the first barrier, so before the counter can advance
+    const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[40];
     __shared__ double cs[kMaxGmresSmem], sn[kMaxGmresSmem], beta[kMaxGmresSmem + 1], hcol[kMaxGmresSmem + 1];
     int r0, r1;
@@ -383,7 +390,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
         }
         __syncthreads();
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
-        if (!precond_apply(a, a.r, v0, r0, r1, apply++)) return;
+        if (!precond_apply(a, a.r, v0, r0, r1, apply++, ep_base)) return;
         __syncthreads();
         double s2 = 0.0;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -412,7 +419,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
             }
             __syncthreads();
             if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
-            if (!precond_apply(a, a.q, vkp, r0, r1, apply++)) return;
+            if (!precond_apply(a, a.q, vkp, r0, r1, apply++, ep_base)) return;
             __syncthreads();
             // h_ik = v_{k+1} . v_i, then v_{k+1} -= h_ik v_i, i = 0..k
             for (int i = 0; i <= k; ++i) {
@@ -506,6 +513,8 @@ __device__ __forceinline__ float row_times32(const Csr& A, const float* __restri
 // each inner solve A d = r is a Jacobi-preconditioned CG whose SpMV, preconditioner
 // and vector updates are FP32 and whose dot products accumulate FP32 products in FP64.
 __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
+    // read before the first barrier, so before the counter can advance
+    const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[40];
     int r0, r1;
     row_range(a.A.n, r0, r1);
@@ -614,9 +623,10 @@ __global__ void k_to_float(long long n, const double* __restrict__ a, float* __r
 }
 
 __global__ void k_precond_apply(KArgs a) {
+    const int ep_base = a.epoch ? *a.epoch : 0;
     int r0, r1;
     row_range(a.A.n, r0, r1);
-    precond_apply(a, a.r, a.z, r0, r1, 0);
+    precond_apply(a, a.r, a.z, r0, r1, 0, ep_base);
 }
 
 }  // namespace pf2
@@ -638,7 +648,7 @@ struct pf2_solver {
     DevBuf<float> val32, d32, r32, p32, q32, z32, invd32;
     DevBuf<int> fwd_order, bwd_order, lt_off, lt_row, lt_pos, done_f, done_b;
     DevBuf<unsigned> tickets;
-    int epoch = 0;
+    DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
 };
@@ -696,6 +706,8 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     PF2_CUDA(cudaMemcpy(S->lt_pos.p, lpos.data(), sizeof(int) * lpos.size(), cudaMemcpyHostToDevice));
     PF2_TRY(S->fact.alloc(nnz));
     PF2_TRY(S->tmp.alloc(n));
+    PF2_TRY(S->epoch.alloc(1));
+    PF2_CUDA(cudaMemset(S->epoch.p, 0, sizeof(int)));
     PF2_TRY(S->done_f.alloc(n));
     PF2_TRY(S->done_b.alloc(n));
     PF2_CUDA(cudaMemset(S->done_f.p, 0, sizeof(int) * n));
@@ -717,6 +729,8 @@ static bool uses_tri(const pf2_solver* S) {
 }
 
 // Preconditioner::initialize(A): ILU/IC factorise a copy of A's values.
+__global__ void k_epoch_advance(int* epoch, int delta) { *epoch += delta; }
+
 __global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __restrict__ diag, double* invd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) invd[i] = 1.0 / val[diag[i]];
@@ -732,11 +746,12 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     if (!uses_tri(S)) return PF2_OK;
     PF2_CUDA(cudaMemcpyAsync(S->fact.p, A->val.p, sizeof(double) * S->nnz, cudaMemcpyDeviceToDevice, st));
     PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned), st));
-    S->epoch += 1;
     Tri T = tri_of(S);
     const int nb = std::min(num_sms() * 8, (int)blocks_for(S->n, kSolverThreads / 32));
-    k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(csr_of(A), T, S->fwd_order.p, S->tickets.p, S->epoch,
+    k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(csr_of(A), T, S->fwd_order.p, S->tickets.p, S->epoch.p,
                                                           S->err.p);
+    PF2_LAUNCH_CHECK();
+    k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
     S->factored = true;
     return PF2_OK;
@@ -782,19 +797,25 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
                                                            : (S->opt.max_iterations + 2);
     if (uses_tri(S)) {
         PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
-        a.epoch_base = S->epoch;
-        S->epoch += 2 * applies + 2;
+        a.epoch = S->epoch.p;
     }
     PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
     PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
     void* args[] = { &a };
     if (precond_only) {
         PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, st);
+        if (uses_tri(S)) {
+            k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 4);
+            PF2_LAUNCH_CHECK();
+        }
         return PF2_OK;
     }
     void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
     PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, st);
-    (void)applies;
+    if (uses_tri(S)) {
+        k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 2 * applies + 2);
+        PF2_LAUNCH_CHECK();
+    }
     return PF2_OK;
 }
 

@@ -296,6 +296,9 @@ pf2_status pf2_flow_destroy(pf2_flow* f);
 /* seedParticles + initParticleVelocity of the zero initial field. */
 pf2_status pf2_flow_seed(pf2_flow* f, void* stream);
 pf2_status pf2_flow_step(pf2_flow* f, void* stream);
+/* From the second step on, pf2_flow_step replays the step as a CUDA graph captured on
+ * the engine's own stream (on by default; 0 launches every kernel each step). */
+pf2_status pf2_flow_set_graphs(pf2_flow* f, int enable);
 enum { PF2_FIELD_UX = 0, PF2_FIELD_UY = 1, PF2_FIELD_UX_OLD = 2, PF2_FIELD_UY_OLD = 3, PF2_FIELD_PRED_X = 4,
        PF2_FIELD_PRED_Y = 5, PF2_FIELD_P = 6, PF2_FIELD_P_OLD = 7 };
 pf2_status pf2_flow_field(pf2_flow* f, int which, double** device_ptr);
