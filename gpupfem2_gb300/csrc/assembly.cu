@@ -522,6 +522,7 @@ pf2_status pf2_params_default(pf2_params* p) {
     p->pressure_criterion = PF2_CRITERION_ABS;
     p->learn_steps = 500;
     p->learn_rate = 1e-3f;
+    p->pressure_ordering = PF2_ORDERING_NATURAL;
     return PF2_OK;
 }
 

@@ -131,9 +131,11 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.precond = p->pressure_precond;
     o.precision = p->pressure_precision;
     o.criterion = p->pressure_criterion;
+    o.ordering = p->pressure_ordering;
     if ((s = pf2_solver_create(F->A[2], &o, &F->cg_p))) return fail(s);
     o.precision = PF2_PRECISION_FP64;
     o.criterion = PF2_CRITERION_ABS;
+    o.ordering = PF2_ORDERING_NATURAL;
     o.precond = PF2_PRECOND_JACOBI;
     if ((s = pf2_solver_create(F->A[3], &o, &F->cg_c))) return fail(s);
     if ((s = F->rec.alloc(kRecords)) || (s = F->h_rec.alloc(kRecords)) || (s = F->loads.alloc(2)) ||

@@ -55,15 +55,22 @@ __global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__
 }
 
 // ------------------------------------------------------------ triangular data
+// The factors live on the pattern of B = P A P^T, where P is the identity (natural
+// order, as the reference) or a multicolour ordering; perm maps a row of B to the row of
+// A, iperm back.
 struct Tri {
     int kind;              // PF2_PRECOND_ILU or PF2_PRECOND_IC
-    const int* fwd_order;  // rows in forward level order
-    const int* bwd_order;  // rows in backward level order
+    Csr B;                 // pattern of the factors (val unused)
+    const int* perm;
+    const int* iperm;
+    const int* fwd_order;  // rows of B in forward level order
+    const int* bwd_order;  // rows of B in backward level order
     const int* lt_off;     // IC: rows of L^T (strictly upper), (row k, position of l_ki)
     const int* lt_row;
     const int* lt_pos;
-    double* fact;          // factor values on the CSR pattern
-    double* tmp;           // forward result
+    double* fact;          // factor values on the pattern of B
+    double* tmp;           // forward result (numbering of B)
+    double* outB;          // backward result (numbering of B)
     int* done_f;           // per-row epoch flags
     int* done_b;
     unsigned* tickets;     // one counter per (apply, direction)
@@ -86,9 +93,10 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err) 
 // counter, so every row a warp waits on was taken earlier by a running warp.
 // dir 0: forward  y = L^{-1} src (unit diagonal for ILU, l_ii for IC)
 // dir 1: backward dst = U^{-1} y (ILU) or L^{-T} y (IC)
-__device__ void tri_solve(const Csr& A, const Tri& T, int dir, const double* src, double* dst, unsigned* ticket,
-                          int epoch, int* err) {
+__device__ void tri_solve(const Tri& T, int dir, const double* src, double* dst, unsigned* ticket, int epoch,
+                          int* err) {
     const int lane = threadIdx.x & 31;
+    const Csr& A = T.B;
     int* done = dir == 0 ? T.done_f : T.done_b;
     const int* order = dir == 0 ? T.fwd_order : T.bwd_order;
     while (true) {
@@ -124,7 +132,8 @@ __device__ void tri_solve(const Csr& A, const Tri& T, int dir, const double* src
         sum = warp_sum(sum);
         if (!__all_sync(0xffffffffu, ok)) return;
         if (lane == 0) {
-            const double in = __ldcg(&src[i]);
+            // the forward solve reads the right-hand side in A's numbering
+            const double in = __ldcg(&src[dir == 0 ? T.perm[i] : i]);
             double v = in - sum;
             if (dir == 1 || T.kind == PF2_PRECOND_IC) v = v / __ldcg(&T.fact[A.diag[i]]);
             __stcg(&dst[i], v);
@@ -136,8 +145,8 @@ __device__ void tri_solve(const Csr& A, const Tri& T, int dir, const double* src
 
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
 // per warp in level order, lane 0 working through the row.
-__global__ void k_factor(Csr A, Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr,
-                         int* err) {
+__global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr, int* err) {
+    const Csr& A = T.B;
     const int lane = threadIdx.x & 31;
     const int epoch = *epoch_ptr + 1;
     double* a = T.fact;
@@ -251,10 +260,13 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
                               int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
         const int ep = ep_base + 2 * apply;
-        tri_solve(a.A, a.T, 0, src, a.T.tmp, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        tri_solve(a.T, 0, src, a.T.tmp, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve(a.A, a.T, 1, a.T.tmp, dst, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
-        return grid_sync(a.bar, gridDim.x);
+        tri_solve(a.T, 1, a.T.tmp, a.T.outB, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return false;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = __ldcg(&a.T.outB[a.T.iperm[i]]);
+        __syncthreads();
+        return true;
     }
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
         dst[i] = (a.precond == PF2_PRECOND_JACOBI) ? src[i] * a.invd[i] : src[i];
@@ -649,6 +661,9 @@ struct pf2_solver {
     DevBuf<int> fwd_order, bwd_order, lt_off, lt_row, lt_pos, done_f, done_b;
     DevBuf<unsigned> tickets;
     DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
+    DevBuf<int> brp, bcol, bdiag, bmap, perm, iperm;  // pattern of the factors and the ordering
+    DevBuf<double> outB;
+    int levels_fwd = 0, levels_bwd = 0, colors = 0;
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
 };
@@ -656,19 +671,59 @@ struct pf2_solver {
 static pf2_status build_tri_plan(pf2_solver* S) {
     const pf2_mesh* M = S->mesh;
     const int n = M->nv, nnz = M->nnz;
-    std::vector<int> rp(n + 1), col(nnz), dg(n);
+    std::vector<int> rp(n + 1), col(nnz);
     PF2_CUDA(cudaMemcpy(rp.data(), M->rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
     PF2_CUDA(cudaMemcpy(col.data(), M->col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
-    PF2_CUDA(cudaMemcpy(dg.data(), M->diag.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    // ordering: natural (the reference's) or greedy multicolour in natural order, rows
+    // of a colour kept in natural order
+    std::vector<int> perm(n), iperm(n);
+    if (S->opt.ordering == PF2_ORDERING_MULTICOLOR) {
+        std::vector<int> color(n, -1);
+        int nc = 0;
+        std::vector<char> used;
+        for (int i = 0; i < n; ++i) {
+            used.assign(nc + 1, 0);
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                if (col[k] < i) used[color[col[k]]] = 1;
+            int c = 0;
+            while (used[c]) ++c;
+            color[i] = c;
+            nc = std::max(nc, c + 1);
+        }
+        S->colors = nc;
+        std::vector<int> cnt(nc + 1, 0);
+        for (int i = 0; i < n; ++i) cnt[color[i] + 1]++;
+        for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
+        for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
+    } else {
+        for (int i = 0; i < n; ++i) perm[i] = i;
+    }
+    for (int r = 0; r < n; ++r) iperm[perm[r]] = r;
+    // pattern of B = P A P^T with the position in A of each entry
+    std::vector<int> brp(n + 1, 0), bcol(nnz), bmap(nnz), bdiag(n);
+    std::vector<std::pair<int, int>> row;
+    for (int r = 0; r < n; ++r) {
+        const int o = perm[r];
+        row.clear();
+        for (int k = rp[o]; k < rp[o + 1]; ++k) row.emplace_back(iperm[col[k]], k);
+        std::sort(row.begin(), row.end());
+        brp[r + 1] = brp[r] + (int)row.size();
+        for (size_t q = 0; q < row.size(); ++q) {
+            bcol[brp[r] + q] = row[q].first;
+            bmap[brp[r] + q] = row[q].second;
+            if (row[q].first == r) bdiag[r] = brp[r] + (int)q;
+        }
+    }
     // forward levels: 1 + max over the strictly lower entries
     std::vector<int> lev(n, 0);
     int nl = 0;
     for (int i = 0; i < n; ++i) {
         int l = 0;
-        for (int k = rp[i]; k < dg[i]; ++k) l = std::max(l, lev[col[k]] + 1);
+        for (int k = brp[i]; k < bdiag[i]; ++k) l = std::max(l, lev[bcol[k]] + 1);
         lev[i] = l;
         nl = std::max(nl, l + 1);
     }
+    S->levels_fwd = nl;
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
@@ -676,40 +731,52 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     PF2_CUDA(cudaMemcpy(S->fwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
     // backward levels: 1 + max over the strictly upper entries (the pattern is symmetric)
     std::fill(lev.begin(), lev.end(), 0);
+    nl = 0;
     for (int i = n - 1; i >= 0; --i) {
         int l = 0;
-        for (int k = dg[i] + 1; k < rp[i + 1]; ++k) l = std::max(l, lev[col[k]] + 1);
+        for (int k = bdiag[i] + 1; k < brp[i + 1]; ++k) l = std::max(l, lev[bcol[k]] + 1);
         lev[i] = l;
+        nl = std::max(nl, l + 1);
     }
+    S->levels_bwd = nl;
     for (int i = 0; i < n; ++i) order[i] = n - 1 - i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
     PF2_TRY(S->bwd_order.alloc(n));
     PF2_CUDA(cudaMemcpy(S->bwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    // rows of L^T: for each k, entries l_ki with i > k ... stored as (row i, position)
+    // rows of L^T: for each k, the entries l_ik with i > k as (row i, position in B)
     std::vector<int> off(n + 1, 0);
     for (int i = 0; i < n; ++i)
-        for (int k = rp[i]; k < dg[i]; ++k) off[col[k] + 1]++;
+        for (int k = brp[i]; k < bdiag[i]; ++k) off[bcol[k] + 1]++;
     for (int i = 0; i < n; ++i) off[i + 1] += off[i];
     std::vector<int> lrow(std::max(off[n], 1)), lpos(std::max(off[n], 1)), fill(off.begin(), off.end() - 1);
     for (int i = 0; i < n; ++i)
-        for (int k = rp[i]; k < dg[i]; ++k) {
-            const int c = col[k];
+        for (int k = brp[i]; k < bdiag[i]; ++k) {
+            const int c = bcol[k];
             lrow[fill[c]] = i;
             lpos[fill[c]] = k;
             fill[c]++;
         }
-    PF2_TRY(S->lt_off.alloc(n + 1));
-    PF2_TRY(S->lt_row.alloc(lrow.size()));
-    PF2_TRY(S->lt_pos.alloc(lpos.size()));
-    PF2_CUDA(cudaMemcpy(S->lt_off.p, off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-    PF2_CUDA(cudaMemcpy(S->lt_row.p, lrow.data(), sizeof(int) * lrow.size(), cudaMemcpyHostToDevice));
-    PF2_CUDA(cudaMemcpy(S->lt_pos.p, lpos.data(), sizeof(int) * lpos.size(), cudaMemcpyHostToDevice));
+    auto up = [&](DevBuf<int>& d, const std::vector<int>& h) -> pf2_status {
+        PF2_TRY(d.alloc(h.size()));
+        PF2_CUDA(cudaMemcpy(d.p, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice));
+        return PF2_OK;
+    };
+    PF2_TRY(up(S->lt_off, off));
+    PF2_TRY(up(S->lt_row, lrow));
+    PF2_TRY(up(S->lt_pos, lpos));
+    PF2_TRY(up(S->brp, brp));
+    PF2_TRY(up(S->bcol, bcol));
+    PF2_TRY(up(S->bdiag, bdiag));
+    PF2_TRY(up(S->bmap, bmap));
+    PF2_TRY(up(S->perm, perm));
+    PF2_TRY(up(S->iperm, iperm));
     PF2_TRY(S->fact.alloc(nnz));
     PF2_TRY(S->tmp.alloc(n));
-    PF2_TRY(S->epoch.alloc(1));
-    PF2_CUDA(cudaMemset(S->epoch.p, 0, sizeof(int)));
+    PF2_TRY(S->outB.alloc(n));
     PF2_TRY(S->done_f.alloc(n));
     PF2_TRY(S->done_b.alloc(n));
+    PF2_TRY(S->epoch.alloc(1));
+    PF2_CUDA(cudaMemset(S->epoch.p, 0, sizeof(int)));
     PF2_CUDA(cudaMemset(S->done_f.p, 0, sizeof(int) * n));
     PF2_CUDA(cudaMemset(S->done_b.p, 0, sizeof(int) * n));
     return PF2_OK;
@@ -720,8 +787,9 @@ static Csr csr_of(const pf2_csr* A) {
 }
 
 static Tri tri_of(pf2_solver* S) {
-    return Tri{ S->opt.precond, S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p,
-                S->fact.p, S->tmp.p, S->done_f.p, S->done_b.p, S->tickets.p };
+    return Tri{ S->opt.precond, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
+                S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
+                S->outB.p, S->done_f.p, S->done_b.p, S->tickets.p };
 }
 
 static bool uses_tri(const pf2_solver* S) {
@@ -730,6 +798,12 @@ static bool uses_tri(const pf2_solver* S) {
 
 // Preconditioner::initialize(A): ILU/IC factorise a copy of A's values.
 __global__ void k_epoch_advance(int* epoch, int delta) { *epoch += delta; }
+
+__global__ void k_gather_values(long long nnz, const double* __restrict__ val, const int* __restrict__ map,
+                                double* __restrict__ out) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x)
+        out[k] = val[map[k]];
+}
 
 __global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __restrict__ diag, double* invd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -744,12 +818,13 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
         return PF2_OK;
     }
     if (!uses_tri(S)) return PF2_OK;
-    PF2_CUDA(cudaMemcpyAsync(S->fact.p, A->val.p, sizeof(double) * S->nnz, cudaMemcpyDeviceToDevice, st));
+    k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, A->val.p,
+                                                                                           S->bmap.p, S->fact.p);
+    PF2_LAUNCH_CHECK();
     PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned), st));
     Tri T = tri_of(S);
     const int nb = std::min(num_sms() * 8, (int)blocks_for(S->n, kSolverThreads / 32));
-    k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(csr_of(A), T, S->fwd_order.p, S->tickets.p, S->epoch.p,
-                                                          S->err.p);
+    k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(T, S->fwd_order.p, S->tickets.p, S->epoch.p, S->err.p);
     PF2_LAUNCH_CHECK();
     k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
@@ -829,6 +904,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     PF2_REQUIRE(opt->precond >= PF2_PRECOND_NONE && opt->precond <= PF2_PRECOND_IC, PF2_BAD_INPUT,
                 "unknown preconditioner %d", opt->precond);
     PF2_REQUIRE(opt->max_iterations >= 0 && opt->tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
+    PF2_REQUIRE(opt->ordering == PF2_ORDERING_NATURAL || opt->ordering == PF2_ORDERING_MULTICOLOR, PF2_BAD_INPUT,
+                "unknown ordering %d", opt->ordering);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || opt->precond == PF2_PRECOND_JACOBI ||

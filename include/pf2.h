@@ -165,6 +165,7 @@ typedef struct pf2_params {
     int pressure_criterion;  /* PF2_CRITERION_* of the pressure solve */
     int learn_steps;         /* PF2_X0_LEARNED: train the network on the first learn_steps steps */
     float learn_rate;        /* AdamW learning rate of that training */
+    int pressure_ordering;   /* PF2_ORDERING_* of an ILU(0)/IC(0) pressure preconditioner */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -207,6 +208,9 @@ enum { PF2_CRITERION_ABS = 0,   /* CG: r^T z < tol^2; GMRES: |beta_k| < tol (the
        PF2_CRITERION_REL = 1 }; /* ||b - A x|| <= tol ||b|| */
 enum { PF2_PRECISION_FP64 = 0, PF2_PRECISION_MIXED = 1 };
 enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
+enum { PF2_ORDERING_NATURAL = 0,    /* ILU(0)/IC(0) on A as numbered (the reference's)     */
+       PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring: ~8 levels, a
+                                        different (weaker) preconditioner, parallel solves */
 
 typedef struct pf2_solver_options {
     int kind;          /* PF2_SOLVER_* */
@@ -217,6 +221,7 @@ typedef struct pf2_solver_options {
     int precision;     /* PF2_PRECISION_* (CG only; MIXED takes Jacobi or no preconditioner and
                           always stops on ||b - A x|| <= tol ||b||) */
     int restart;       /* GMRES Krylov dimension; 0 = max_iterations (no restart, as the reference) */
+    int ordering;      /* PF2_ORDERING_* of ILU(0)/IC(0) */
 } pf2_solver_options;
 
 typedef struct pf2_solve_info {

@@ -94,3 +94,61 @@ def test_mixed_precision_refinement_reaches_fp64_residual(cuda):
     info64 = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL).solve(A, x64, b)
     assert info64.converged == 1
     assert rel_err(xs, x64.cpu().numpy()) < 1e-6
+
+
+def _greedy_colour_perm(rp, col):
+    n = rp.size - 1
+    colour = -np.ones(n, int)
+    for i in range(n):
+        used = {colour[j] for j in col[rp[i]:rp[i + 1]] if j < i}
+        c = 0
+        while c in used:
+            c += 1
+        colour[i] = c
+    return np.argsort(colour, kind="stable"), colour.max() + 1
+
+
+@pytest.mark.parametrize("pc", ["ilu", "ic"])
+def test_multicolour_preconditioner_matches_oracle_on_the_permuted_matrix(cuda, pc):
+    m, A, rp, col, val, rhs = _system(32, 8)
+    perm, ncol = _greedy_colour_perm(rp, col)
+    assert ncol <= 10
+    iperm = np.empty_like(perm)
+    iperm[perm] = np.arange(perm.size)
+    # B = P A P^T as CSR with sorted columns
+    rows = []
+    for r in range(perm.size):
+        o = perm[r]
+        ent = sorted((iperm[col[k]], val[k]) for k in range(rp[o], rp[o + 1]))
+        rows.append(ent)
+    brp = np.zeros(perm.size + 1, np.int32)
+    brp[1:] = np.cumsum([len(e) for e in rows])
+    bcol = np.array([c for e in rows for c, _ in e], np.int32)
+    bval = np.array([v for e in rows for _, v in e])
+    f = O.ilu0(brp, bcol, bval) if pc == "ilu" else O.ic0(brp, bcol, bval)
+    src_b = np.ascontiguousarray(rhs[perm])
+    out_b, tmp = np.empty_like(src_b), np.empty_like(src_b)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    O.lib().or_precond_apply.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 7
+    O.lib().or_precond_apply(O.PRECOND[pc], perm.size, p(brp), p(bcol), p(f), None, p(src_b), p(out_b), p(tmp))
+    ref = out_b[iperm]
+    s = g.LinearSolver(A, "cg", pc, ordering=1)
+    s.setup(A)
+    src = torch.tensor(rhs, device="cuda")
+    dst = torch.empty_like(src)
+    s.apply_preconditioner(dst, src)
+    assert rel_err(dst.cpu().numpy(), ref) < 1e-12
+
+
+@pytest.mark.parametrize("pc", ["ilu", "ic"])
+def test_multicolour_solve_agrees_with_natural(cuda, pc):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    xs = []
+    for ordering in (0, 1):
+        x = torch.zeros_like(b)
+        info = g.LinearSolver(A, "cg", pc, tol=1e-10, maxit=2000, criterion=g.CRITERION_REL,
+                              ordering=ordering).solve(A, x, b)
+        assert info.converged == 1
+        xs.append(x.cpu().numpy())
+    assert rel_err(xs[1], xs[0]) < 1e-8
