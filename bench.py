@@ -159,6 +159,108 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def _timed(fn):
+    import torch
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record()
+    out = fn()
+    b.record()
+    torch.cuda.synchronize()
+    return out, a.elapsed_time(b)
+
+
+def study_solver(args):
+    """Pressure solve to a 1e-8 relative residual on the cylinder mesh and its 1:4
+    refinement: FP64 PCG (Jacobi, IC(0) multicolour) against the mixed-precision
+    refinement.  b = A x* with x* uniform in [-1, 1] (splitmix64 seed 0), x0 = 0."""
+    import torch
+    import gpupfem2_gb300 as g
+    out = []
+    xy, tri = mg.cylinder_channel()
+    meshes = [("cylinder_1M", xy, tri)]
+    if not args.quick:
+        x4, t4 = mg.refine_uniform(xy, tri, snap_circle=(0.2, 0.2, 0.05, 1e-3))
+        meshes.append(("cylinder_4M", x4, t4))
+    for name, mxy, mtri in meshes:
+        m = g.Mesh2D.from_arrays(mxy, mtri)
+        _, _, bp = mg.channel_boundary_nodes(mxy, 2.2, 0.41, 1.5, cylinder=(0.2, 0.2, 0.05))
+        A = g.SparseMatrixCSR(m)
+        p = g.default_params(rho=1.0, mu=1e-3, dt=5e-4)
+        x, yv = mxy[:, 0], mxy[:, 1]
+        px = torch.tensor(4 * 1.5 * yv * (0.41 - yv) / 0.41 ** 2, device="cuda")
+        py = torch.tensor(0.1 * np.sin(np.pi * x / 2.2), device="cuda")
+        rhs = torch.empty(m.nv, dtype=torch.float64, device="cuda")
+        g.assemble_pressure(m, p, px, py, None, A, rhs, g.DirichletBCs(m.nv, bp))
+        xs = torch.tensor(mg.uniform_pm1(0, m.nv), device="cuda")
+        b = torch.empty_like(xs)
+        g.spmv(A, xs, b)
+        rows = []
+        cases = [("fp64_jacobi", dict(precond="jacobi")),
+                 ("fp64_ic0_multicolour", dict(precond="ic", ordering=1)),
+                 ("mixed_jacobi", dict(precond="jacobi", precision=g.PRECISION_MIXED))]
+        for label, kw in cases:
+            s = g.LinearSolver(A, "cg", tol=1e-8, maxit=20000, criterion=g.CRITERION_REL, **kw)
+            x0 = torch.zeros_like(b)
+            s.solve(A, x0, b)  # warm-up (first launch, factorisation)
+            times = []
+            for _ in range(3):
+                x0 = torch.zeros_like(b)
+                info, ms = _timed(lambda: s.solve(A, x0, b))
+                times.append(ms)
+            r = torch.empty_like(b)
+            g.spmv(A, x0, r)
+            res = float(torch.linalg.norm(b - r) / torch.linalg.norm(b))
+            rows.append({"solver": label, "ms": statistics.median(times), "iterations": info.iterations,
+                         "outer": info.outer_iterations, "converged": info.converged, "rel_residual": res,
+                         "x_err": float(torch.linalg.norm(x0 - xs) / torch.linalg.norm(xs))})
+        out.append({"mesh": name, "nodes": m.nv, "nnz": A.nnz, "solvers": rows})
+    print(json.dumps({"study": "pressure_solver", "criterion": "||b - A x|| <= 1e-8 ||b||", "results": out}))
+
+
+def study_learned(args):
+    """Cylinder flow: the pressure solve of each step (1e-8 relative residual) with the
+    plain FP64 PCG against mixed precision alone and mixed precision with the learned
+    initial guess (trained online on the first --train steps, used afterwards)."""
+    import ctypes
+    import torch
+    import gpupfem2_gb300 as g
+    w, xy, tri, bu, bv, bp, prm = build_case("cylinder", 0)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
+    res = {}
+    variants = [("fp64_plain", dict(pressure_precision=0, pressure_x0=0)),
+                ("mixed", dict(pressure_precision=1, pressure_x0=0)),
+                ("mixed_learned", dict(pressure_precision=1, pressure_x0=1))]
+    L = g.lib()
+    for label, kw in variants:
+        prm2 = dict(prm, pressure_criterion=1, learn_steps=args.train, learn_rate=1e-3, **kw)
+        eng = g.FlowEngine(m, g.default_params(**prm2), bu, bv, bp, capacity_factor=2.0)
+        eng.seed()
+        for _ in range(args.train):
+            eng.step()
+        eng.info()
+        g._check(L.pf2_flow_enable_timing(eng.h, args.eval), "timing")
+        its, used = [], 0
+        for _ in range(args.eval):
+            eng.step()
+            inf = eng.info()
+            its.append(inf.it_pressure[0] + inf.it_pressure[1])
+            used += inf.guess_used
+        ph = (ctypes.c_double * 9)()
+        nst = ctypes.c_int()
+        g._check(L.pf2_flow_phase_times(eng.h, ph, ctypes.byref(nst)), "phase times")
+        res[label] = {"pressure_ms_per_step": ph[5] / max(nst.value, 1), "iterations_per_step": statistics.mean(its),
+                      "guess_used_steps": used}
+        del eng
+        torch.cuda.synchronize()
+    base = res["fp64_plain"]["pressure_ms_per_step"]
+    for v in res.values():
+        v["time_vs_fp64_plain"] = v["pressure_ms_per_step"] / base
+    print(json.dumps({"study": "learned_guess", "train_steps": args.train, "eval_steps": args.eval,
+                      "criterion": "||b - A x|| <= 1e-8 ||b||", "results": res}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,7 +271,16 @@ def main():
     ap.add_argument("--precond", type=int, default=None, help="pressure preconditioner override (0 J, 1 ILU, 2 IC)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--study", default=None, choices=["solver", "learned"])
+    ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--train", type=int, default=40)
+    ap.add_argument("--eval", type=int, default=40)
     args = ap.parse_args()
+    if args.study:
+        import torch
+        torch.cuda.set_device(0)
+        (study_solver if args.study == "solver" else study_learned)(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

@@ -179,7 +179,7 @@ class SparseMatrixCSR:
         self.rows, self.nnz = n.value, nnz.value
 
     def __del__(self):
-        if getattr(self, "h", None) and _lib is not None:
+        if getattr(self, "h", None) and _lib is not None and not getattr(self, "borrowed", False):
             _lib.pf2_csr_destroy(self.h)
             self.h = None
 
@@ -400,6 +400,18 @@ class FlowEngine:
 
     def step(self):
         _check(lib().pf2_flow_step(self.h, _stream()), "pf2_flow_step")
+
+    def system(self, which):
+        """(matrix, rhs device pointer) of one of the flow's systems (2 = pressure)."""
+        a, r = C.c_void_p(), C.c_void_p()
+        _check(lib().pf2_flow_system(self.h, int(which), C.byref(a), C.byref(r)), "pf2_flow_system")
+        A = SparseMatrixCSR.__new__(SparseMatrixCSR)
+        A.mesh, A.h = self.mesh, a
+        n, nnz = C.c_int(), C.c_int()
+        _check(lib().pf2_csr_sizes(a, C.byref(n), C.byref(nnz)), "pf2_csr_sizes")
+        A.rows, A.nnz = n.value, nnz.value
+        A.borrowed = True
+        return A, r.value
 
     def set_graphs(self, enable):
         _check(lib().pf2_flow_set_graphs(self.h, int(enable)), "pf2_flow_set_graphs")

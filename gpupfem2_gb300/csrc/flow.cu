@@ -340,6 +340,13 @@ pf2_status pf2_flow_set_boundary_values(pf2_flow* F, int which, const double* va
     return pf2_bc_set_values(F->bc[which], values, stream);
 }
 
+pf2_status pf2_flow_system(pf2_flow* F, int which, pf2_csr** A, double** rhs) {
+    PF2_REQUIRE(F && A && rhs && which >= 0 && which < 5, PF2_BAD_INPUT, "bad system request");
+    *A = F->A[which];
+    *rhs = F->b[which].p;
+    return PF2_OK;
+}
+
 pf2_status pf2_flow_particles(pf2_flow* F, pf2_particles** ph) {
     PF2_REQUIRE(F && ph, PF2_BAD_INPUT, "null argument");
     *ph = F->ph;

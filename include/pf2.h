@@ -311,6 +311,10 @@ pf2_status pf2_flow_field(pf2_flow* f, int which, double** device_ptr);
 pf2_status pf2_flow_download_field(pf2_flow* f, int which, double* host_dst);
 pf2_status pf2_flow_upload_field(pf2_flow* f, int which, const double* host_src);
 pf2_status pf2_flow_particles(pf2_flow* f, pf2_particles** ph);
+/* The flow's own systems (0 prediction x, 1 prediction y, 2 pressure, 3 correction x,
+ * 4 correction y) as assembled by the last step: matrix handle (owned by the flow) and
+ * device rhs pointer. */
+pf2_status pf2_flow_system(pf2_flow* f, int which, pf2_csr** A, double** rhs);
 /* New values for a Dirichlet set of the flow (0 velocity x, 1 velocity y, 2 pressure),
  * device double[n_bc] in the order the set was created with (a time-dependent inflow). */
 pf2_status pf2_flow_set_boundary_values(pf2_flow* f, int which, const double* values_dev, void* stream);
