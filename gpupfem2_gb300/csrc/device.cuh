@@ -119,15 +119,74 @@ __device__ __forceinline__ double block_sum(double v, double* sh /* >= 33 double
     return sh[32];
 }
 
+// Block-wide sums of NV values at once (fixed order); every thread gets the results.
+// sh holds at least 33 * NV doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum_n(double (&v)[NV], double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = warp_sum(v[j]);
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) sh[32 * j + w] = v[j];
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) {
+            double t = lane < nw ? sh[32 * j + lane] : 0.0;
+            t = warp_sum(t);
+            if (lane == 0) sh[32 * NV + j] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = sh[32 * NV + j];
+}
+
 // ------------------------------------------------------------ grid barrier
 // Barrier over all blocks of a cooperative launch (all blocks co-resident).  The wait is
-// bounded: after `limit` polls it records DEV_TIMEOUT in *err and returns, and callers
-// check *err after every barrier, so no block waits forever.
+// bounded: after `kBarrierPolls` polls it records DEV_TIMEOUT in *err (and where it gave up
+// in rec) and returns, and callers check the result after every barrier, so no block
+// waits forever.
 struct GridBarrier {
     unsigned int* count;  // zero-initialised
     unsigned int* gen;
     int* err;
+    double* part;  // 4 x gridDim per-block partial sums (grid_reduce)
+    double* tot;   // 4 grid totals (grid_reduce)
+    int* rec;      // where a wait gave up: {kind, a, b, c, d}, kind 0 = none
 };
+
+constexpr long long kBarrierPolls = 1ll << 24;
+constexpr long long kFlagPolls = 1ll << 21;
+
+// First timeout of a launch records its place (kind 1: grid barrier, 2: row flag).
+__device__ __forceinline__ void record_timeout(int* rec, int kind, int a, int b, int c, int d) {
+    if (rec && atomicCAS(&rec[0], 0, kind) == 0) {
+        rec[1] = a;
+        rec[2] = b;
+        rec[3] = c;
+        rec[4] = d;
+        __threadfence();
+    }
+}
+
+// Thread 0 waits until the barrier generation moves past g.
+__device__ __forceinline__ void wait_generation(const GridBarrier& b, unsigned g) {
+    volatile unsigned int* vgen = b.gen;
+    long long polls = 0;
+    while (*vgen == g) {
+        if (++polls > kBarrierPolls) {
+            atomicExch(b.err, (int)DEV_TIMEOUT);
+            record_timeout(b.rec, 1, (int)blockIdx.x, (int)g, (int)*(volatile unsigned*)b.count, 0);
+            break;
+        }
+        if (*(volatile int*)b.err != 0) break;
+    }
+    __threadfence();
+}
 
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks) {
     __syncthreads();
@@ -140,16 +199,63 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks
             __threadfence();
             atomicAdd(b.gen, 1u);
         } else {
-            long long polls = 0;
-            while (*vgen == g) {
-                if (++polls > (1ll << 26)) {  // ~ seconds
-                    atomicExch(b.err, (int)DEV_TIMEOUT);
-                    break;
-                }
-                if (*(volatile int*)b.err != 0) break;
-            }
+            wait_generation(b, g);
         }
+    }
+    __syncthreads();
+    return *(volatile int*)b.err == 0;
+}
+
+// Barrier fused with grid-wide sums of NV (<= 4) values: each block contributes its
+// block sums, the last block to arrive adds the per-block partials in block order
+// (the same order whichever block is last, so the totals are reproducible bit for bit)
+// and publishes the totals before it releases the barrier.  On return v holds the
+// totals in every thread of every block.  sh holds at least 33 * NV doubles.
+template <int NV>
+__device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV], double* sh) {
+    __shared__ double s_tot[4];
+    __shared__ int s_last;
+    __shared__ unsigned s_gen;
+    block_sum_n<NV>(v, sh);
+    const unsigned G = gridDim.x;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) __stcg(&b.part[j * G + blockIdx.x], v[j]);
+        volatile unsigned int* vgen = b.gen;
+        s_gen = *vgen;
         __threadfence();
+        s_last = (atomicAdd(b.count, 1u) == G - 1) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        double t[NV];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) t[j] = 0.0;
+        // thread k sums partials k, k + blockDim, ... in increasing order
+        for (unsigned k = threadIdx.x; k < G; k += blockDim.x) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) t[j] += __ldcg(&b.part[j * G + k]);
+        }
+        block_sum_n<NV>(t, sh);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) __stcg(&b.tot[j], t[j]);
+            *b.count = 0;
+            __threadfence();
+            atomicAdd(b.gen, 1u);
+        }
+#pragma unroll
+        for (int j = 0; j < NV; ++j) v[j] = t[j];
+    } else {
+        if (threadIdx.x == 0) {
+            wait_generation(b, s_gen);
+#pragma unroll
+            for (int j = 0; j < NV; ++j) s_tot[j] = __ldcg(&b.tot[j]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < NV; ++j) v[j] = s_tot[j];
     }
     __syncthreads();
     return *(volatile int*)b.err == 0;

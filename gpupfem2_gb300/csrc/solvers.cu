@@ -24,6 +24,8 @@ namespace pf2 {
 constexpr int kSolverThreads = 256;
 constexpr int kGroup = 8;  // lanes per row in SpMV
 constexpr int kMaxGmresSmem = 1024;
+constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
+constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
 
 struct Csr {
     int n;
@@ -71,16 +73,21 @@ struct Tri {
     double* fact;          // factor values on the pattern of B
     double* tmp;           // forward result (numbering of B)
     double* outB;          // backward result (numbering of B)
+    float* fact32;         // mixed precision: FP32 copies of the three above
+    float* tmp32;
+    float* outB32;
     int* done_f;           // per-row epoch flags
     int* done_b;
     unsigned* tickets;     // one counter per (apply, direction)
+    int* rec;              // where a wait gave up (GridBarrier::rec)
 };
 
-__device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err) {
+__device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, int* rec, int row, int dep) {
     long long polls = 0;
     while (*(volatile const int*)flag != epoch) {
-        if (++polls > (1ll << 24)) {
+        if (++polls > kFlagPolls) {
             atomicExch(err, (int)DEV_TIMEOUT);
+            record_timeout(rec, 2, row, dep, epoch, *(volatile const int*)flag);
             return false;
         }
         if (*(volatile int*)err != 0) return false;
@@ -93,7 +100,9 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err) 
 // counter, so every row a warp waits on was taken earlier by a running warp.
 // dir 0: forward  y = L^{-1} src (unit diagonal for ILU, l_ii for IC)
 // dir 1: backward dst = U^{-1} y (ILU) or L^{-T} y (IC)
-__device__ void tri_solve(const Tri& T, int dir, const double* src, double* dst, unsigned* ticket, int epoch,
+// V is double (the FP64 preconditioner) or float (the FP32 apply of the mixed solver).
+template <class V>
+__device__ void tri_solve(const Tri& T, int dir, const V* src, V* dst, const V* fact, unsigned* ticket, int epoch,
                           int* err) {
     const int lane = threadIdx.x & 31;
     const Csr& A = T.B;
@@ -105,37 +114,38 @@ __device__ void tri_solve(const Tri& T, int dir, const double* src, double* dst,
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= (unsigned)A.n) break;
         const int i = order[t];
-        double sum = 0.0;
+        V sum = V(0);
         bool ok = true;
         if (dir == 0) {
             const int s = A.rowptr[i], d = A.diag[i];
             for (int k = s + lane; k < d; k += 32) {
                 const int j = A.col[k];
-                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
-                sum += __ldcg(&T.fact[k]) * __ldcg(&dst[j]);
+                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
+                sum += __ldcg(&fact[k]) * __ldcg(&dst[j]);
             }
         } else if (T.kind == PF2_PRECOND_ILU) {
             const int d = A.diag[i], e = A.rowptr[i + 1];
             for (int k = d + 1 + lane; k < e; k += 32) {
                 const int j = A.col[k];
-                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
-                sum += __ldcg(&T.fact[k]) * __ldcg(&dst[j]);
+                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
+                sum += __ldcg(&fact[k]) * __ldcg(&dst[j]);
             }
         } else {
             const int s = T.lt_off[i], e = T.lt_off[i + 1];
             for (int k = s + lane; k < e; k += 32) {
                 const int j = T.lt_row[k];
-                if (!wait_flag(&done[j], epoch, err)) { ok = false; break; }
-                sum += __ldcg(&T.fact[T.lt_pos[k]]) * __ldcg(&dst[j]);
+                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
+                sum += __ldcg(&fact[T.lt_pos[k]]) * __ldcg(&dst[j]);
             }
         }
-        sum = warp_sum(sum);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
         if (!__all_sync(0xffffffffu, ok)) return;
         if (lane == 0) {
             // the forward solve reads the right-hand side in A's numbering
-            const double in = __ldcg(&src[dir == 0 ? T.perm[i] : i]);
-            double v = in - sum;
-            if (dir == 1 || T.kind == PF2_PRECOND_IC) v = v / __ldcg(&T.fact[A.diag[i]]);
+            const V in = __ldcg(&src[dir == 0 ? T.perm[i] : i]);
+            V v = in - sum;
+            if (dir == 1 || T.kind == PF2_PRECOND_IC) v = v / __ldcg(&fact[A.diag[i]]);
             __stcg(&dst[i], v);
             __threadfence();
             atomicExch(&done[i], epoch);
@@ -162,7 +172,7 @@ __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket,
         if (T.kind == PF2_PRECOND_ILU) {
             for (int kk = s; kk < d && ok; ++kk) {
                 const int k = A.col[kk];
-                if (!wait_flag(&T.done_f[k], epoch, err)) { ok = false; break; }
+                if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
                 const double aik = __ldcg(&a[kk]) / __ldcg(&a[A.diag[k]]);
                 __stcg(&a[kk], aik);
                 const int ks = A.diag[k] + 1, ke = A.rowptr[k + 1];
@@ -176,7 +186,7 @@ __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket,
         } else {
             for (int kk = s; kk < d && ok; ++kk) {
                 const int k = A.col[kk];
-                if (!wait_flag(&T.done_f[k], epoch, err)) { ok = false; break; }
+                if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
                 double sum = __ldcg(&a[kk]);
                 int p = s, q = A.rowptr[k];
                 const int qe = A.diag[k];
@@ -240,29 +250,15 @@ __device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
     r1 = min(n, r0 + chunk);
 }
 
-// Fixed-order grid sum of per-block partials `part` (already written) after a barrier.
-__device__ __forceinline__ double grid_total(const double* part, double* sh) {
-    double v = 0.0;
-    if (threadIdx.x < 32) {
-        for (int k = threadIdx.x; k < (int)gridDim.x; k += 32) v += __ldcg(&part[k]);
-        v = warp_sum(v);
-        if (threadIdx.x == 0) sh[32] = v;
-    }
-    __syncthreads();
-    v = sh[32];
-    __syncthreads();
-    return v;
-}
-
 // Preconditioner apply z = M^{-1} r over the rows of this block (Jacobi) or the whole
 // grid (ILU/IC; includes grid barriers).  `apply` counts the applies of this solve.
 __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply,
                               int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
         const int ep = ep_base + 2 * apply;
-        tri_solve(a.T, 0, src, a.T.tmp, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        tri_solve<double>(a.T, 0, src, a.T.tmp, a.T.fact, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve(a.T, 1, a.T.tmp, a.T.outB, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        tri_solve<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = __ldcg(&a.T.outB[a.T.iperm[i]]);
         __syncthreads();
@@ -273,18 +269,18 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
     return true;
 }
 
-// SolverCG::solve (linear_solver.cu:440-515).
+// SolverCG::solve (linear_solver.cu:440-515).  Per iteration: q = A p with p.q (one fused
+// barrier-reduction), x/r update, z = M^{-1} r with r.z (and r.r) (one fused
+// barrier-reduction), p = z + beta p (one barrier).
 __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
-    __shared__ double sh[40];
+    __shared__ double sh[kShDoubles];
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    double* P0 = a.partial;
-    double* P1 = a.partial + gridDim.x;
-    double* P2 = a.partial + 2 * gridDim.x;
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
+    const bool rel = a.criterion == PF2_CRITERION_REL;
     // Jacobi: inverse diagonal (PreconditionerJacobi::initialize, preconditioners.cu:3-14)
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
@@ -298,75 +294,71 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
     if (!precond_apply(a, a.r, a.z, r0, r1, apply++, ep_base)) return;
     __syncthreads();
-    double g = 0.0, bb = 0.0;
+    double red[3] = { 0.0, 0.0, 0.0 };  // r.z, b.b, r.r
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
         const double zi = __ldcg(&a.z[i]);
+        const double ri = a.r[i];
         a.p[i] = zi;
-        g += a.r[i] * zi;
-        bb += a.b[i] * a.b[i];
+        red[0] += ri * zi;
+        red[1] += a.b[i] * a.b[i];
+        red[2] += ri * ri;
     }
-    g = block_sum(g, sh);
-    bb = block_sum(bb, sh);
-    if (threadIdx.x == 0) { P0[blockIdx.x] = g; P2[blockIdx.x] = bb; }
-    if (!grid_sync(a.bar, gridDim.x)) return;
-    double gamma = grid_total(P0, sh);
-    const double bnorm = sqrt(grid_total(P2, sh));
+    if (!grid_reduce<3>(a.bar, red, sh)) return;
+    double gamma = red[0];
+    const double bnorm = sqrt(red[1]);
+    double rr = red[2];
     const double tol2 = a.tol * a.tol;
-    auto done_test = [&](double gm, double rr) {
-        return a.criterion == PF2_CRITERION_ABS ? (gm < tol2) : (sqrt(rr) <= a.tol * bnorm);
-    };
-    double rr = 0.0;
-    if (a.criterion == PF2_CRITERION_REL) {
-        double t = 0.0;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) t += a.r[i] * a.r[i];
-        t = block_sum(t, sh);
-        if (threadIdx.x == 0) P1[blockIdx.x] = t;
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        rr = grid_total(P1, sh);
-    }
+    auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
     int it = 0;
     bool conv = done_test(gamma, rr);
     while (!conv && it < a.maxit) {
         ++it;
-        double pq = 0.0;
+        double pq[1] = { 0.0 };
         for (int i = r0 + grp; i < r1; i += ngrp) {
             const double v = row_times(a.A, i, a.p, lane);
-            if (lane == 0) { a.q[i] = v; pq += a.p[i] * v; }
+            if (lane == 0) { a.q[i] = v; pq[0] += a.p[i] * v; }
         }
-        pq = block_sum(pq, sh);
-        if (threadIdx.x == 0) P1[blockIdx.x] = pq;
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        pq = grid_total(P1, sh);
-        const double alpha = gamma / pq;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            a.x[i] += alpha * a.p[i];
-            a.r[i] -= alpha * a.q[i];
+        if (!grid_reduce<1>(a.bar, pq, sh)) return;
+        const double alpha = gamma / pq[0];
+        double g2[2] = { 0.0, 0.0 };
+        if (global_pc) {
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                a.x[i] += alpha * a.p[i];
+                a.r[i] -= alpha * a.q[i];
+            }
+            __syncthreads();
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            if (!precond_apply(a, a.r, a.z, r0, r1, apply++, ep_base)) return;
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                const double ri = a.r[i];
+                g2[0] += ri * __ldcg(&a.z[i]);
+                g2[1] += ri * ri;
+            }
+        } else {
+            const bool jac = a.precond == PF2_PRECOND_JACOBI;
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                a.x[i] += alpha * a.p[i];
+                const double ri = a.r[i] - alpha * a.q[i];
+                const double zi = jac ? ri * a.invd[i] : ri;
+                a.r[i] = ri;
+                a.z[i] = zi;
+                g2[0] += ri * zi;
+                g2[1] += ri * ri;
+            }
         }
-        __syncthreads();
-        if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
-        if (!precond_apply(a, a.r, a.z, r0, r1, apply++, ep_base)) return;
-        __syncthreads();
-        double gn = 0.0, rn = 0.0;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            gn += a.r[i] * __ldcg(&a.z[i]);
-            if (a.criterion == PF2_CRITERION_REL) rn += a.r[i] * a.r[i];
-        }
-        gn = block_sum(gn, sh);
-        if (a.criterion == PF2_CRITERION_REL) rn = block_sum(rn, sh);
-        if (threadIdx.x == 0) { P0[blockIdx.x] = gn; P2[blockIdx.x] = rn; }
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        const double gnew = grid_total(P0, sh);
-        if (a.criterion == PF2_CRITERION_REL) rr = grid_total(P2, sh);
+        if (!grid_reduce<2>(a.bar, g2, sh)) return;
+        const double gnew = g2[0];
+        rr = g2[1];
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
         const double beta = gnew / gamma;
         gamma = gnew;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = __ldcg(&a.z[i]) + beta * a.p[i];
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = a.z[i] + beta * a.p[i];
         if (!grid_sync(a.bar, gridDim.x)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
-        a.out->residual = a.criterion == PF2_CRITERION_ABS ? sqrt(gamma) : sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -378,14 +370,12 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
 __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
-    __shared__ double sh[40];
+    __shared__ double sh[kShDoubles];
     __shared__ double cs[kMaxGmresSmem], sn[kMaxGmresSmem], beta[kMaxGmresSmem + 1], hcol[kMaxGmresSmem + 1];
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const int n = a.A.n;
     const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    double* P0 = a.partial;
-    double* P1 = a.partial + gridDim.x;
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
@@ -404,15 +394,13 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
         if (!precond_apply(a, a.r, v0, r0, r1, apply++, ep_base)) return;
         __syncthreads();
-        double s2 = 0.0;
+        double s2[1] = { 0.0 };
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const double vi = __ldcg(&v0[i]);
-            s2 += vi * vi;
+            s2[0] += vi * vi;
         }
-        s2 = block_sum(s2, sh);
-        if (threadIdx.x == 0) P0[blockIdx.x] = s2;
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        const double b0 = sqrt(grid_total(P0, sh));
+        if (!grid_reduce<1>(a.bar, s2, sh)) return;
+        const double b0 = sqrt(s2[0]);
         res = b0;
         if (b0 < a.tol) { conv = true; break; }
         if (total_it >= a.maxit) break;
@@ -436,27 +424,21 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
             // h_ik = v_{k+1} . v_i, then v_{k+1} -= h_ik v_i, i = 0..k
             for (int i = 0; i <= k; ++i) {
                 const double* vi = a.V + (size_t)i * n;
-                double d = 0.0;
-                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) d += __ldcg(&vkp[j]) * vi[j];
-                d = block_sum(d, sh);
-                double* P = (i & 1) ? P1 : P0;
-                if (threadIdx.x == 0) P[blockIdx.x] = d;
-                if (!grid_sync(a.bar, gridDim.x)) return;
-                const double h = grid_total(P, sh);
+                double d[1] = { 0.0 };
+                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) d[0] += __ldcg(&vkp[j]) * vi[j];
+                if (!grid_reduce<1>(a.bar, d, sh)) return;
+                const double h = d[0];
                 if (threadIdx.x == 0) hcol[i] = h;
                 for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) - h * vi[j];
                 __syncthreads();
             }
-            double nn = 0.0;
+            double nn[1] = { 0.0 };
             for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) {
                 const double v = __ldcg(&vkp[j]);
-                nn += v * v;
+                nn[0] += v * v;
             }
-            nn = block_sum(nn, sh);
-            double* P = ((k + 1) & 1) ? P1 : P0;
-            if (threadIdx.x == 0) P[blockIdx.x] = nn;
-            if (!grid_sync(a.bar, gridDim.x)) return;
-            const double aux = sqrt(grid_total(P, sh));
+            if (!grid_reduce<1>(a.bar, nn, sh)) return;
+            const double aux = sqrt(nn[0]);
             for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) / aux;
             if (threadIdx.x == 0) {
                 double* h = hcol;
@@ -520,96 +502,119 @@ __device__ __forceinline__ float row_times32(const Csr& A, const float* __restri
     return sum;
 }
 
+// FP32 preconditioner apply of the mixed solver: ILU(0)/IC(0) with the factors rounded
+// to FP32 (grid-wide, includes grid barriers) or Jacobi / none on this block's rows.
+__device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, int r0, int r1, int apply,
+                                int ep_base) {
+    if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
+        const int ep = ep_base + 2 * apply;
+        tri_solve<float>(a.T, 0, src, a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return false;
+        tri_solve<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return false;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = __ldcg(&a.T.outB32[a.T.iperm[i]]);
+        __syncthreads();
+        return true;
+    }
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = src[i] * a.invd32[i];
+    __syncthreads();
+    return true;
+}
+
 // Mixed-precision iterative refinement (no reference counterpart): the outer loop keeps
 // x, r = b - A x (FP64 SpMV), the update x += d and the test ||r|| <= tol ||b|| in FP64;
-// each inner solve A d = r is a Jacobi-preconditioned CG whose SpMV, preconditioner
-// and vector updates are FP32 and whose dot products accumulate FP32 products in FP64.
+// each inner solve A d = r is a preconditioned CG (Jacobi, ILU(0) or IC(0)) whose SpMV,
+// preconditioner apply and vector updates are FP32 and whose dot products accumulate
+// FP32 products in FP64.
 __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
-    __shared__ double sh[40];
+    __shared__ double sh[kShDoubles];
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    double* P0 = a.partial;
-    double* P1 = a.partial + gridDim.x;
-    double* P2 = a.partial + 2 * gridDim.x;
+    const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
         a.invd32[i] = (a.precond == PF2_PRECOND_JACOBI) ? (float)(1.0 / a.A.val[a.A.diag[i]]) : 1.0f;
-    double bb = 0.0;
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) bb += a.b[i] * a.b[i];
-    bb = block_sum(bb, sh);
-    if (threadIdx.x == 0) P2[blockIdx.x] = bb;
-    if (!grid_sync(a.bar, gridDim.x)) return;
-    const double bnorm = sqrt(grid_total(P2, sh));
-    int total = 0, outer = 0;
+    double bb[1] = { 0.0 };
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) bb[0] += a.b[i] * a.b[i];
+    if (!grid_reduce<1>(a.bar, bb, sh)) return;
+    const double bnorm = sqrt(bb[0]);
+    int total = 0, outer = 0, apply = 0;
     bool conv = false;
     double rnorm = 0.0;
     while (true) {
         // r = b - A x in FP64
-        double rr = 0.0;
+        double rr[1] = { 0.0 };
         for (int i = r0 + grp; i < r1; i += ngrp) {
             const double v = row_times(a.A, i, a.x, lane);
             if (lane == 0) {
                 const double ri = a.b[i] - v;
                 a.r[i] = ri;
-                rr += ri * ri;
+                rr[0] += ri * ri;
             }
         }
-        rr = block_sum(rr, sh);
-        if (threadIdx.x == 0) P0[blockIdx.x] = rr;
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        rnorm = sqrt(grid_total(P0, sh));
+        if (!grid_reduce<1>(a.bar, rr, sh)) return;
+        rnorm = sqrt(rr[0]);
         if (rnorm <= a.tol * bnorm) { conv = true; break; }
         if (outer >= a.max_outer || total >= a.maxit) break;
         ++outer;
-        // inner CG in FP32
-        double g = 0.0;
+        // inner CG in FP32: d = 0, r32 = r, z = M^{-1} r32, p = z
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            const float ri = (float)a.r[i];
-            const float zi = ri * a.invd32[i];
-            a.r32[i] = ri;
+            a.r32[i] = (float)a.r[i];
             a.d32[i] = 0.0f;
-            a.z32[i] = zi;
-            a.p32[i] = zi;
-            g += (double)ri * (double)zi;
         }
-        g = block_sum(g, sh);
-        if (threadIdx.x == 0) P1[blockIdx.x] = g;
-        if (!grid_sync(a.bar, gridDim.x)) return;
-        double gamma = grid_total(P1, sh);
+        __syncthreads();
+        if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+        if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
+        double g[1] = { 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const float zi = a.z32[i];
+            a.p32[i] = zi;
+            g[0] += (double)a.r32[i] * (double)zi;
+        }
+        if (!grid_reduce<1>(a.bar, g, sh)) return;
+        double gamma = g[0];
         const double target = a.inner_eta * rnorm;
         while (total < a.maxit) {
             ++total;
-            double pq = 0.0;
+            double pq[1] = { 0.0 };
             for (int i = r0 + grp; i < r1; i += ngrp) {
                 const float v = row_times32(a.A, a.val32, i, a.p32, lane);
                 if (lane == 0) {
                     a.q32[i] = v;
-                    pq += (double)a.p32[i] * (double)v;
+                    pq[0] += (double)a.p32[i] * (double)v;
                 }
             }
-            pq = block_sum(pq, sh);
-            if (threadIdx.x == 0) P0[blockIdx.x] = pq;
-            if (!grid_sync(a.bar, gridDim.x)) return;
-            pq = grid_total(P0, sh);
-            const float alpha = (float)(gamma / pq);
+            if (!grid_reduce<1>(a.bar, pq, sh)) return;
+            const float alpha = (float)(gamma / pq[0]);
             double gn = 0.0, rn = 0.0;
-            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-                a.d32[i] += alpha * a.p32[i];
-                const float ri = a.r32[i] - alpha * a.q32[i];
-                const float zi = ri * a.invd32[i];
-                a.r32[i] = ri;
-                a.z32[i] = zi;
-                gn += (double)ri * (double)zi;
-                rn += (double)ri * (double)ri;
+            if (global_pc) {
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    a.d32[i] += alpha * a.p32[i];
+                    const float ri = a.r32[i] - alpha * a.q32[i];
+                    a.r32[i] = ri;
+                    rn += (double)ri * (double)ri;
+                }
+                __syncthreads();
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gn += (double)a.r32[i] * (double)a.z32[i];
+            } else {
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    a.d32[i] += alpha * a.p32[i];
+                    const float ri = a.r32[i] - alpha * a.q32[i];
+                    const float zi = ri * a.invd32[i];
+                    a.r32[i] = ri;
+                    a.z32[i] = zi;
+                    gn += (double)ri * (double)zi;
+                    rn += (double)ri * (double)ri;
+                }
             }
-            gn = block_sum(gn, sh);
-            rn = block_sum(rn, sh);
-            if (threadIdx.x == 0) { P1[blockIdx.x] = gn; P2[blockIdx.x] = rn; }
-            if (!grid_sync(a.bar, gridDim.x)) return;
-            const double gnew = grid_total(P1, sh);
-            const double rin = sqrt(grid_total(P2, sh));
+            double g2[2] = { gn, rn };
+            if (!grid_reduce<2>(a.bar, g2, sh)) return;
+            const double gnew = g2[0];
+            const double rin = sqrt(g2[1]);
             if (rin <= target) break;
             const float beta = (float)(gnew / gamma);
             gamma = gnew;
@@ -652,6 +657,7 @@ struct pf2_solver {
     DevBuf<double> r, z, p, q, invd, partial, V, H;
     DevBuf<unsigned> bar;  // count, gen
     DevBuf<int> err;
+    DevBuf<int> rec;  // where a device wait gave up (5 ints)
     DevBuf<SolveOut> out;
     PinnedBuf<SolveOut> h_out;
     // ILU / IC
@@ -663,6 +669,7 @@ struct pf2_solver {
     DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
     DevBuf<int> brp, bcol, bdiag, bmap, perm, iperm;  // pattern of the factors and the ordering
     DevBuf<double> outB;
+    DevBuf<float> fact32, tmp32, outB32;  // mixed precision with ILU/IC
     int levels_fwd = 0, levels_bwd = 0, colors = 0;
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
@@ -789,7 +796,8 @@ static Csr csr_of(const pf2_csr* A) {
 static Tri tri_of(pf2_solver* S) {
     return Tri{ S->opt.precond, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
-                S->outB.p, S->done_f.p, S->done_b.p, S->tickets.p };
+                S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
+                S->rec.p };
 }
 
 static bool uses_tri(const pf2_solver* S) {
@@ -812,6 +820,12 @@ __global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __r
 
 static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     S->last = A;
+    const bool mixed = S->opt.precision == PF2_PRECISION_MIXED;
+    if (mixed) {
+        k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, A->val.p,
+                                                                                        S->val32.p);
+        PF2_LAUNCH_CHECK();
+    }
     if (S->opt.precond == PF2_PRECOND_JACOBI) {
         k_inv_diag<<<blocks_for(S->n), kThreads, 0, st>>>(S->n, A->val.p, A->mesh->diag.p, S->invd.p);
         PF2_LAUNCH_CHECK();
@@ -822,14 +836,31 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
                                                                                            S->bmap.p, S->fact.p);
     PF2_LAUNCH_CHECK();
     PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned), st));
+    PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
+    PF2_CUDA(cudaMemsetAsync(S->rec.p, 0, 5 * sizeof(int), st));
     Tri T = tri_of(S);
     const int nb = std::min(num_sms() * 8, (int)blocks_for(S->n, kSolverThreads / 32));
     k_factor<<<std::max(nb, 1), kSolverThreads, 0, st>>>(T, S->fwd_order.p, S->tickets.p, S->epoch.p, S->err.p);
     PF2_LAUNCH_CHECK();
     k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
+    if (mixed) {
+        k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fact.p,
+                                                                                        S->fact32.p);
+        PF2_LAUNCH_CHECK();
+    }
     S->factored = true;
     return PF2_OK;
+}
+
+// Upper bound of the preconditioner applies of one solve (each uses two tickets and two
+// row-flag epochs): CG one per iteration plus the first; mixed CG one per inner
+// iteration plus one per refinement; GMRES one per iteration plus two per restart.
+static int max_applies(const pf2_solver* S) {
+    const int it = S->opt.max_iterations;
+    if (S->opt.kind == PF2_SOLVER_GMRES) return it + 2 * (it / std::max(S->m, 1)) + 4;
+    if (S->opt.precision == PF2_PRECISION_MIXED) return it + kMaxOuter + 2;
+    return it + 2;
 }
 
 static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, const double* b, cudaStream_t st,
@@ -845,7 +876,8 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.q = S->q.p;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
-    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p };
+    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->partial.p + 4 * (size_t)S->blocks,
+                         S->rec.p };
     a.T = tri_of(S);
     a.tol = S->opt.tolerance;
     a.maxit = S->opt.max_iterations;
@@ -856,8 +888,6 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.m = S->m;
     const bool mixed = S->opt.precision == PF2_PRECISION_MIXED && !precond_only;
     if (mixed) {
-        k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, a.A.val, S->val32.p);
-        PF2_LAUNCH_CHECK();
         a.val32 = S->val32.p;
         a.d32 = S->d32.p;
         a.r32 = S->r32.p;
@@ -866,16 +896,16 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         a.z32 = S->z32.p;
         a.invd32 = S->invd32.p;
         a.inner_eta = 1e-4;
-        a.max_outer = 40;
+        a.max_outer = kMaxOuter;
     }
-    const int applies = (S->opt.kind == PF2_SOLVER_GMRES) ? (S->opt.max_iterations + 2 * (S->opt.max_iterations / std::max(S->m, 1)) + 4)
-                                                           : (S->opt.max_iterations + 2);
+    const int applies = max_applies(S);
     if (uses_tri(S)) {
         PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
         a.epoch = S->epoch.p;
     }
     PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
     PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
+    PF2_CUDA(cudaMemsetAsync(S->rec.p, 0, 5 * sizeof(int), st));
     void* args[] = { &a };
     if (precond_only) {
         PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, st);
@@ -908,9 +938,6 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
                 "unknown ordering %d", opt->ordering);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
-    PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || opt->precond == PF2_PRECOND_JACOBI ||
-                    opt->precond == PF2_PRECOND_NONE,
-                PF2_BAD_INPUT, "the mixed-precision solver takes Jacobi or no preconditioner");
     pf2_solver* S = new pf2_solver();
     S->opt = *opt;
     S->mesh = A->mesh;
@@ -929,8 +956,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     pf2_status s;
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
-        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
-        (s = S->err.alloc(1)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
+        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks + 4)) || (s = S->bar.alloc(2)) ||
+        (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
         return fail(s);
     if (mixed && ((s = S->val32.alloc(S->nnz)) || (s = S->d32.alloc(S->n)) || (s = S->r32.alloc(S->n)) ||
                   (s = S->p32.alloc(S->n)) || (s = S->q32.alloc(S->n)) || (s = S->z32.alloc(S->n)) ||
@@ -944,8 +971,9 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     }
     if (uses_tri(S)) {
         if ((s = build_tri_plan(S))) return fail(s);
-        const int applies = S->opt.max_iterations + 2 * (S->opt.max_iterations / std::max(S->m, 1)) + 4;
-        if ((s = S->tickets.alloc(2 * (size_t)applies + 2))) return fail(s);
+        if ((s = S->tickets.alloc(2 * (size_t)max_applies(S) + 2))) return fail(s);
+        if (mixed && ((s = S->fact32.alloc(S->nnz)) || (s = S->tmp32.alloc(S->n)) || (s = S->outB32.alloc(S->n))))
+            return fail(s);
     }
     *out = S;
     return PF2_OK;
@@ -997,16 +1025,21 @@ pf2_status pf2_solver_solve(pf2_solver* S, const pf2_csr* A, double* x, const do
     PF2_TRY(factorize(S, A, st));
     PF2_TRY(launch_solver(S, A, x, b, st));
     if (!info) return PF2_OK;
-    int err = 0;
+    int err = 0, rec[5] = { 0, 0, 0, 0, 0 };
     PF2_CUDA(cudaMemcpyAsync(S->h_out.p, S->out.p, sizeof(SolveOut), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(&err, S->err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(rec, S->rec.p, sizeof(rec), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaStreamSynchronize(st));
     info->iterations = S->h_out.p->iterations;
     info->converged = S->h_out.p->converged;
     info->residual = S->h_out.p->residual;
     info->outer_iterations = S->opt.precision == PF2_PRECISION_MIXED ? S->h_out.p->pad : 1;
     info->status = err ? err : S->h_out.p->status;
-    PF2_REQUIRE(err == 0, (pf2_status)err, "device-side wait timed out in the solver");
+    PF2_REQUIRE(err == 0, (pf2_status)err,
+                rec[0] == 1   ? "grid barrier timed out in the solver (block %d, generation %d, arrived %d)"
+                : rec[0] == 2 ? "row wait timed out in the solver (row %d waited for row %d, epoch %d, flag %d)"
+                              : "device-side wait timed out in the solver",
+                rec[1], rec[2], rec[3], rec[4]);
     if (!info->converged) {
         set_error("solver did not converge in %d iterations (residual %g)", info->iterations, info->residual);
         return PF2_NOT_CONVERGED;

@@ -77,14 +77,16 @@ def test_spmv(cuda):
     assert rel_err(y.cpu().numpy(), O.spmv(rp, col, val, x)) < 1e-14
 
 
-def test_mixed_precision_refinement_reaches_fp64_residual(cuda):
-    """FP32 inner CG inside FP64 iterative refinement reaches ||b - A x|| <= 1e-8 ||b||,
-    with the residual checked by the oracle's FP64 SpMV."""
+@pytest.mark.parametrize("pc,ordering", [("jacobi", 0), ("ic", 0), ("ilu", 0), ("ic", 1)])
+def test_mixed_precision_refinement_reaches_fp64_residual(cuda, pc, ordering):
+    """FP32 inner CG (FP32 Jacobi or FP32 ILU(0)/IC(0) factors) inside FP64 iterative
+    refinement reaches ||b - A x|| <= 1e-8 ||b||, with the residual checked by the
+    oracle's FP64 SpMV."""
     m, A, rp, col, val, rhs = _system(128, 32)
     b = torch.tensor(rhs, device="cuda")
     x = torch.zeros_like(b)
-    s = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL,
-                       precision=g.PRECISION_MIXED)
+    s = g.LinearSolver(A, "cg", pc, tol=1e-8, maxit=5000, criterion=g.CRITERION_REL,
+                       precision=g.PRECISION_MIXED, ordering=ordering)
     info = s.solve(A, x, b)
     assert info.converged == 1 and info.outer_iterations >= 2
     xs = x.cpu().numpy()
