@@ -48,7 +48,7 @@ class Params(C.Structure):
                 ("body_cx", C.c_double), ("body_cy", C.c_double),
                 ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int),
                 ("pressure_criterion", C.c_int), ("learn_steps", C.c_int), ("learn_rate", C.c_float),
-                ("pressure_ordering", C.c_int)]
+                ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int)]
 
 
 class MeshView(C.Structure):
@@ -64,7 +64,8 @@ class DirichletNode(C.Structure):
 
 class SolverOptions(C.Structure):
     _fields_ = [("kind", C.c_int), ("precond", C.c_int), ("tolerance", C.c_double), ("max_iterations", C.c_int),
-                ("criterion", C.c_int), ("precision", C.c_int), ("restart", C.c_int), ("ordering", C.c_int)]
+                ("criterion", C.c_int), ("precision", C.c_int), ("restart", C.c_int), ("ordering", C.c_int),
+                ("orthogonalization", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -275,7 +276,7 @@ class LinearSolver:
     preconditioner (preconditioners.cuh)."""
 
     def __init__(self, A: SparseMatrixCSR, kind="cg", precond="jacobi", tol=1e-8, maxit=1000,
-                 criterion=CRITERION_ABS, precision=PRECISION_FP64, restart=0, ordering=0):
+                 criterion=CRITERION_ABS, precision=PRECISION_FP64, restart=0, ordering=0, orthogonalization=0):
         o = SolverOptions()
         o.kind = SOLVER_GMRES if kind == "gmres" else SOLVER_CG
         o.precond = PRECOND[precond] if isinstance(precond, str) else int(precond)
@@ -285,6 +286,7 @@ class LinearSolver:
         o.precision = precision
         o.restart = restart
         o.ordering = ordering
+        o.orthogonalization = orthogonalization
         self.h = C.c_void_p()
         _check(lib().pf2_solver_create(A.h, C.byref(o), C.byref(self.h)), "pf2_solver_create")
 

@@ -125,9 +125,11 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.kind = PF2_SOLVER_GMRES;
     o.precond = PF2_PRECOND_JACOBI;
     o.restart = p->gmres_restart;
+    o.orthogonalization = p->gmres_orthogonalization;
     if ((s = pf2_solver_create(F->A[0], &o, &F->gmres))) return fail(s);
     o.kind = PF2_SOLVER_CG;
     o.restart = 0;
+    o.orthogonalization = PF2_GS_MODIFIED;
     o.precond = p->pressure_precond;
     o.precision = p->pressure_precision;
     o.criterion = p->pressure_criterion;

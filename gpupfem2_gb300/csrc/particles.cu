@@ -69,61 +69,80 @@ struct MeshRefs {
 
 // kAdvectParticles (:54-70) for every substep, the location of sortParticlesInCells
 // (:363-395, kernels :117-162) after each, and kCountParticlesInSubcells (:173-181).
+// Warps stride over the particles together so that the ranks of particles that land in
+// the same cell come from one atomic per cell and warp (the order of ranks is free: the
+// gather restores the old order).
 __global__ void __launch_bounds__(256) k_advect(const int* __restrict__ np_ptr, int substeps, double dts, Centers C,
                                                 MeshRefs M, const double* __restrict__ ux,
                                                 const double* __restrict__ uy, PState P, int* count, int* mask,
                                                 int* rank, int level, double step) {
     const int np = *np_ptr;
     const int ppc = level * level;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-        int cw = P.cw[p];
-        if (cw < 0) { rank[p] = -1; continue; }
-        int c = cw & kCellMask;
-        double l0 = P.l0[p], l1 = P.l1[p];
-        double l2 = third_coord(cw, l0, l1, C);
-        double x = P.x[p], y = P.y[p];
-        bool lost = false;
-        for (int s = 0; s < substeps; ++s) {
-            const int4 t = M.tri[c];
-            const double vx = interp3(l0, l1, l2, __ldg(&ux[t.x]), __ldg(&ux[t.y]), __ldg(&ux[t.z]));
-            const double vy = interp3(l0, l1, l2, __ldg(&uy[t.x]), __ldg(&uy[t.y]), __ldg(&uy[t.z]));
-            x = __fma_rn(vx, dts, x);
-            y = __fma_rn(vy, dts, y);
-            double n0, n1, n2;
-            global_to_local(x, y, M.invJ[c], M.v3[c], n0, n1, n2);
-            if (!inside_unit(n0, n1, n2)) {
-                const int o = M.nb_off[c], e = M.nb_off[c + 1];
-                int found = -1;
-                for (int k = o; k < e; ++k) {
-                    const int nb = M.nb_idx[k];
-                    const double4_32a J = M.invJ[nb];
-                    const double2 V = M.v3[nb];
-                    if (!maybe_inside_f32(x, y, J, V)) continue;
-                    global_to_local(x, y, J, V, n0, n1, n2);
-                    if (inside_unit(n0, n1, n2)) { found = nb; break; }
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long wb = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); wb < np; wb += stride) {
+        const int p = (int)(wb + lane);
+        int key = -1;  // cell the particle ends in, -1 if none
+        int sub = 0;
+        if (p < np) {
+            const int cw = P.cw[p];
+            if (cw >= 0) {
+                int c = cw & kCellMask;
+                double l0 = P.l0[p], l1 = P.l1[p];
+                double l2 = third_coord(cw, l0, l1, C);
+                double x = P.x[p], y = P.y[p];
+                bool lost = false;
+                for (int s = 0; s < substeps; ++s) {
+                    const int4 t = M.tri[c];
+                    const double vx = interp3(l0, l1, l2, __ldg(&ux[t.x]), __ldg(&ux[t.y]), __ldg(&ux[t.z]));
+                    const double vy = interp3(l0, l1, l2, __ldg(&uy[t.x]), __ldg(&uy[t.y]), __ldg(&uy[t.z]));
+                    x = __fma_rn(vx, dts, x);
+                    y = __fma_rn(vy, dts, y);
+                    double n0, n1, n2;
+                    global_to_local(x, y, M.invJ[c], M.v3[c], n0, n1, n2);
+                    if (!inside_unit(n0, n1, n2)) {
+                        const int o = M.nb_off[c], e = M.nb_off[c + 1];
+                        int found = -1;
+                        for (int k = o; k < e; ++k) {
+                            const int nb = M.nb_idx[k];
+                            const double4_32a J = M.invJ[nb];
+                            const double2 V = M.v3[nb];
+                            if (!maybe_inside_f32(x, y, J, V)) continue;
+                            global_to_local(x, y, J, V, n0, n1, n2);
+                            if (inside_unit(n0, n1, n2)) { found = nb; break; }
+                        }
+                        if (found < 0) { lost = true; break; }
+                        c = found;
+                    }
+                    l0 = n0;
+                    l1 = n1;
+                    l2 = n2;
                 }
-                if (found < 0) { lost = true; break; }
-                c = found;
+                P.x[p] = x;
+                P.y[p] = y;
+                P.l0[p] = l0;
+                P.l1[p] = l1;
+                if (lost) {
+                    P.cw[p] = -1;
+                } else {
+                    // a located particle loses its centroid flag; with no substeps it keeps it
+                    P.cw[p] = substeps > 0 ? c : cw;
+                    key = c;
+                    sub = determine_subcell(level, step, l0, l1, l2);
+                }
             }
-            l0 = n0;
-            l1 = n1;
-            l2 = n2;
         }
-        P.x[p] = x;
-        P.y[p] = y;
-        P.l0[p] = l0;
-        P.l1[p] = l1;
-        if (lost) {
-            P.cw[p] = -1;
-            rank[p] = -1;
-            continue;
+        // one atomic per (warp, cell); each lane's rank = group base + lanes below it
+        const unsigned grp = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(grp) - 1;
+        int base = 0;
+        if (lane == leader && key >= 0) base = atomicAdd(&count[key], __popc(grp));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (p < np) rank[p] = key >= 0 ? base + __popc(grp & ((1u << lane) - 1u)) : -1;
+        if (key >= 0) {
+            const int tc = key + sub / ppc;
+            if (tc < M.nc) atomicOr(&mask[tc], 1 << (sub % ppc));
         }
-        // a located particle loses its centroid flag; with no substeps it keeps it
-        P.cw[p] = substeps > 0 ? c : cw;
-        rank[p] = atomicAdd(&count[c], 1);
-        const int sub = determine_subcell(level, step, l0, l1, l2);
-        const int tc = c + sub / ppc;
-        if (tc < M.nc) atomicOr(&mask[tc], 1 << (sub % ppc));
     }
 }
 
@@ -182,66 +201,89 @@ __device__ __forceinline__ void add_partials(double acc[9], double l0, double l1
     acc[8] = __dadd_rn(acc[8], l2);
 }
 
-// Per cell: stable order, move, reseed (kAddParticlesToCell :197-236), partial sums.
+// Per cell, one warp: stable order, move, reseed (kAddParticlesToCell :197-236), partial
+// sums.  The cell's particles arrive in perm[s, s + n) in the order the atomics handed
+// out ranks; each lane ranks its particle by old index against all n (the old order is
+// the order the cell keeps), moves it to slot s + rank, then lanes fill the missing
+// sub-cells after them.  The nine partial sums are formed over the slots in a fixed
+// lane order after the moves, so they do not depend on the atomics' order.
 __global__ void __launch_bounds__(256) k_gather(int nc, const int* __restrict__ seg, int* count, int* mask,
-                                                int* perm, PState S, PState D, Centers C, int level, int reseed,
-                                                const double2* __restrict__ xy, const int4* __restrict__ tri,
-                                                const double* __restrict__ ux, const double* __restrict__ uy,
-                                                Partials part, long long cap, int* cnt) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c == 0) cnt[0] = cnt[1];
-    if (c >= nc) return;
+                                                const int* __restrict__ perm, PState S, PState D, Centers C,
+                                                int level, int reseed, const double2* __restrict__ xy,
+                                                const int4* __restrict__ tri, const double* __restrict__ ux,
+                                                const double* __restrict__ uy, Partials part, long long cap,
+                                                int* cnt) {
+    const int lane = threadIdx.x & 31;
+    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = cnt[1];
+    if (c >= nc) return;  // uniform over the warp
     const int ppc = level * level;
     const int s = seg[c], n = count[c];
-    const int m = mask[c];
-    count[c] = 0;
-    mask[c] = 0;
-    const int nadd = reseed ? ppc - __popc((unsigned)m & ((1u << ppc) - 1u)) : 0;
+    const unsigned m = (unsigned)mask[c];
+    __syncwarp();
+    if (lane == 0) {
+        count[c] = 0;
+        mask[c] = 0;
+    }
+    const unsigned full = (1u << ppc) - 1u;
+    const int nadd = reseed ? ppc - __popc(m & full) : 0;
     if ((long long)s + n + nadd > cap) return;
-    // restore the previous order of the cell's particles (the ranks came from atomics)
-    for (int a = s + 1; a < s + n; ++a) {
-        const int v = perm[a];
-        int b = a - 1;
-        while (b >= s && perm[b] > v) { perm[b + 1] = perm[b]; --b; }
-        perm[b + 1] = v;
+    // existing particles: lane handles entries base + lane of perm[s, s + n)
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        const int v = i < n ? perm[s + i] : 0x7fffffff;
+        int r = 0;
+        for (int cb = 0; cb < n; cb += 32) {
+            const int w = cb + lane < n ? perm[s + cb + lane] : 0x7fffffff;
+            const int lim = min(32, n - cb);
+            for (int j = 0; j < lim; ++j) r += (__shfl_sync(0xffffffffu, w, j) < v) ? 1 : 0;
+        }
+        if (i < n) {
+            const int o = s + r;
+            D.x[o] = S.x[v];
+            D.y[o] = S.y[v];
+            D.l0[o] = S.l0[v];
+            D.l1[o] = S.l1[v];
+            D.u[o] = S.u[v];
+            D.v[o] = S.v[v];
+            D.cw[o] = S.cw[v];
+        }
     }
-    double acc[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-    for (int k = 0; k < n; ++k) {
-        const int p = perm[s + k], o = s + k;
-        const int w = S.cw[p];
-        const double l0 = S.l0[p], l1 = S.l1[p], u = S.u[p], v = S.v[p];
-        D.x[o] = S.x[p];
-        D.y[o] = S.y[p];
-        D.l0[o] = l0;
-        D.l1[o] = l1;
-        D.u[o] = u;
-        D.v[o] = v;
-        D.cw[o] = w;
-        add_partials(acc, l0, l1, third_coord(w, l0, l1, C), u, v);
-    }
+    // reseed: the q-th missing sub-cell goes to slot s + n + q
     if (nadd) {
         const int4 t = tri[c];
         const double2 A = xy[t.x], B = xy[t.y], E = xy[t.z];
         const double u0 = ux[t.x], u1 = ux[t.y], u2 = ux[t.z];
         const double w0 = uy[t.x], w1 = uy[t.y], w2 = uy[t.z];
-        int j = 0;
-        for (int k = 0; k < ppc; ++k) {
-            if ((m >> k) & 1) continue;
-            const int o = s + n + j++;
+        const unsigned missing = ~m & full;
+        for (int q = lane; q < nadd; q += 32) {
+            const int k = (int)__fns(missing, 0, q + 1);
+            const int o = s + n + q;
             const double L0 = C.c[k][0], L1 = C.c[k][1], L2 = C.c[k][2];
-            const double u = interp3(L0, L1, L2, u0, u1, u2), v = interp3(L0, L1, L2, w0, w1, w2);
             D.x[o] = local_to_global(L0, L1, L2, A.x, B.x, E.x);
             D.y[o] = local_to_global(L0, L1, L2, A.y, B.y, E.y);
             D.l0[o] = L0;
             D.l1[o] = L1;
-            D.u[o] = u;
-            D.v[o] = v;
+            D.u[o] = interp3(L0, L1, L2, u0, u1, u2);
+            D.v[o] = interp3(L0, L1, L2, w0, w1, w2);
             D.cw[o] = c | ((k + 1) << kCellBits);
-            add_partials(acc, L0, L1, L2, u, v);
         }
     }
+    __syncwarp();
+    // partial sums over the cell's slots, lane j taking slots j, j + 32, ...
+    double acc[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+    const int tot = n + nadd;
+    for (int k = lane; k < tot; k += 32) {
+        const int o = s + k;
+        const int w = D.cw[o];
+        const double l0 = D.l0[o], l1 = D.l1[o];
+        add_partials(acc, l0, l1, third_coord(w, l0, l1, C), D.u[o], D.v[o]);
+    }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) part.s[(size_t)k * nc + c] = acc[k];
+    for (int k = 0; k < 9; ++k) {
+        const double v = warp_sum(acc[k]);
+        if (lane == k) part.s[(size_t)k * nc + c] = v;
+    }
 }
 
 // Partial sums of every cell from the current (cell-ordered) particles.
@@ -368,7 +410,8 @@ static pf2_status sort_cells(pf2_particles* H, bool ranked, bool reseed, const d
     k_scatter<<<particle_grid(), kThreads, 0, st>>>(H->cnt.p, H->cw[H->cur].p, H->rank.p, H->seg.p, H->perm.p, H->cap);
     PF2_LAUNCH_CHECK();
     const int nxt = 1 - H->cur;
-    k_gather<<<blocks_for(nc), kThreads, 0, st>>>(nc, H->seg.p, H->count.p, H->mask.p, H->perm.p, H->state(H->cur),
+    k_gather<<<blocks_for((long long)nc * 32, 256), 256, 0, st>>>(nc, H->seg.p, H->count.p, H->mask.p, H->perm.p,
+                                                                 H->state(H->cur),
                                                   H->state(nxt), H->C, H->level, reseed ? 1 : 0, M->xy.p, M->tri4.p,
                                                   ux, uy, Partials{ H->part.p, nc }, H->cap, H->cnt.p);
     PF2_LAUNCH_CHECK();

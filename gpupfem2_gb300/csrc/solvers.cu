@@ -96,60 +96,95 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, 
     return true;
 }
 
-// Sync-free triangular solve: warps take rows in level order from a shared ticket
-// counter, so every row a warp waits on was taken earlier by a running warp.
-// dir 0: forward  y = L^{-1} src (unit diagonal for ILU, l_ii for IC)
-// dir 1: backward dst = U^{-1} y (ILU) or L^{-T} y (IC)
+// "Not yet written" marker of the triangular-solve vectors: all bits set, a NaN that
+// arithmetic never produces (the GPU returns its canonical NaN), so a byte memset of
+// 0xff initialises a vector to it.
+template <class V> struct Pending;
+template <> struct Pending<double> {
+    using Bits = unsigned long long;
+    static constexpr Bits kBits = ~0ull;
+    __device__ static Bits bits(double v) { return (Bits)__double_as_longlong(v); }
+    __device__ static double marker() { return __longlong_as_double((long long)kBits); }
+};
+template <> struct Pending<float> {
+    using Bits = unsigned int;
+    static constexpr Bits kBits = ~0u;
+    __device__ static Bits bits(float v) { return (Bits)__float_as_uint(v); }
+    __device__ static float marker() { return __uint_as_float(kBits); }
+};
+
+// Value of row j of the vector being solved for, once its writer has stored it (bounded).
+template <class V>
+__device__ __forceinline__ bool wait_value(const V* dst, int j, V& out, int* err, int* rec, int row) {
+    long long polls = 0;
+    while (true) {
+        const V v = *(volatile const V*)&dst[j];
+        if (Pending<V>::bits(v) != Pending<V>::kBits) { out = v; return true; }
+        if (++polls > kFlagPolls) {
+            atomicExch(err, (int)DEV_TIMEOUT);
+            record_timeout(rec, 2, row, j, 0, 0);
+            return false;
+        }
+        if (*(volatile int*)err != 0) return false;
+    }
+}
+
+// Sync-free triangular solve, one row per lane: warps take 32 rows at a time in level
+// order from a shared ticket counter, so every row a lane waits on was taken earlier by a
+// running lane.  The vector solved for starts as all "pending" markers and a row's value
+// doubles as its completion flag (one 8-byte store, no fence, no separate flag).
+// dir 0: forward  tmp = L^{-1} src (unit diagonal for ILU, l_ii for IC), src in A's numbering
+// dir 1: backward dst = U^{-1} tmp (ILU) or L^{-T} tmp (IC); each row resets its tmp entry
+// to pending after reading it, ready for the next forward solve.
 // V is double (the FP64 preconditioner) or float (the FP32 apply of the mixed solver).
 template <class V>
-__device__ void tri_solve(const Tri& T, int dir, const V* src, V* dst, const V* fact, unsigned* ticket, int epoch,
-                          int* err) {
+__device__ void tri_solve(const Tri& T, int dir, V* src, V* dst, const V* fact, unsigned* ticket, int* err) {
     const int lane = threadIdx.x & 31;
     const Csr& A = T.B;
-    int* done = dir == 0 ? T.done_f : T.done_b;
     const int* order = dir == 0 ? T.fwd_order : T.bwd_order;
+    const bool ic = T.kind == PF2_PRECOND_IC;
     while (true) {
-        unsigned t = 0;
-        if (lane == 0) t = atomicAdd(ticket, 1u);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= (unsigned)A.n) break;
-        const int i = order[t];
-        V sum = V(0);
-        bool ok = true;
-        if (dir == 0) {
-            const int s = A.rowptr[i], d = A.diag[i];
-            for (int k = s + lane; k < d; k += 32) {
-                const int j = A.col[k];
-                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
-                sum += __ldcg(&fact[k]) * __ldcg(&dst[j]);
+        unsigned base = 0;
+        if (lane == 0) base = atomicAdd(ticket, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= (unsigned)A.n) break;
+        const unsigned t = base + lane;
+        if (t < (unsigned)A.n) {
+            const int i = __ldg(&order[t]);
+            int s, e;
+            const int* cols;
+            if (dir == 0) {
+                s = __ldg(&A.rowptr[i]);
+                e = __ldg(&A.diag[i]);
+                cols = A.col;
+            } else if (!ic) {
+                s = __ldg(&A.diag[i]) + 1;
+                e = __ldg(&A.rowptr[i + 1]);
+                cols = A.col;
+            } else {
+                s = __ldg(&T.lt_off[i]);
+                e = __ldg(&T.lt_off[i + 1]);
+                cols = T.lt_row;
             }
-        } else if (T.kind == PF2_PRECOND_ILU) {
-            const int d = A.diag[i], e = A.rowptr[i + 1];
-            for (int k = d + 1 + lane; k < e; k += 32) {
-                const int j = A.col[k];
-                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
-                sum += __ldcg(&fact[k]) * __ldcg(&dst[j]);
+            const V in = __ldcg(&src[dir == 0 ? __ldg(&T.perm[i]) : i]);
+            const V d = (dir == 1 || ic) ? __ldcg(&fact[__ldg(&A.diag[i])]) : V(1);
+            V sum = V(0);
+            bool ok = true;
+            for (int k = s; k < e; ++k) {
+                const int j = __ldg(&cols[k]);
+                const V f = __ldcg(&fact[(dir == 1 && ic) ? __ldg(&T.lt_pos[k]) : k]);
+                V xj;
+                if (!wait_value(dst, j, xj, err, T.rec, i)) { ok = false; break; }
+                sum += f * xj;
             }
-        } else {
-            const int s = T.lt_off[i], e = T.lt_off[i + 1];
-            for (int k = s + lane; k < e; k += 32) {
-                const int j = T.lt_row[k];
-                if (!wait_flag(&done[j], epoch, err, T.rec, i, j)) { ok = false; break; }
-                sum += __ldcg(&fact[T.lt_pos[k]]) * __ldcg(&dst[j]);
+            if (ok) {
+                V v = in - sum;
+                if (dir == 1 || ic) v = v / d;
+                __stcg(&dst[i], v);
+                if (dir == 1) __stcg(&src[i], Pending<V>::marker());
             }
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-        if (!__all_sync(0xffffffffu, ok)) return;
-        if (lane == 0) {
-            // the forward solve reads the right-hand side in A's numbering
-            const V in = __ldcg(&src[dir == 0 ? T.perm[i] : i]);
-            V v = in - sum;
-            if (dir == 1 || T.kind == PF2_PRECOND_IC) v = v / __ldcg(&fact[A.diag[i]]);
-            __stcg(&dst[i], v);
-            __threadfence();
-            atomicExch(&done[i], epoch);
-        }
+        if (*(volatile int*)err != 0) break;
     }
 }
 
@@ -237,6 +272,9 @@ struct KArgs {
     double* V;      // (m+1) x n
     double* H;      // m x m, column-major
     int m;          // Krylov dimension
+    int gs;         // PF2_GS_MODIFIED or PF2_GS_CLASSICAL_TWICE
+    double* vpart;  // (m + 1) x gridDim partial dots (classical Gram-Schmidt)
+    double* vtot;   // m + 1 totals
     // mixed precision
     const float* val32;   // FP32 copy of the matrix values
     float *d32, *r32, *p32, *q32, *z32, *invd32;
@@ -255,12 +293,15 @@ __device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
 __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply,
                               int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
-        const int ep = ep_base + 2 * apply;
-        tri_solve<double>(a.T, 0, src, a.T.tmp, a.T.fact, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        tri_solve<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, &a.T.tickets[2 * apply], a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        tri_solve<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, &a.T.tickets[2 * apply + 1], a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = __ldcg(&a.T.outB[a.T.iperm[i]]);
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const int k = a.T.iperm[i];
+            dst[i] = __ldcg(&a.T.outB[k]);
+            __stcg(&a.T.outB[k], Pending<double>::marker());
+        }
         __syncthreads();
         return true;
     }
@@ -363,6 +404,39 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     }
 }
 
+// out[i] = this block's part of w . V_i (rows r0..r1), i < K; warp q takes i = q, q + 8, ...
+__device__ __forceinline__ void block_dots(const double* V, int n, int K, const double* w, int r0, int r1,
+                                           double* out) {
+    const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wq; i < K; i += nw) {
+        const double* vi = V + (size_t)i * n;
+        double d = 0.0;
+        for (int j = r0 + lane; j < r1; j += 32) d += w[j] * vi[j];
+        d = warp_sum(d);
+        if (lane == 0) out[i] = d;
+    }
+    __syncthreads();
+}
+
+// Grid-wide sums of K per-block values (vals, shared memory), in two barriers: every
+// block stores its K partials, block b adds up values b, b + G, ... over the blocks in
+// block order, then every block reads the K totals back into vals.
+__device__ bool grid_reduce_vec(const KArgs& a, double* vals, int K, double* sh) {
+    const int G = gridDim.x;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) __stcg(&a.vpart[(size_t)k * G + blockIdx.x], vals[k]);
+    if (!grid_sync(a.bar, G)) return false;
+    for (int k = blockIdx.x; k < K; k += G) {
+        double t = 0.0;
+        for (int q = threadIdx.x; q < G; q += blockDim.x) t += __ldcg(&a.vpart[(size_t)k * G + q]);
+        t = block_sum(t, sh);
+        if (threadIdx.x == 0) __stcg(&a.vtot[k], t);
+    }
+    if (!grid_sync(a.bar, G)) return false;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) vals[k] = __ldcg(&a.vtot[k]);
+    __syncthreads();
+    return true;
+}
+
 // SolverGMRES::solve (linear_solver.cu:560-660): left-preconditioned GMRES, the
 // projections taken one after another on the updated vector, Givens rotations
 // (updateHcolumn :40-66), stop on |beta_k| < tol; x changes only on convergence.  With
@@ -372,6 +446,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[kShDoubles];
     __shared__ double cs[kMaxGmresSmem], sn[kMaxGmresSmem], beta[kMaxGmresSmem + 1], hcol[kMaxGmresSmem + 1];
+    __shared__ double h2[kMaxGmresSmem + 1];
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const int n = a.A.n;
@@ -421,16 +496,33 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
             if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
             if (!precond_apply(a, a.q, vkp, r0, r1, apply++, ep_base)) return;
             __syncthreads();
-            // h_ik = v_{k+1} . v_i, then v_{k+1} -= h_ik v_i, i = 0..k
-            for (int i = 0; i <= k; ++i) {
-                const double* vi = a.V + (size_t)i * n;
-                double d[1] = { 0.0 };
-                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) d[0] += __ldcg(&vkp[j]) * vi[j];
-                if (!grid_reduce<1>(a.bar, d, sh)) return;
-                const double h = d[0];
-                if (threadIdx.x == 0) hcol[i] = h;
-                for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) - h * vi[j];
+            if (a.gs == PF2_GS_CLASSICAL_TWICE) {
+                // h = V^T v_{k+1}, v_{k+1} -= V h, twice; the second pass's h is added
+                for (int pass = 0; pass < 2; ++pass) {
+                    double* hv = pass == 0 ? hcol : h2;
+                    block_dots(a.V, n, k + 1, vkp, r0, r1, hv);
+                    if (!grid_reduce_vec(a, hv, k + 1, sh)) return;
+                    for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) {
+                        double v = vkp[j];
+                        for (int i = 0; i <= k; ++i) v -= hv[i] * a.V[(size_t)i * n + j];
+                        vkp[j] = v;
+                    }
+                    __syncthreads();
+                }
+                for (int i = threadIdx.x; i <= k; i += blockDim.x) hcol[i] += h2[i];
                 __syncthreads();
+            } else {
+                // h_ik = v_{k+1} . v_i, then v_{k+1} -= h_ik v_i, i = 0..k (the reference's order)
+                for (int i = 0; i <= k; ++i) {
+                    const double* vi = a.V + (size_t)i * n;
+                    double d[1] = { 0.0 };
+                    for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) d[0] += __ldcg(&vkp[j]) * vi[j];
+                    if (!grid_reduce<1>(a.bar, d, sh)) return;
+                    const double h = d[0];
+                    if (threadIdx.x == 0) hcol[i] = h;
+                    for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) vkp[j] = __ldcg(&vkp[j]) - h * vi[j];
+                    __syncthreads();
+                }
             }
             double nn[1] = { 0.0 };
             for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) {
@@ -507,12 +599,15 @@ __device__ __forceinline__ float row_times32(const Csr& A, const float* __restri
 __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, int r0, int r1, int apply,
                                 int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
-        const int ep = ep_base + 2 * apply;
-        tri_solve<float>(a.T, 0, src, a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply], ep + 1, a.bar.err);
+        tri_solve<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply], a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, &a.T.tickets[2 * apply + 1], ep + 2, a.bar.err);
+        tri_solve<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, &a.T.tickets[2 * apply + 1], a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return false;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) dst[i] = __ldcg(&a.T.outB32[a.T.iperm[i]]);
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const int k = a.T.iperm[i];
+            dst[i] = __ldcg(&a.T.outB32[k]);
+            __stcg(&a.T.outB32[k], Pending<float>::marker());
+        }
         __syncthreads();
         return true;
     }
@@ -654,7 +749,7 @@ struct pf2_solver {
     pf2_solver_options opt{};
     const pf2_mesh* mesh = nullptr;
     int n = 0, nnz = 0, blocks = 0, m = 0;
-    DevBuf<double> r, z, p, q, invd, partial, V, H;
+    DevBuf<double> r, z, p, q, invd, partial, V, H, vpart;
     DevBuf<unsigned> bar;  // count, gen
     DevBuf<int> err;
     DevBuf<int> rec;  // where a device wait gave up (5 ints)
@@ -886,6 +981,9 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.V = S->V.p;
     a.H = S->H.p;
     a.m = S->m;
+    a.gs = S->opt.orthogonalization;
+    a.vpart = S->vpart.p;
+    a.vtot = S->vpart.p ? S->vpart.p + (size_t)(S->m + 1) * S->blocks : nullptr;
     const bool mixed = S->opt.precision == PF2_PRECISION_MIXED && !precond_only;
     if (mixed) {
         a.val32 = S->val32.p;
@@ -901,6 +999,13 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     const int applies = max_applies(S);
     if (uses_tri(S)) {
         PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
+        // triangular-solve vectors start as "pending" (all bits set)
+        PF2_CUDA(cudaMemsetAsync(S->tmp.p, 0xff, S->tmp.bytes(), st));
+        PF2_CUDA(cudaMemsetAsync(S->outB.p, 0xff, S->outB.bytes(), st));
+        if (S->tmp32.p) {
+            PF2_CUDA(cudaMemsetAsync(S->tmp32.p, 0xff, S->tmp32.bytes(), st));
+            PF2_CUDA(cudaMemsetAsync(S->outB32.p, 0xff, S->outB32.bytes(), st));
+        }
         a.epoch = S->epoch.p;
     }
     PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
@@ -936,6 +1041,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     PF2_REQUIRE(opt->max_iterations >= 0 && opt->tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
     PF2_REQUIRE(opt->ordering == PF2_ORDERING_NATURAL || opt->ordering == PF2_ORDERING_MULTICOLOR, PF2_BAD_INPUT,
                 "unknown ordering %d", opt->ordering);
+    PF2_REQUIRE(opt->orthogonalization == PF2_GS_MODIFIED || opt->orthogonalization == PF2_GS_CLASSICAL_TWICE,
+                PF2_BAD_INPUT, "unknown orthogonalization %d", opt->orthogonalization);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
     pf2_solver* S = new pf2_solver();
@@ -968,6 +1075,9 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
         m = std::max(1, std::min(m, std::min(S->opt.max_iterations, kMaxGmresSmem - 1)));
         S->m = m;
         if ((s = S->V.alloc((size_t)(m + 1) * S->n)) || (s = S->H.alloc((size_t)m * m))) return fail(s);
+        if (opt->orthogonalization == PF2_GS_CLASSICAL_TWICE &&
+            (s = S->vpart.alloc((size_t)(m + 1) * (S->blocks + 1))))
+            return fail(s);
     }
     if (uses_tri(S)) {
         if ((s = build_tri_plan(S))) return fail(s);

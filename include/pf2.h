@@ -166,6 +166,7 @@ typedef struct pf2_params {
     int learn_steps;         /* PF2_X0_LEARNED: train the network on the first learn_steps steps */
     float learn_rate;        /* AdamW learning rate of that training */
     int pressure_ordering;   /* PF2_ORDERING_* of an ILU(0)/IC(0) pressure preconditioner */
+    int gmres_orthogonalization; /* PF2_GS_* of the prediction GMRES */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -211,6 +212,8 @@ enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
 enum { PF2_ORDERING_NATURAL = 0,    /* ILU(0)/IC(0) on A as numbered (the reference's)     */
        PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring: ~8 levels, a
                                         different (weaker) preconditioner, parallel solves */
+enum { PF2_GS_MODIFIED = 0,           /* GMRES Gram-Schmidt as the reference (linear_solver.cu:480-487) */
+       PF2_GS_CLASSICAL_TWICE = 1 };  /* classical Gram-Schmidt with one reorthogonalisation */
 
 typedef struct pf2_solver_options {
     int kind;          /* PF2_SOLVER_* */
@@ -218,10 +221,11 @@ typedef struct pf2_solver_options {
     double tolerance;
     int max_iterations;
     int criterion;     /* PF2_CRITERION_* */
-    int precision;     /* PF2_PRECISION_* (CG only; MIXED takes Jacobi or no preconditioner and
-                          always stops on ||b - A x|| <= tol ||b||) */
+    int precision;     /* PF2_PRECISION_* (CG only; MIXED always stops on ||b - A x|| <= tol ||b||) */
     int restart;       /* GMRES Krylov dimension; 0 = max_iterations (no restart, as the reference) */
     int ordering;      /* PF2_ORDERING_* of ILU(0)/IC(0) */
+    int orthogonalization; /* GMRES: PF2_GS_MODIFIED (the reference's, one reduction per basis
+                              vector) or PF2_GS_CLASSICAL_TWICE (two batched reductions) */
 } pf2_solver_options;
 
 typedef struct pf2_solve_info {

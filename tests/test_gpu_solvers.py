@@ -154,3 +154,20 @@ def test_multicolour_solve_agrees_with_natural(cuda, pc):
         assert info.converged == 1
         xs.append(x.cpu().numpy())
     assert rel_err(xs[1], xs[0]) < 1e-8
+
+
+@pytest.mark.parametrize("pc,restart", [("jacobi", 0), ("ilu", 0), ("jacobi", 20)])
+def test_gmres_classical_gram_schmidt_twice_matches_oracle(cuda, pc, restart):
+    """GMRES with classical Gram-Schmidt applied twice (two batched reductions per
+    iteration) converges like the reference's modified Gram-Schmidt."""
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "gmres", pc, tol=1e-8, maxit=2000, restart=restart,
+                          orthogonalization=1).solve(A, x, b)
+    assert info.converged == 1
+    if restart == 0:
+        ox, oinfo = O.gmres(rp, col, val, rhs, tol=1e-8, maxit=2000, precond=pc)
+        assert abs(info.iterations - oinfo.iterations) <= 2
+    ref, _ = O.pcg(rp, col, val, rhs, tol=1e-12, maxit=5000, precond="jacobi")
+    assert rel_err(x.cpu().numpy(), ref) < 1e-6
