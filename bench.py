@@ -177,50 +177,63 @@ def _timed(fn):
 
 
 def study_solver(args):
-    """Pressure solve to a 1e-8 relative residual on the cylinder mesh and its 1:4
-    refinement: FP64 PCG (Jacobi, IC(0) multicolour) against the mixed-precision
-    refinement.  b = A x* with x* uniform in [-1, 1] (splitmix64 seed 0), x0 = 0."""
+    """Pressure solve to a 1e-8 relative residual on the flow's own pressure matrix after
+    --record steps of the cylinder case, on the 994,240-triangle mesh and its 1:4
+    refinement (3,976,960 triangles): FP64 PCG and the mixed-precision refinement, with
+    Jacobi and IC(0) (natural and multicolour order).  b = A x* with x* uniform in
+    [-1, 1] (splitmix64 seed 0), x0 = 0; median of 3 solves after one warm-up."""
     import torch
     import gpupfem2_gb300 as g
-    out = []
-    xy, tri = mg.cylinder_channel()
+    w = WORKLOADS["cylinder"]
+    xy, tri = w["mesh"]()
     meshes = [("cylinder_1M", xy, tri)]
     if not args.quick:
         x4, t4 = mg.refine_uniform(xy, tri, snap_circle=(0.2, 0.2, 0.05, 1e-3))
         meshes.append(("cylinder_4M", x4, t4))
+    out = []
     for name, mxy, mtri in meshes:
         m = g.Mesh2D.from_arrays(mxy, mtri)
-        _, _, bp = mg.channel_boundary_nodes(mxy, 2.2, 0.41, 1.5, cylinder=(0.2, 0.2, 0.05))
-        A = g.SparseMatrixCSR(m)
-        p = g.default_params(rho=1.0, mu=1e-3, dt=5e-4)
-        x, yv = mxy[:, 0], mxy[:, 1]
-        px = torch.tensor(4 * 1.5 * yv * (0.41 - yv) / 0.41 ** 2, device="cuda")
-        py = torch.tensor(0.1 * np.sin(np.pi * x / 2.2), device="cuda")
-        rhs = torch.empty(m.nv, dtype=torch.float64, device="cuda")
-        g.assemble_pressure(m, p, px, py, None, A, rhs, g.DirichletBCs(m.nv, bp))
+        m.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
+        bu, bv, bp = mg.channel_boundary_nodes(mxy, w["lx"], w["ly"], 1.5, cylinder=w["cyl"])
+        prm = dict(w["params"], pressure_precond=0, calculate_loads=0)
+        eng = g.FlowEngine(m, g.default_params(**prm), bu, bv, bp, capacity_factor=2.0)
+        eng.seed()
+        for _ in range(args.record):
+            eng.step()
+        A, _ = eng.system(2)
         xs = torch.tensor(mg.uniform_pm1(0, m.nv), device="cuda")
         b = torch.empty_like(xs)
         g.spmv(A, xs, b)
+        bn = float(torch.linalg.norm(b))
         rows = []
         cases = [("fp64_jacobi", dict(precond="jacobi")),
+                 ("fp64_ic0_natural", dict(precond="ic", ordering=0)),
                  ("fp64_ic0_multicolour", dict(precond="ic", ordering=1)),
-                 ("mixed_jacobi", dict(precond="jacobi", precision=g.PRECISION_MIXED))]
+                 ("mixed_jacobi", dict(precond="jacobi", precision=g.PRECISION_MIXED)),
+                 ("mixed_ic0_natural", dict(precond="ic", ordering=0, precision=g.PRECISION_MIXED)),
+                 ("mixed_ic0_multicolour", dict(precond="ic", ordering=1, precision=g.PRECISION_MIXED))]
         for label, kw in cases:
             s = g.LinearSolver(A, "cg", tol=1e-8, maxit=20000, criterion=g.CRITERION_REL, **kw)
-            x0 = torch.zeros_like(b)
-            s.solve(A, x0, b)  # warm-up (first launch, factorisation)
-            times = []
-            for _ in range(3):
+            times, info, x0 = [], None, None
+            for rep in range(4):
                 x0 = torch.zeros_like(b)
-                info, ms = _timed(lambda: s.solve(A, x0, b))
-                times.append(ms)
+                info, ms = _timed(lambda: s.solve(A, x0, b, check=False))
+                if rep:
+                    times.append(ms)
             r = torch.empty_like(b)
             g.spmv(A, x0, r)
-            res = float(torch.linalg.norm(b - r) / torch.linalg.norm(b))
-            rows.append({"solver": label, "ms": statistics.median(times), "iterations": info.iterations,
-                         "outer": info.outer_iterations, "converged": info.converged, "rel_residual": res,
+            rows.append({"solver": label, "ms": round(statistics.median(times), 3), "iterations": info.iterations,
+                         "outer": info.outer_iterations, "converged": info.converged, "status": info.status,
+                         "rel_residual_fp64": float(torch.linalg.norm(b - r)) / bn,
                          "x_err": float(torch.linalg.norm(x0 - xs) / torch.linalg.norm(xs))})
-        out.append({"mesh": name, "nodes": m.nv, "nnz": A.nnz, "solvers": rows})
+            del s
+        base = rows[0]["ms"]
+        for r_ in rows:
+            r_["time_vs_fp64_jacobi"] = round(r_["ms"] / base, 4)
+        out.append({"mesh": name, "triangles": int(mtri.shape[0]), "nodes": m.nv, "nnz": A.nnz,
+                    "matrix": "pressure system of the flow after %d steps" % args.record, "solvers": rows})
+        del eng, A
+        torch.cuda.synchronize()
     print(json.dumps({"study": "pressure_solver", "criterion": "||b - A x|| <= 1e-8 ||b||", "results": out}))
 
 
@@ -281,6 +294,7 @@ def main():
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--train", type=int, default=40)
     ap.add_argument("--eval", type=int, default=40)
+    ap.add_argument("--record", type=int, default=3)
     args = ap.parse_args()
     if args.study:
         import torch
@@ -358,9 +372,23 @@ def main():
         eng.info()
     torch.cuda.synchronize()
     e2e_ms = 1000.0 * (time.perf_counter() - t0) / args.e2e_steps
+    # ---- SpMV on the flow's pressure matrix (device events, 20 launches)
+    Ap, _ = eng.system(2)
+    nnz = Ap.nnz
+    xs = torch.ones(mesh.nv, dtype=torch.float64, device="cuda")
+    ys = torch.empty_like(xs)
+    g.spmv(Ap, xs, ys)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(20):
+        g.spmv(Ap, xs, ys)
+    e1.record()
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / 20
+    spmv_bytes = 12.0 * nnz + 4.0 * (mesh.nv + 1) + 16.0 * mesh.nv
     # ---- roofline of the dominant phase
     peak, peak_kind = measured_peaks()
-    nnz = g.SparseMatrixCSR(mesh).nnz
     np_ = info.particles
     pres_iters = sum(info.it_pressure[k] for k in range(prm["n_outer"]))
     dominant = max(phase_ms, key=phase_ms.get)
@@ -395,6 +423,14 @@ def main():
                    "phase_ms": {k: round(v, 4) for k, v in phase_ms.items()}, "cx": info.cx, "cy": info.cy},
         "e2e": {"value": e2e_ms, "unit": "ms/step", "h2d_bytes_per_step": int(inflow.numel() * 8),
                 "d2h_bytes_per_step": int(3 * nv * 8 + 8 * 5 * 8)},
+        "metrics": {
+            "particles_per_s": np_ / (phase_ms["particles"] * 1e-3) if phase_ms["particles"] > 0 else None,
+            "elements_assembled_per_s": int(tri.shape[0]) * 5 * prm["n_outer"] / (1e-3 * (
+                phase_ms["prediction_assembly"] + phase_ms["pressure_assembly"] + phase_ms["correction_assembly"])),
+            "spmv_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9, "spmv_ms": spmv_ms,
+            "spmv_frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peak,
+            "pressure_iterations_per_solve": pres_iters / prm["n_outer"],
+            "pressure_ms_per_solve": phase_ms["pressure_solve"] / prm["n_outer"]},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,

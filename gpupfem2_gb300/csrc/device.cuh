@@ -188,7 +188,10 @@ __device__ __forceinline__ void wait_generation(const GridBarrier& b, unsigned g
     __threadfence();
 }
 
+// The error word is read once per block (thread 0) so that every thread of a block takes
+// the same branch afterwards.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks) {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned int* vgen = b.gen;
@@ -201,9 +204,10 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks
         } else {
             wait_generation(b, g);
         }
+        s_ok = *(volatile int*)b.err == 0;
     }
     __syncthreads();
-    return *(volatile int*)b.err == 0;
+    return s_ok != 0;
 }
 
 // Barrier fused with grid-wide sums of NV (<= 4) values: each block contributes its
@@ -214,7 +218,7 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV], double* sh) {
     __shared__ double s_tot[4];
-    __shared__ int s_last;
+    __shared__ int s_last, s_ok;
     __shared__ unsigned s_gen;
     block_sum_n<NV>(v, sh);
     const unsigned G = gridDim.x;
@@ -257,8 +261,9 @@ __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV
 #pragma unroll
         for (int j = 0; j < NV; ++j) v[j] = s_tot[j];
     }
+    if (threadIdx.x == 0) s_ok = *(volatile int*)b.err == 0;
     __syncthreads();
-    return *(volatile int*)b.err == 0;
+    return s_ok != 0;
 }
 
 }  // namespace pf2

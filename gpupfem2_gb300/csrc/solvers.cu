@@ -184,7 +184,8 @@ __device__ void tri_solve(const Tri& T, int dir, V* src, V* dst, const V* fact, 
                 if (dir == 1) __stcg(&src[i], Pending<V>::marker());
             }
         }
-        if (*(volatile int*)err != 0) break;
+        // warp-uniform exit: every lane reaches the next ticket broadcast or none does
+        if (__any_sync(0xffffffffu, *(volatile int*)err != 0)) break;
     }
 }
 
@@ -200,48 +201,52 @@ __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket,
         if (lane == 0) t = atomicAdd(ticket, 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= (unsigned)A.n) break;
-        if (lane != 0) continue;
-        const int i = order[t];
-        const int s = A.rowptr[i], d = A.diag[i], e = A.rowptr[i + 1];
         bool ok = true;
-        if (T.kind == PF2_PRECOND_ILU) {
-            for (int kk = s; kk < d && ok; ++kk) {
-                const int k = A.col[kk];
-                if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
-                const double aik = __ldcg(&a[kk]) / __ldcg(&a[A.diag[k]]);
-                __stcg(&a[kk], aik);
-                const int ks = A.diag[k] + 1, ke = A.rowptr[k + 1];
-                int q = ks;
-                for (int jj = kk + 1; jj < e; ++jj) {
-                    const int j = A.col[jj];
-                    while (q < ke && A.col[q] < j) ++q;
-                    if (q < ke && A.col[q] == j) __stcg(&a[jj], __ldcg(&a[jj]) - aik * __ldcg(&a[q]));
+        const int i = order[t];
+        if (lane == 0) {
+            const int s = A.rowptr[i], d = A.diag[i], e = A.rowptr[i + 1];
+            if (T.kind == PF2_PRECOND_ILU) {
+                for (int kk = s; kk < d && ok; ++kk) {
+                    const int k = A.col[kk];
+                    if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
+                    const double aik = __ldcg(&a[kk]) / __ldcg(&a[A.diag[k]]);
+                    __stcg(&a[kk], aik);
+                    const int ks = A.diag[k] + 1, ke = A.rowptr[k + 1];
+                    int q = ks;
+                    for (int jj = kk + 1; jj < e; ++jj) {
+                        const int j = A.col[jj];
+                        while (q < ke && A.col[q] < j) ++q;
+                        if (q < ke && A.col[q] == j) __stcg(&a[jj], __ldcg(&a[jj]) - aik * __ldcg(&a[q]));
+                    }
                 }
-            }
-        } else {
-            for (int kk = s; kk < d && ok; ++kk) {
-                const int k = A.col[kk];
-                if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
-                double sum = __ldcg(&a[kk]);
-                int p = s, q = A.rowptr[k];
-                const int qe = A.diag[k];
-                while (p < kk && q < qe) {
-                    const int cp = A.col[p], cq = A.col[q];
-                    if (cp == cq) { sum -= __ldcg(&a[p]) * __ldcg(&a[q]); ++p; ++q; }
-                    else if (cp < cq) ++p;
-                    else ++q;
+            } else {
+                for (int kk = s; kk < d && ok; ++kk) {
+                    const int k = A.col[kk];
+                    if (!wait_flag(&T.done_f[k], epoch, err, T.rec, i, k)) { ok = false; break; }
+                    double sum = __ldcg(&a[kk]);
+                    int p = s, q = A.rowptr[k];
+                    const int qe = A.diag[k];
+                    while (p < kk && q < qe) {
+                        const int cp = A.col[p], cq = A.col[q];
+                        if (cp == cq) { sum -= __ldcg(&a[p]) * __ldcg(&a[q]); ++p; ++q; }
+                        else if (cp < cq) ++p;
+                        else ++q;
+                    }
+                    __stcg(&a[kk], sum / __ldcg(&a[A.diag[k]]));
                 }
-                __stcg(&a[kk], sum / __ldcg(&a[A.diag[k]]));
-            }
-            if (ok) {
-                double dd = __ldcg(&a[d]);
-                for (int kk = s; kk < d; ++kk) { const double l = __ldcg(&a[kk]); dd -= l * l; }
-                __stcg(&a[d], sqrt(dd));
+                if (ok) {
+                    double dd = __ldcg(&a[d]);
+                    for (int kk = s; kk < d; ++kk) { const double l = __ldcg(&a[kk]); dd -= l * l; }
+                    __stcg(&a[d], sqrt(dd));
+                }
             }
         }
-        if (!ok) return;
-        __threadfence();
-        atomicExch(&T.done_f[i], epoch);
+        // lanes 1..31 wait here while lane 0 works through the row
+        if (__any_sync(0xffffffffu, !ok)) return;
+        if (lane == 0) {
+            __threadfence();
+            atomicExch(&T.done_f[i], epoch);
+        }
     }
 }
 
