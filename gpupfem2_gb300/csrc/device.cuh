@@ -159,7 +159,7 @@ struct GridBarrier {
     int* rec;      // where a wait gave up: {kind, a, b, c, d}, kind 0 = none
 };
 
-constexpr long long kBarrierPolls = 1ll << 24;
+constexpr long long kBarrierPolls = 1ll << 22;
 constexpr long long kFlagPolls = 1ll << 21;
 
 // First timeout of a launch records its place (kind 1: grid barrier, 2: row flag).

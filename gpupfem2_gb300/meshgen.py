@@ -163,8 +163,10 @@ def cylinder_channel(seed: int = 0, nxh: int = 700, nyh: int = 800, nr: int = 24
     P = xy_c[cid[per[:, 0], per[:, 1]]]
     C = np.array(center)
     d = P - C
-    ang = np.arctan2(d[:, 1], d[:, 0])
-    Q = C + radius * np.stack([np.cos(ang), np.sin(ang)], axis=1)
+    # inner nodes along the rays (IEEE-exact operations only, so the mesh is the same bits
+    # on every platform: no libm trigonometry)
+    dn = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1])
+    Q = C + radius * (d / dn[:, None])
     w = np.concatenate([[0.0], first_layer + (1.0 - first_layer) * np.arange(nr) / (nr - 1)])
     # ring layers k = 0..nr-1 are new nodes; layer nr is the perimeter
     ring_xy = (1.0 - w[:nr, None, None]) * Q[None] + w[:nr, None, None] * P[None]
@@ -197,6 +199,11 @@ def cylinder_channel(seed: int = 0, nxh: int = 700, nyh: int = 800, nr: int = 24
     return xy, tri.astype(np.int32)
 
 
+def _dist(dx, dy):
+    """sqrt(dx^2 + dy^2) from IEEE-exact operations (same bits on every platform)."""
+    return np.sqrt(np.multiply(dx, dx) + np.multiply(dy, dy))
+
+
 def refine_uniform(xy: np.ndarray, tri: np.ndarray, snap_circle=None):
     """1:4 refinement: every triangle is split through its edge midpoints.
 
@@ -213,11 +220,11 @@ def refine_uniform(xy: np.ndarray, tri: np.ndarray, snap_circle=None):
     mid = 0.5 * (xy[a] + xy[b])
     if snap_circle is not None:
         cx, cy, r, tol = snap_circle
-        da = np.abs(np.hypot(xy[a, 0] - cx, xy[a, 1] - cy) - r) < tol
-        db = np.abs(np.hypot(xy[b, 0] - cx, xy[b, 1] - cy) - r) < tol
+        da = np.abs(_dist(xy[a, 0] - cx, xy[a, 1] - cy) - r) < tol
+        db = np.abs(_dist(xy[b, 0] - cx, xy[b, 1] - cy) - r) < tol
         on = da & db
         v = mid[on] - np.array([cx, cy])
-        mid[on] = np.array([cx, cy]) + r * v / np.linalg.norm(v, axis=1)[:, None]
+        mid[on] = np.array([cx, cy]) + r * v / _dist(v[:, 0], v[:, 1])[:, None]
     nt = tri.shape[0]
     m = (nv + inv).reshape(3, nt).T  # m01, m12, m20
     v0, v1, v2 = tri[:, 0], tri[:, 1], tri[:, 2]
@@ -285,7 +292,7 @@ def channel_boundary_nodes(xy: np.ndarray, lx: float, ly: float, umax: float = 1
         elif abs(y) < tol or abs(y - ly) < tol:
             vx.append((i, 0.0))
             vy.append((i, 0.0))
-        elif cylinder is not None and abs(np.hypot(x - cylinder[0], y - cylinder[1]) - cylinder[2]) < body_tol:
+        elif cylinder is not None and abs(_dist(x - cylinder[0], y - cylinder[1]) - cylinder[2]) < body_tol:
             vx.append((i, 0.0))
             vy.append((i, 0.0))
     return vx, vy, pr
