@@ -146,9 +146,12 @@ def cpu_baseline(name, precond, max_seconds=25.0):
         if len(times) >= 3:
             break
     ms = 1000.0 * statistics.median(times)
-    return {"value": ms, "unit": "ms/step", "cores": 1, "kind": "port",
+    threads = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count() or 1
+    return {"value": ms, "unit": "ms/step", "cores": threads, "kind": "port",
             "sample": "%d oracle step(s) of the full %s workload (%d triangles, %d particles at the start), "
-                      "median" % (len(times), name, tri.shape[0], tri.shape[0] * prm["level"] ** 2)}
+                      "median; FP64 C port, OpenMP over particles and SpMV rows (%d threads), "
+                      "the rest single-threaded" % (len(times), name, tri.shape[0], tri.shape[0] * prm["level"] ** 2,
+                                                    threads)}
 
 
 def run_reference(args):

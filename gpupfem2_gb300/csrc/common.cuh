@@ -46,10 +46,10 @@ void count_launch();
         ::pf2::count_launch();                                                           \
         PF2_CUDA(cudaGetLastError());                                                    \
     } while (0)
-#define PF2_COOP_LAUNCH(fn, grid, block, args, st)                                       \
+#define PF2_COOP_LAUNCH(fn, grid, block, args, smem, st)                                 \
     do {                                                                                 \
         ::pf2::count_launch();                                                           \
-        PF2_CUDA(cudaLaunchCooperativeKernel((fn), (grid), (block), (args), 0, (st)));   \
+        PF2_CUDA(cudaLaunchCooperativeKernel((fn), (grid), (block), (args), (smem), (st))); \
     } while (0)
 
 // ------------------------------------------------------ device buffers

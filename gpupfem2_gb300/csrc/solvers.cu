@@ -11,6 +11,7 @@
 // identical bits.  The ILU(0)/IC(0) factorisation and triangular solves walk the rows
 // in level order; a row waits (bounded) until the rows it depends on are done.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -26,6 +27,8 @@ constexpr int kGroup = 8;  // lanes per row in SpMV
 constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
+constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
+constexpr int kBandMinLevels = 128;  // dependency chains at least this long use the banded solve
 
 struct Csr {
     int n;
@@ -60,8 +63,21 @@ __global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__
 // The factors live on the pattern of B = P A P^T, where P is the identity (natural
 // order, as the reference) or a multicolour ordering; perm maps a row of B to the row of
 // A, iperm back.
+// Banded triangular solve plan: the rows of B cut into P contiguous ranges, one block per
+// range.  Per direction, each range's rows are grouped by their level counted over the
+// dependencies inside the range only (lptr/lord, ranges' levels at rlev[r] ..
+// rlev[r + 1]); dependencies on other ranges are waited for in global memory.
+struct Band {
+    int P;                 // ranges; 0 = sync-free row-per-lane solve instead
+    int R;                 // rows per range (the block's shared-memory window)
+    const int* rs;         // P + 1 range starts
+    const int *f_rlev, *f_lptr, *f_lord;
+    const int *b_rlev, *b_lptr, *b_lord;
+};
+
 struct Tri {
     int kind;              // PF2_PRECOND_ILU or PF2_PRECOND_IC
+    Band band;
     Csr B;                 // pattern of the factors (val unused)
     const int* perm;
     const int* iperm;
@@ -189,6 +205,80 @@ __device__ void tri_solve(const Tri& T, int dir, V* src, V* dst, const V* fact, 
     }
 }
 
+extern __shared__ __align__(16) unsigned char pf2_band_smem[];
+
+// Banded triangular solve (same arithmetic as tri_solve): block b takes ranges b, b + G,
+// ...; inside a range, levels are separated by __syncthreads and values of the range come
+// from the block's shared-memory window; values of other ranges (which only depend on
+// ranges processed before them) are waited for as in tri_solve.  A dependency chain then
+// costs a block barrier per step instead of a round trip through L2.
+template <class V>
+__device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, const V* fact, int* err) {
+    const Band& Bd = T.band;
+    const Csr& A = T.B;
+    V* xs = reinterpret_cast<V*>(pf2_band_smem);
+    const bool ic = T.kind == PF2_PRECOND_IC;
+    const int* rlev = dir == 0 ? Bd.f_rlev : Bd.b_rlev;
+    const int* lptr = dir == 0 ? Bd.f_lptr : Bd.b_lptr;
+    const int* lord = dir == 0 ? Bd.f_lord : Bd.b_lord;
+    bool failed = false;
+    // forward: ranges in increasing order (they wait on lower ranges); backward: decreasing
+    const int nmine = blockIdx.x < Bd.P ? (Bd.P - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    for (int q = 0; q < nmine; ++q) {
+        const int r = (int)blockIdx.x + (dir == 0 ? q : nmine - 1 - q) * (int)gridDim.x;
+        const int r0 = __ldg(&Bd.rs[r]), r1 = __ldg(&Bd.rs[r + 1]);
+        const int l1 = __ldg(&rlev[r + 1]);
+        for (int L = __ldg(&rlev[r]); L < l1; ++L) {
+            const int e1 = __ldg(&lptr[L + 1]);
+            for (int t = __ldg(&lptr[L]) + threadIdx.x; t < e1; t += blockDim.x) {
+                const int i = __ldg(&lord[t]);
+                int s, e;
+                const int* cols;
+                if (dir == 0) {
+                    s = __ldg(&A.rowptr[i]);
+                    e = __ldg(&A.diag[i]);
+                    cols = A.col;
+                } else if (!ic) {
+                    s = __ldg(&A.diag[i]) + 1;
+                    e = __ldg(&A.rowptr[i + 1]);
+                    cols = A.col;
+                } else {
+                    s = __ldg(&T.lt_off[i]);
+                    e = __ldg(&T.lt_off[i + 1]);
+                    cols = T.lt_row;
+                }
+                const V in = __ldcg(&src[dir == 0 ? __ldg(&T.perm[i]) : i]);
+                const V d = (dir == 1 || ic) ? __ldcg(&fact[__ldg(&A.diag[i])]) : V(1);
+                V sum = V(0);
+                bool ok = true;
+                for (int k = s; k < e; ++k) {
+                    const int j = __ldg(&cols[k]);
+                    const V f = __ldcg(&fact[(dir == 1 && ic) ? __ldg(&T.lt_pos[k]) : k]);
+                    V xj;
+                    if (j >= r0 && j < r1) {
+                        xj = xs[j - r0];
+                    } else if (!wait_value(dst, j, xj, err, T.rec, i)) {
+                        ok = false;
+                        break;
+                    }
+                    sum += f * xj;
+                }
+                if (ok) {
+                    V v = in - sum;
+                    if (dir == 1 || ic) v = v / d;
+                    xs[i - r0] = v;
+                    __stcg(&dst[i], v);
+                    if (dir == 1) __stcg(&src[i], Pending<V>::marker());
+                } else {
+                    failed = true;
+                }
+            }
+            if (__syncthreads_or(failed)) return false;
+        }
+    }
+    return true;
+}
+
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
 // per warp in level order, lane 0 working through the row.
 __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr, int* err) {
@@ -298,9 +388,16 @@ __device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
 __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, int r0, int r1, int apply,
                               int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
-        tri_solve<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, &a.T.tickets[2 * apply], a.bar.err);
-        if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, &a.T.tickets[2 * apply + 1], a.bar.err);
+        if (a.T.band.P) {
+            tri_solve_banded<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve_banded<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, a.bar.err);
+        } else {
+            tri_solve<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, &a.T.tickets[2 * apply],
+                              a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, &a.T.tickets[2 * apply + 1], a.bar.err);
+        }
         if (!grid_sync(a.bar, gridDim.x)) return false;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const int k = a.T.iperm[i];
@@ -604,9 +701,16 @@ __device__ __forceinline__ float row_times32(const Csr& A, const float* __restri
 __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, int r0, int r1, int apply,
                                 int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
-        tri_solve<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply], a.bar.err);
-        if (!grid_sync(a.bar, gridDim.x)) return false;
-        tri_solve<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, &a.T.tickets[2 * apply + 1], a.bar.err);
+        if (a.T.band.P) {
+            tri_solve_banded<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve_banded<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, a.bar.err);
+        } else {
+            tri_solve<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply],
+                             a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, &a.T.tickets[2 * apply + 1], a.bar.err);
+        }
         if (!grid_sync(a.bar, gridDim.x)) return false;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const int k = a.T.iperm[i];
@@ -768,6 +872,9 @@ struct pf2_solver {
     DevBuf<unsigned> tickets;
     DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
     DevBuf<int> brp, bcol, bdiag, bmap, perm, iperm;  // pattern of the factors and the ordering
+    DevBuf<int> band_rs, f_rlev, f_lptr, f_lord, b_rlev, b_lptr, b_lord;  // banded solve plan
+    int band_P = 0, band_R = 0;
+    size_t smem = 0;  // dynamic shared memory of the solver kernels (banded window)
     DevBuf<double> outB;
     DevBuf<float> fact32, tmp32, outB32;  // mixed precision with ILU/IC
     int levels_fwd = 0, levels_bwd = 0, colors = 0;
@@ -886,6 +993,67 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     PF2_CUDA(cudaMemset(S->epoch.p, 0, sizeof(int)));
     PF2_CUDA(cudaMemset(S->done_f.p, 0, sizeof(int) * n));
     PF2_CUDA(cudaMemset(S->done_b.p, 0, sizeof(int) * n));
+    // long dependency chains (the natural order of a mesh numbered column by column):
+    // banded solve, ranges of kBandRows rows, levels counted inside each range
+    // PF2_BAND_ROWS / PF2_BAND_MIN_LEVELS override the range size and the threshold
+    // (tuning and tests)
+    int band_rows = kBandRows, band_min = kBandMinLevels;
+    if (const char* e = getenv("PF2_BAND_ROWS")) band_rows = std::max(32, std::min(kBandRows, atoi(e)));
+    if (const char* e = getenv("PF2_BAND_MIN_LEVELS")) band_min = std::max(1, atoi(e));
+    S->band_P = 0;
+    if (std::max(S->levels_fwd, S->levels_bwd) >= band_min) {
+        const int R = std::min(n, band_rows);
+        const int P = (n + R - 1) / R;
+        std::vector<int> rs(P + 1);
+        for (int r = 0; r <= P; ++r) rs[r] = std::min(n, r * R);
+        for (int dir = 0; dir < 2; ++dir) {
+            std::vector<int> rlev(P + 1, 0), lptr, lord;
+            lord.reserve(n);
+            std::vector<int> loc(n, 0);
+            for (int r = 0; r < P; ++r) {
+                const int r0 = rs[r], r1 = rs[r + 1];
+                int nl = 0;
+                auto deps = [&](int i, auto&& f) {
+                    if (dir == 0) {
+                        for (int k = brp[i]; k < bdiag[i]; ++k) f(bcol[k]);
+                    } else if (S->opt.precond == PF2_PRECOND_ILU) {
+                        for (int k = bdiag[i] + 1; k < brp[i + 1]; ++k) f(bcol[k]);
+                    } else {
+                        for (int k = off[i]; k < off[i + 1]; ++k) f(lrow[k]);
+                    }
+                };
+                for (int q = 0; q < r1 - r0; ++q) {
+                    const int i = dir == 0 ? r0 + q : r1 - 1 - q;
+                    int l = 0;
+                    deps(i, [&](int j) {
+                        if (j >= r0 && j < r1) l = std::max(l, loc[j] + 1);
+                    });
+                    loc[i] = l;
+                    nl = std::max(nl, l + 1);
+                }
+                // rows of the range grouped by level, in processing order inside a level
+                std::vector<int> cnt(nl + 1, 0);
+                for (int i = r0; i < r1; ++i) cnt[loc[i] + 1]++;
+                for (int l = 0; l < nl; ++l) cnt[l + 1] += cnt[l];
+                const int base = (int)lord.size();
+                lord.resize(base + (r1 - r0));
+                rlev[r] = (int)lptr.size();
+                for (int l = 0; l < nl; ++l) lptr.push_back(base + cnt[l]);
+                for (int q = 0; q < r1 - r0; ++q) {
+                    const int i = dir == 0 ? r0 + q : r1 - 1 - q;
+                    lord[base + cnt[loc[i]]++] = i;
+                }
+            }
+            rlev[P] = (int)lptr.size();
+            lptr.push_back(n);
+            PF2_TRY(up(dir == 0 ? S->f_rlev : S->b_rlev, rlev));
+            PF2_TRY(up(dir == 0 ? S->f_lptr : S->b_lptr, lptr));
+            PF2_TRY(up(dir == 0 ? S->f_lord : S->b_lord, lord));
+        }
+        PF2_TRY(up(S->band_rs, rs));
+        S->band_P = P;
+        S->band_R = R;
+    }
     return PF2_OK;
 }
 
@@ -894,7 +1062,9 @@ static Csr csr_of(const pf2_csr* A) {
 }
 
 static Tri tri_of(pf2_solver* S) {
-    return Tri{ S->opt.precond, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
+    const Band band{ S->band_P, S->band_R, S->band_rs.p, S->f_rlev.p, S->f_lptr.p, S->f_lord.p,
+                     S->b_rlev.p, S->b_lptr.p, S->b_lord.p };
+    return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
                 S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
                 S->rec.p };
@@ -1018,7 +1188,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     PF2_CUDA(cudaMemsetAsync(S->rec.p, 0, 5 * sizeof(int), st));
     void* args[] = { &a };
     if (precond_only) {
-        PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, st);
+        PF2_COOP_LAUNCH((void*)k_precond_apply, dim3(S->blocks), dim3(kSolverThreads), args, S->smem, st);
         if (uses_tri(S)) {
             k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 4);
             PF2_LAUNCH_CHECK();
@@ -1026,7 +1196,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         return PF2_OK;
     }
     void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
-    PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, st);
+    PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, S->smem, st);
     if (uses_tri(S)) {
         k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 2 * applies + 2);
         PF2_LAUNCH_CHECK();
@@ -1059,14 +1229,29 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // SolverGMRES::init clamps the iteration limit to the matrix size (linear_solver.cu:396-399)
     if (opt->kind == PF2_SOLVER_GMRES && S->opt.max_iterations > S->n) S->opt.max_iterations = S->n;
     int occ = 0;
+    pf2_status s;
     const bool mixed = opt->precision == PF2_PRECISION_MIXED;
+    if (uses_tri(S) && (s = build_tri_plan(S))) return fail(s);
+    // the banded triangular solve keeps a range of the solution in shared memory
+    S->smem = S->band_P ? sizeof(double) * (size_t)S->band_R : 0;
     void* fn = (opt->kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolverThreads, 0) != cudaSuccess || occ < 1)
+    if (S->smem) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->smem) != cudaSuccess ||
+            cudaFuncSetAttribute((void*)k_precond_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)S->smem) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "shared-memory attribute", __FILE__, __LINE__));
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kSolverThreads, S->smem) != cudaSuccess || occ < 1)
         return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
-    const int maxb = occ * num_sms();
+    int occ_pc = occ;
+    if (uses_tri(S) &&
+        (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pc, (void*)k_precond_apply, kSolverThreads, S->smem) !=
+             cudaSuccess ||
+         occ_pc < 1))
+        return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
+    const int maxb = std::min(occ, occ_pc) * num_sms();
     // at least ~512 rows per block keeps the barrier count per unit of work low
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
-    pf2_status s;
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks + 4)) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
@@ -1085,7 +1270,6 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
             return fail(s);
     }
     if (uses_tri(S)) {
-        if ((s = build_tri_plan(S))) return fail(s);
         if ((s = S->tickets.alloc(2 * (size_t)max_applies(S) + 2))) return fail(s);
         if (mixed && ((s = S->fact32.alloc(S->nnz)) || (s = S->tmp32.alloc(S->n)) || (s = S->outB32.alloc(S->n))))
             return fail(s);

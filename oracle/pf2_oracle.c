@@ -209,6 +209,8 @@ int or_find_in_row(const int* rowptr, const int* col, int row, int target)
 
 void or_spmv(int n, const int* rowptr, const int* col, const double* val, const double* x, double* y)
 {
+    /* rows are independent: the threads change no bits */
+#pragma omp parallel for schedule(static) if (n > 65536)
     for (int i = 0; i < n; ++i) {
         double s = 0.0;
         for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * x[col[k]];
@@ -691,6 +693,8 @@ int or_advect(int np, int cap, double* px, double* py, double* l0, double* l1, d
     (void)nv;
     const double dts = dt / substeps;
     int deleted = 0;
+    /* particles are independent: the threads change no bits */
+#pragma omp parallel for schedule(static) reduction(+ : deleted) if (np > 65536)
     for (int p = 0; p < np; ++p) {
         int c = cell[p];
         double L[3] = { l0[p], l1[p], l2[p] };

@@ -171,3 +171,32 @@ def test_gmres_classical_gram_schmidt_twice_matches_oracle(cuda, pc, restart):
         assert abs(info.iterations - oinfo.iterations) <= 2
     ref, _ = O.pcg(rp, col, val, rhs, tol=1e-12, maxit=5000, precond="jacobi")
     assert rel_err(x.cpu().numpy(), ref) < 1e-6
+
+
+@pytest.mark.parametrize("pc", ["ilu", "ic"])
+@pytest.mark.parametrize("band_rows", [None, "256"])
+def test_banded_triangular_solves_match_oracle(cuda, pc, band_rows, monkeypatch):
+    """Natural order on the 256 x 64 channel (about 320 levels): the banded solve (ranges
+    of rows, one block each) gives the oracle's preconditioner, also with more ranges than
+    blocks (256-row ranges), and the CG solve converges as the oracle's."""
+    if band_rows:
+        monkeypatch.setenv("PF2_BAND_ROWS", band_rows)
+    m, A, rp, col, val, rhs = _system(256, 64)
+    s = g.LinearSolver(A, "cg", pc, tol=1e-8, maxit=2000)
+    s.setup(A)
+    src = torch.tensor(rhs, device="cuda")
+    dst = torch.empty_like(src)
+    s.apply_preconditioner(dst, src)
+    f = O.ilu0(rp, col, val) if pc == "ilu" else O.ic0(rp, col, val)
+    ref, tmp = np.empty_like(rhs), np.empty_like(rhs)
+    src_h = np.ascontiguousarray(rhs)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    O.lib().or_precond_apply.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 7
+    O.lib().or_precond_apply(O.PRECOND[pc], rp.size - 1, p(rp), p(col), p(f), None, p(src_h), p(ref), p(tmp))
+    assert rel_err(dst.cpu().numpy(), ref) < 1e-12
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = s.solve(A, x, b)
+    ox, oinfo = O.pcg(rp, col, val, rhs, tol=1e-8, maxit=2000, precond=pc)
+    assert info.converged == 1 and abs(info.iterations - oinfo.iterations) <= 2
+    assert rel_err(x.cpu().numpy(), ox) < 1e-6
