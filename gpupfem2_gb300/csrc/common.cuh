@@ -127,7 +127,7 @@ constexpr double kDoubleMin = 2e-6;  // CONSTANTS::DOUBLE_MIN (src/common/consta
 // particle that still sits at a sub-cell centroid (seeded or reseeded and not yet
 // located), whose third barycentric coordinate is the centroid's stored one rather
 // than 1 - l0 - l1.
-constexpr int kCellBits = 27;
+constexpr int kCellBits = 26;  // cell index bits; bits 26..30 hold 1 + sub-cell, the sign bit stays clear
 constexpr int kCellMask = (1 << kCellBits) - 1;
 constexpr int kMaxCells = kCellMask;
 

@@ -40,8 +40,10 @@ struct Csr {
 
 // y_i = sum_k a_ik x_k for the rows a group of kGroup lanes handles; x may be written
 // by other blocks during the kernel, so it is read through L2.
+// Every lane of the warp must call this the same number of times (the group shuffles use
+// the full warp mask): callers pass row -1 past the end of their rows.
 __device__ __forceinline__ double row_times(const Csr& A, int row, const double* x, int lane) {
-    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
+    const int s = row >= 0 ? __ldg(&A.rowptr[row]) : 0, e = row >= 0 ? __ldg(&A.rowptr[row + 1]) : 0;
     double sum = 0.0;
     for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&A.val[k]) * __ldcg(&x[__ldg(&A.col[k])]);
 #pragma unroll
@@ -53,9 +55,12 @@ __global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__
     const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
     const int lane = threadIdx.x % kGroup;
     const int ngroups = gridDim.x * blockDim.x / kGroup;
-    for (int row = gid; row < A.n; row += ngroups) {
-        const double v = row_times(A, row, x, lane);
-        if (lane == 0) y[row] = v;
+    const int wbase = gid - (threadIdx.x & 31) / kGroup;  // first group of this warp
+    for (int b = wbase; b < A.n; b += ngroups) {  // uniform over the warp
+        const int row = b + (threadIdx.x & 31) / kGroup;
+        const bool valid = row < A.n;
+        const double v = row_times(A, valid ? row : -1, x, lane);
+        if (valid && lane == 0) y[row] = v;
     }
 }
 
@@ -428,9 +433,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
     // r = b - A x
-    for (int i = r0 + grp; i < r1; i += ngrp) {
-        const double v = row_times(a.A, i, a.x, lane);
-        if (lane == 0) a.r[i] = a.b[i] - v;
+    for (int rb = r0; rb < r1; rb += ngrp) {  // uniform over the block: full-warp shuffles
+        const int i = rb + grp;
+        const bool valid = i < r1;
+        const double v = row_times(a.A, valid ? i : -1, a.x, lane);
+        if (valid && lane == 0) a.r[i] = a.b[i] - v;
     }
     __syncthreads();
     int apply = 0;
@@ -457,9 +464,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     while (!conv && it < a.maxit) {
         ++it;
         double pq[1] = { 0.0 };
-        for (int i = r0 + grp; i < r1; i += ngrp) {
-            const double v = row_times(a.A, i, a.p, lane);
-            if (lane == 0) { a.q[i] = v; pq[0] += a.p[i] * v; }
+        for (int rb = r0; rb < r1; rb += ngrp) {
+            const int i = rb + grp;
+            const bool valid = i < r1;
+            const double v = row_times(a.A, valid ? i : -1, a.p, lane);
+            if (valid && lane == 0) { a.q[i] = v; pq[0] += a.p[i] * v; }
         }
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
@@ -563,9 +572,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     while (true) {
         // v0 = M^{-1}(b - A x), beta0 = ||v0||
         double* v0 = a.V;
-        for (int i = r0 + grp; i < r1; i += ngrp) {
-            const double v = row_times(a.A, i, a.x, lane);
-            if (lane == 0) a.r[i] = a.b[i] - v;
+        for (int rb = r0; rb < r1; rb += ngrp) {
+            const int i = rb + grp;
+            const bool valid = i < r1;
+            const double v = row_times(a.A, valid ? i : -1, a.x, lane);
+            if (valid && lane == 0) a.r[i] = a.b[i] - v;
         }
         __syncthreads();
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
@@ -590,9 +601,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
             ++total_it;
             double* vk = a.V + (size_t)k * n;
             double* vkp = a.V + (size_t)(k + 1) * n;
-            for (int i = r0 + grp; i < r1; i += ngrp) {
-                const double v = row_times(a.A, i, vk, lane);
-                if (lane == 0) a.q[i] = v;
+            for (int rb = r0; rb < r1; rb += ngrp) {
+                const int i = rb + grp;
+                const bool valid = i < r1;
+                const double v = row_times(a.A, valid ? i : -1, vk, lane);
+                if (valid && lane == 0) a.q[i] = v;
             }
             __syncthreads();
             if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
@@ -688,7 +701,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
 // only where other blocks write them during the kernel).
 __device__ __forceinline__ float row_times32(const Csr& A, const float* __restrict__ val32, int row, const float* x,
                                              int lane) {
-    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
+    const int s = row >= 0 ? __ldg(&A.rowptr[row]) : 0, e = row >= 0 ? __ldg(&A.rowptr[row + 1]) : 0;
     float sum = 0.0f;
     for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&val32[k]) * __ldcg(&x[__ldg(&A.col[k])]);
 #pragma unroll
@@ -750,9 +763,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     while (true) {
         // r = b - A x in FP64
         double rr[1] = { 0.0 };
-        for (int i = r0 + grp; i < r1; i += ngrp) {
-            const double v = row_times(a.A, i, a.x, lane);
-            if (lane == 0) {
+        for (int rb = r0; rb < r1; rb += ngrp) {
+            const int i = rb + grp;
+            const bool valid = i < r1;
+            const double v = row_times(a.A, valid ? i : -1, a.x, lane);
+            if (valid && lane == 0) {
                 const double ri = a.b[i] - v;
                 a.r[i] = ri;
                 rr[0] += ri * ri;
@@ -783,9 +798,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
         while (total < a.maxit) {
             ++total;
             double pq[1] = { 0.0 };
-            for (int i = r0 + grp; i < r1; i += ngrp) {
-                const float v = row_times32(a.A, a.val32, i, a.p32, lane);
-                if (lane == 0) {
+            for (int rb = r0; rb < r1; rb += ngrp) {  // uniform over the block: full-warp shuffles
+                const int i = rb + grp;
+                const bool valid = i < r1;
+                const float v = row_times32(a.A, a.val32, valid ? i : -1, a.p32, lane);
+                if (valid && lane == 0) {
                     a.q32[i] = v;
                     pq[0] += (double)a.p32[i] * (double)v;
                 }
