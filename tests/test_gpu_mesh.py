@@ -38,7 +38,8 @@ def test_edge_boundary_ids(cuda):
     ids = m.download("edge_ids")
     ref = O.edge_boundary_ids(xy, tri, 2.2, 0.41, (0.2, 0.2, 0.05))
     assert np.array_equal(ids, ref)
-    assert (ids == 3).sum() == 600 and (ids == 1).sum() > 0
+    # one body edge per O-grid ray: the box [0.1, 0.3]^2 has 20 + 20 + 20 + 20 perimeter nodes at h = 0.01
+    assert (ids == 3).sum() == 80 and (ids == 1).sum() > 0
 
 
 def test_load_dat_equals_arrays(cuda, tmp_path):
