@@ -154,8 +154,7 @@ struct GridBarrier {
     unsigned int* count;  // zero-initialised
     unsigned int* gen;
     int* err;
-    double* part;  // 4 x gridDim per-block partial sums (grid_reduce)
-    double* tot;   // 4 grid totals (grid_reduce)
+    double* part;  // 2 x 4 x gridDim per-block partial sums (grid_reduce)
     int* rec;      // where a wait gave up: {kind, a, b, c, d}, kind 0 = none
 };
 
@@ -210,59 +209,49 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks
     return s_ok != 0;
 }
 
-// Barrier fused with grid-wide sums of NV (<= 4) values: each block contributes its
-// block sums, the last block to arrive adds the per-block partials in block order
-// (the same order whichever block is last, so the totals are reproducible bit for bit)
-// and publishes the totals before it releases the barrier.  On return v holds the
-// totals in every thread of every block.  sh holds at least 33 * NV doubles.
+// Barrier fused with grid-wide sums of NV (<= 4) values.  Each block stores its block
+// sums in one of two partial arrays (chosen by the parity of the barrier generation) and
+// arrives; once released, every block adds all blocks' partials in block order, so all
+// blocks get the same bits whatever the arrival order.  Two arrays suffice: a block can
+// be at most one barrier ahead of the slowest reader of the other array.  On return v
+// holds the totals in every thread.  sh holds at least 33 * NV doubles; part holds
+// 2 x 4 x gridDim doubles.
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV], double* sh) {
-    __shared__ double s_tot[4];
-    __shared__ int s_last, s_ok;
+    __shared__ int s_ok;
     __shared__ unsigned s_gen;
     block_sum_n<NV>(v, sh);
     const unsigned G = gridDim.x;
     if (threadIdx.x == 0) {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) __stcg(&b.part[j * G + blockIdx.x], v[j]);
         volatile unsigned int* vgen = b.gen;
-        s_gen = *vgen;
+        const unsigned g = *vgen;
+        double* part = b.part + (size_t)(g & 1u) * 4 * G;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], v[j]);
         __threadfence();
-        s_last = (atomicAdd(b.count, 1u) == G - 1) ? 1 : 0;
-    }
-    __syncthreads();
-    if (s_last) {
-        __threadfence();
-        double t[NV];
-#pragma unroll
-        for (int j = 0; j < NV; ++j) t[j] = 0.0;
-        // thread k sums partials k, k + blockDim, ... in increasing order
-        for (unsigned k = threadIdx.x; k < G; k += blockDim.x) {
-#pragma unroll
-            for (int j = 0; j < NV; ++j) t[j] += __ldcg(&b.part[j * G + k]);
-        }
-        block_sum_n<NV>(t, sh);
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int j = 0; j < NV; ++j) __stcg(&b.tot[j], t[j]);
+        if (atomicAdd(b.count, 1u) == G - 1) {
             *b.count = 0;
             __threadfence();
             atomicAdd(b.gen, 1u);
+        } else {
+            wait_generation(b, g);
         }
-#pragma unroll
-        for (int j = 0; j < NV; ++j) v[j] = t[j];
-    } else {
-        if (threadIdx.x == 0) {
-            wait_generation(b, s_gen);
-#pragma unroll
-            for (int j = 0; j < NV; ++j) s_tot[j] = __ldcg(&b.tot[j]);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int j = 0; j < NV; ++j) v[j] = s_tot[j];
+        s_gen = g;
+        s_ok = *(volatile int*)b.err == 0;
     }
-    if (threadIdx.x == 0) s_ok = *(volatile int*)b.err == 0;
     __syncthreads();
+    const double* part = b.part + (size_t)(s_gen & 1u) * 4 * G;
+    double t[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) t[j] = 0.0;
+    // thread k adds partials k, k + blockDim, ... in increasing order, then a fixed tree
+    for (unsigned k = threadIdx.x; k < G; k += blockDim.x) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) t[j] += __ldcg(&part[j * G + k]);
+    }
+    block_sum_n<NV>(t, sh);
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = t[j];
     return s_ok != 0;
 }
 

@@ -28,7 +28,8 @@ constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
 constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
-constexpr int kBandMinLevels = 128;  // dependency chains at least this long use the banded solve
+constexpr int kBandMinLevels = 128;
+constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)  // dependency chains at least this long use the banded solve
 
 struct Csr {
     int n;
@@ -1163,8 +1164,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.q = S->q.p;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
-    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->partial.p + 4 * (size_t)S->blocks,
-                         S->rec.p };
+    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->rec.p };
     a.T = tri_of(S);
     a.tol = S->opt.tolerance;
     a.maxit = S->opt.max_iterations;
@@ -1266,11 +1266,15 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
              cudaSuccess ||
          occ_pc < 1))
         return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
-    const int maxb = std::min(occ, occ_pc) * num_sms();
+    // blocks per SM: fewer blocks make cheaper grid barriers (one arrival atomic per block);
+    // PF2_SOLVER_BLOCKS_PER_SM overrides the default of kSolverBlocksPerSm (tuning)
+    int bps = kSolverBlocksPerSm;
+    if (const char* e = getenv("PF2_SOLVER_BLOCKS_PER_SM")) bps = std::max(1, atoi(e));
+    const int maxb = std::min(std::min(occ, occ_pc), bps) * num_sms();
     // at least ~512 rows per block keeps the barrier count per unit of work low
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
-        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(4 * (size_t)S->blocks + 4)) || (s = S->bar.alloc(2)) ||
+        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
         return fail(s);
     if (mixed && ((s = S->val32.alloc(S->nnz)) || (s = S->d32.alloc(S->n)) || (s = S->r32.alloc(S->n)) ||
