@@ -39,13 +39,13 @@ WORKLOADS = {
     "cylinder": dict(mesh=lambda: mg.cylinder_channel(), lx=2.2, ly=0.41, cyl=(0.2, 0.2, 0.05),
                      params=dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3,
                                  pressure_precond=2, calculate_loads=1, body_boundary_id=3, thickness=0.1,
-                                 mean_velocity=1.0)),
+                                 mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1)),
     # the same case at a quarter of the cells (248,560 triangles): small captures under ncu
     "cylinder_quarter": dict(mesh=lambda: mg.cylinder_channel(nxh=350, nyh=400, nr=12), lx=2.2, ly=0.41,
                              cyl=(0.2, 0.2, 0.05),
                              params=dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3,
                                          pressure_precond=2, calculate_loads=1, body_boundary_id=3, thickness=0.1,
-                                         mean_velocity=1.0)),
+                                         mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1)),
     "channel": dict(mesh=lambda: mg.channel(), lx=4.0, ly=1.0, cyl=None,
                     params=dict(rho=1.0, mu=0.01, dt=0.005, scheme=0, level=3, n_outer=2, substeps=3,
                                 pressure_precond=1)),
@@ -66,13 +66,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def build_case(name, precond=None):
+def build_case(name, precond=None, ordering=None, gs=None):
     w = WORKLOADS[name]
     xy, tri = w["mesh"]()
     bu, bv, bp = mg.channel_boundary_nodes(xy, w["lx"], w["ly"], 1.5, cylinder=w["cyl"])
     prm = dict(w["params"])
     if precond is not None:
         prm["pressure_precond"] = precond
+    if ordering is not None:
+        prm["pressure_ordering"] = ordering
+    if gs is not None:
+        prm["gmres_orthogonalization"] = gs
     return w, xy, tri, bu, bv, bp, prm
 
 
@@ -129,8 +133,9 @@ def cpu_baseline(name, precond, max_seconds=25.0):
     """The oracle's step on a bounded sample of the workload (one host core)."""
     from oracle import oracle as O
     w, xy, tri, bu, bv, bp, prm = build_case(name, precond)
+    # the oracle runs the reference's algorithm: natural-order ILU/IC, modified Gram-Schmidt
     kw = {k: v for k, v in prm.items() if k not in ("calculate_loads", "body_boundary_id", "mean_velocity",
-                                                    "thickness")}
+                                                    "thickness", "pressure_ordering", "gmres_orthogonalization")}
     cyl = w["cyl"]
     op = O.make_params(lx=w["lx"], ly=w["ly"], tol=1e-8, has_cylinder=int(cyl is not None),
                        cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
@@ -291,6 +296,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="cylinder", choices=list(WORKLOADS))
     ap.add_argument("--precond", type=int, default=None, help="pressure preconditioner override (0 J, 1 ILU, 2 IC)")
+    ap.add_argument("--ordering", type=int, default=None, help="ILU/IC ordering override (0 natural, 1 multicolour)")
+    ap.add_argument("--gs", type=int, default=None, help="GMRES Gram-Schmidt override (0 modified, 1 classical twice)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--study", default=None, choices=["solver", "learned"])
@@ -318,7 +325,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond)
+    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond, args.ordering, args.gs)
     mesh = g.Mesh2D.from_arrays(xy, tri)
     mesh.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
     params = g.default_params(**prm)
@@ -416,6 +423,8 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": args.workload, "triangles": int(tri.shape[0]), "nodes": int(nv), "nnz": int(nnz),
                    "particles": int(np_), "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
+                   "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
+                   "gmres_gram_schmidt": ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)],
                    "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
                    "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),
                    "iterations_last_step": {"prediction": [list(info.it_prediction[c])[:prm["n_outer"]]
