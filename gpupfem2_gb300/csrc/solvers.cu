@@ -71,14 +71,29 @@ __global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__
 // A, iperm back.
 // Banded triangular solve plan: the rows of B cut into P contiguous ranges, one block per
 // range.  Per direction, each range's rows are grouped by their level counted over the
-// dependencies inside the range only (lptr/lord, ranges' levels at rlev[r] ..
-// rlev[r + 1]); dependencies on other ranges are waited for in global memory.
+// dependencies inside the range only, levels cut into steps of at most one row per thread
+// (range r owns steps rstep[r] .. rstep[r + 1], step s holds slots sptr[s] .. sptr[s + 1]).
+// A slot is one row with everything its solve needs at fixed-stride positions: the row,
+// the index of its right-hand side, K dependency columns (-1 padded) and, gathered after
+// each factorisation, their factor values and the inverse of the dividing diagonal.
+struct BandDir {
+    const int* rstep;
+    const int* sptr;
+    const int* row;    // [slot]
+    const int* rhs;    // [slot] right-hand side index (A's numbering forward, B's backward)
+    const int* dep;    // [slot * K + k]
+    double* val;       // [slot * K + k] factor values
+    double* dinv;      // [slot] 1 / dividing diagonal (1 for ILU forward)
+    float* val32;      // FP32 copies (mixed precision)
+    float* dinv32;
+};
+
 struct Band {
-    int P;                 // ranges; 0 = sync-free row-per-lane solve instead
-    int R;                 // rows per range (the block's shared-memory window)
-    const int* rs;         // P + 1 range starts
-    const int *f_rlev, *f_lptr, *f_lord;
-    const int *b_rlev, *b_lptr, *b_lord;
+    int P;             // ranges; 0 = sync-free row-per-lane solve instead
+    int R;             // rows per range (the block's shared-memory window)
+    int K;             // dependency slots per row
+    const int* rs;     // P + 1 range starts
+    BandDir f, b;
 };
 
 struct Tri {
@@ -213,73 +228,108 @@ __device__ void tri_solve(const Tri& T, int dir, V* src, V* dst, const V* fact, 
 
 extern __shared__ __align__(16) unsigned char pf2_band_smem[];
 
-// Banded triangular solve (same arithmetic as tri_solve): block b takes ranges b, b + G,
-// ...; inside a range, levels are separated by __syncthreads and values of the range come
-// from the block's shared-memory window; values of other ranges (which only depend on
-// ranges processed before them) are waited for as in tri_solve.  A dependency chain then
-// costs a block barrier per step instead of a round trip through L2.
+// Banded triangular solve: block b takes ranges b, b + G, ... (forward in increasing,
+// backward in decreasing order: a range waits only on ranges solved before it).  Steps
+// of a range are separated by __syncthreads; values of the range come from the block's
+// shared-memory window, values of other ranges are waited for as in tri_solve.  Each
+// thread loads its next step's slot while it solves the current one, so a dependency
+// chain costs one block barrier per step.  The diagonal division of tri_solve is a
+// multiplication by the stored inverse here.
+template <class V> struct BandVals;
+template <> struct BandVals<double> {
+    __device__ static const double* val(const BandDir& D) { return D.val; }
+    __device__ static const double* dinv(const BandDir& D) { return D.dinv; }
+};
+template <> struct BandVals<float> {
+    __device__ static const float* val(const BandDir& D) { return D.val32; }
+    __device__ static const float* dinv(const BandDir& D) { return D.dinv32; }
+};
+
+constexpr int kBandMaxDeps = 8;
+
+__device__ __forceinline__ void prefetch_l1(const void* p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// Pull slot t's fixed-stride record into L1 ahead of its step.
 template <class V>
-__device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, const V* fact, int* err) {
+__device__ __forceinline__ void band_prefetch(const BandDir& D, int K, int t) {
+    prefetch_l1(D.row + t);
+    prefetch_l1(D.rhs + t);
+    prefetch_l1(BandVals<V>::dinv(D) + t);
+    prefetch_l1(D.dep + (size_t)t * K);
+    prefetch_l1(D.dep + (size_t)t * K + K - 1);
+    prefetch_l1(BandVals<V>::val(D) + (size_t)t * K);
+    prefetch_l1(BandVals<V>::val(D) + (size_t)t * K + K - 1);
+}
+
+template <class V>
+__device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, int* err) {
     const Band& Bd = T.band;
-    const Csr& A = T.B;
+    const BandDir& D = dir == 0 ? Bd.f : Bd.b;
+    const int K = Bd.K;
+    const V* vals = BandVals<V>::val(D);
+    const V* dinv = BandVals<V>::dinv(D);
     V* xs = reinterpret_cast<V*>(pf2_band_smem);
-    const bool ic = T.kind == PF2_PRECOND_IC;
-    const int* rlev = dir == 0 ? Bd.f_rlev : Bd.b_rlev;
-    const int* lptr = dir == 0 ? Bd.f_lptr : Bd.b_lptr;
-    const int* lord = dir == 0 ? Bd.f_lord : Bd.b_lord;
     bool failed = false;
-    // forward: ranges in increasing order (they wait on lower ranges); backward: decreasing
+    const int tid = (int)threadIdx.x;
     const int nmine = blockIdx.x < Bd.P ? (Bd.P - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     for (int q = 0; q < nmine; ++q) {
         const int r = (int)blockIdx.x + (dir == 0 ? q : nmine - 1 - q) * (int)gridDim.x;
         const int r0 = __ldg(&Bd.rs[r]), r1 = __ldg(&Bd.rs[r + 1]);
-        const int l1 = __ldg(&rlev[r + 1]);
-        for (int L = __ldg(&rlev[r]); L < l1; ++L) {
-            const int e1 = __ldg(&lptr[L + 1]);
-            for (int t = __ldg(&lptr[L]) + threadIdx.x; t < e1; t += blockDim.x) {
-                const int i = __ldg(&lord[t]);
-                int s, e;
-                const int* cols;
-                if (dir == 0) {
-                    s = __ldg(&A.rowptr[i]);
-                    e = __ldg(&A.diag[i]);
-                    cols = A.col;
-                } else if (!ic) {
-                    s = __ldg(&A.diag[i]) + 1;
-                    e = __ldg(&A.rowptr[i + 1]);
-                    cols = A.col;
-                } else {
-                    s = __ldg(&T.lt_off[i]);
-                    e = __ldg(&T.lt_off[i + 1]);
-                    cols = T.lt_row;
+        const int s0 = __ldg(&D.rstep[r]), s1 = __ldg(&D.rstep[r + 1]);
+        // slot of this thread in the current and next step; the right-hand side of the
+        // next step is loaded one step ahead, the rest of its record prefetched to L1
+        int t = __ldg(&D.sptr[s0]) + tid, te = __ldg(&D.sptr[s0 + 1]);
+        V in = V(0);
+        if (t < te) in = __ldcg(&src[__ldg(&D.rhs[t])]);
+        if (s0 + 1 < s1) {
+            const int u = te + tid;
+            if (u < __ldg(&D.sptr[s0 + 2])) band_prefetch<V>(D, K, u);
+        }
+        for (int st = s0; st < s1; ++st) {
+            int tn = 0, tne = 0;
+            V in_next = V(0);
+            if (st + 1 < s1) {
+                tn = te + tid;
+                tne = __ldg(&D.sptr[st + 2]);
+                if (tn < tne) in_next = __ldcg(&src[__ldg(&D.rhs[tn])]);
+                if (st + 2 < s1) {
+                    const int u = tne + tid;
+                    if (u < __ldg(&D.sptr[st + 3])) band_prefetch<V>(D, K, u);
                 }
-                const V in = __ldcg(&src[dir == 0 ? __ldg(&T.perm[i]) : i]);
-                const V d = (dir == 1 || ic) ? __ldcg(&fact[__ldg(&A.diag[i])]) : V(1);
+            }
+            if (t < te) {
+                const int row = __ldg(&D.row[t]);
+                const V di = __ldg(&dinv[t]);
                 V sum = V(0);
                 bool ok = true;
-                for (int k = s; k < e; ++k) {
-                    const int j = __ldg(&cols[k]);
-                    const V f = __ldcg(&fact[(dir == 1 && ic) ? __ldg(&T.lt_pos[k]) : k]);
+                for (int k = 0; k < K; ++k) {
+                    const int j = __ldg(&D.dep[(size_t)t * K + k]);
+                    if (j < 0) break;
+                    const V f = __ldg(&vals[(size_t)t * K + k]);
                     V xj;
                     if (j >= r0 && j < r1) {
                         xj = xs[j - r0];
-                    } else if (!wait_value(dst, j, xj, err, T.rec, i)) {
+                    } else if (!wait_value(dst, j, xj, err, T.rec, row)) {
                         ok = false;
                         break;
                     }
                     sum += f * xj;
                 }
                 if (ok) {
-                    V v = in - sum;
-                    if (dir == 1 || ic) v = v / d;
-                    xs[i - r0] = v;
-                    __stcg(&dst[i], v);
-                    if (dir == 1) __stcg(&src[i], Pending<V>::marker());
+                    const V v = (in - sum) * di;
+                    xs[row - r0] = v;
+                    __stcg(&dst[row], v);
+                    if (dir == 1) __stcg(&src[row], Pending<V>::marker());
                 } else {
                     failed = true;
                 }
             }
             if (__syncthreads_or(failed)) return false;
+            t = tn;
+            te = tne;
+            in = in_next;
         }
     }
     return true;
@@ -395,9 +445,9 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
                               int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
         if (a.T.band.P) {
-            tri_solve_banded<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, a.bar.err);
+            tri_solve_banded<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return false;
-            tri_solve_banded<double>(a.T, 1, a.T.tmp, a.T.outB, a.T.fact, a.bar.err);
+            tri_solve_banded<double>(a.T, 1, a.T.tmp, a.T.outB, a.bar.err);
         } else {
             tri_solve<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, &a.T.tickets[2 * apply],
                               a.bar.err);
@@ -716,9 +766,9 @@ __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, in
                                 int ep_base) {
     if (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC) {
         if (a.T.band.P) {
-            tri_solve_banded<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, a.bar.err);
+            tri_solve_banded<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return false;
-            tri_solve_banded<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.T.fact32, a.bar.err);
+            tri_solve_banded<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.bar.err);
         } else {
             tri_solve<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply],
                              a.bar.err);
@@ -872,6 +922,12 @@ __global__ void k_precond_apply(KArgs a) {
 
 using namespace pf2;
 
+struct BandHost {
+    DevBuf<int> rstep, sptr, row, rhs, dep, pos, dpos;
+    DevBuf<double> val, dinv;
+    DevBuf<float> val32, dinv32;
+};
+
 struct pf2_solver {
     pf2_solver_options opt{};
     const pf2_mesh* mesh = nullptr;
@@ -890,8 +946,9 @@ struct pf2_solver {
     DevBuf<unsigned> tickets;
     DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
     DevBuf<int> brp, bcol, bdiag, bmap, perm, iperm;  // pattern of the factors and the ordering
-    DevBuf<int> band_rs, f_rlev, f_lptr, f_lord, b_rlev, b_lptr, b_lord;  // banded solve plan
-    int band_P = 0, band_R = 0;
+    DevBuf<int> band_rs;
+    BandHost band[2];  // banded solve plan, forward and backward
+    int band_P = 0, band_R = 0, band_K = 0;
     size_t smem = 0;  // dynamic shared memory of the solver kernels (banded window)
     DevBuf<double> outB;
     DevBuf<float> fact32, tmp32, outB32;  // mixed precision with ILU/IC
@@ -1019,58 +1076,94 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     if (const char* e = getenv("PF2_BAND_ROWS")) band_rows = std::max(32, std::min(kBandRows, atoi(e)));
     if (const char* e = getenv("PF2_BAND_MIN_LEVELS")) band_min = std::max(1, atoi(e));
     S->band_P = 0;
-    if (std::max(S->levels_fwd, S->levels_bwd) >= band_min) {
+    const bool ic = S->opt.precond == PF2_PRECOND_IC;
+    // dependencies of row i in a direction: (column, factor position)
+    auto deps = [&](int dir, int i, auto&& f) {
+        if (dir == 0) {
+            for (int k = brp[i]; k < bdiag[i]; ++k) f(bcol[k], k);
+        } else if (!ic) {
+            for (int k = bdiag[i] + 1; k < brp[i + 1]; ++k) f(bcol[k], k);
+        } else {
+            for (int k = off[i]; k < off[i + 1]; ++k) f(lrow[k], lpos[k]);
+        }
+    };
+    int K = 1;
+    for (int dir = 0; dir < 2; ++dir)
+        for (int i = 0; i < n; ++i) {
+            int c = 0;
+            deps(dir, i, [&](int, int) { ++c; });
+            K = std::max(K, c);
+        }
+    if (std::max(S->levels_fwd, S->levels_bwd) >= band_min && K <= kBandMaxDeps) {
         const int R = std::min(n, band_rows);
         const int P = (n + R - 1) / R;
         std::vector<int> rs(P + 1);
         for (int r = 0; r <= P; ++r) rs[r] = std::min(n, r * R);
         for (int dir = 0; dir < 2; ++dir) {
-            std::vector<int> rlev(P + 1, 0), lptr, lord;
-            lord.reserve(n);
+            BandHost& H = S->band[dir];
+            std::vector<int> rstep(P + 1, 0), sptr, srow;
+            srow.reserve(n);
             std::vector<int> loc(n, 0);
             for (int r = 0; r < P; ++r) {
                 const int r0 = rs[r], r1 = rs[r + 1];
                 int nl = 0;
-                auto deps = [&](int i, auto&& f) {
-                    if (dir == 0) {
-                        for (int k = brp[i]; k < bdiag[i]; ++k) f(bcol[k]);
-                    } else if (S->opt.precond == PF2_PRECOND_ILU) {
-                        for (int k = bdiag[i] + 1; k < brp[i + 1]; ++k) f(bcol[k]);
-                    } else {
-                        for (int k = off[i]; k < off[i + 1]; ++k) f(lrow[k]);
-                    }
-                };
                 for (int q = 0; q < r1 - r0; ++q) {
                     const int i = dir == 0 ? r0 + q : r1 - 1 - q;
                     int l = 0;
-                    deps(i, [&](int j) {
+                    deps(dir, i, [&](int j, int) {
                         if (j >= r0 && j < r1) l = std::max(l, loc[j] + 1);
                     });
                     loc[i] = l;
                     nl = std::max(nl, l + 1);
                 }
-                // rows of the range grouped by level, in processing order inside a level
+                // rows grouped by level (processing order inside a level), levels cut into
+                // steps of at most one row per thread
                 std::vector<int> cnt(nl + 1, 0);
                 for (int i = r0; i < r1; ++i) cnt[loc[i] + 1]++;
                 for (int l = 0; l < nl; ++l) cnt[l + 1] += cnt[l];
-                const int base = (int)lord.size();
-                lord.resize(base + (r1 - r0));
-                rlev[r] = (int)lptr.size();
-                for (int l = 0; l < nl; ++l) lptr.push_back(base + cnt[l]);
+                const int base = (int)srow.size();
+                srow.resize(base + (r1 - r0));
+                std::vector<int> fill(cnt.begin(), cnt.end() - 1);
                 for (int q = 0; q < r1 - r0; ++q) {
                     const int i = dir == 0 ? r0 + q : r1 - 1 - q;
-                    lord[base + cnt[loc[i]]++] = i;
+                    srow[base + fill[loc[i]]++] = i;
                 }
+                rstep[r] = (int)sptr.size();
+                for (int l = 0; l < nl; ++l)
+                    for (int t = cnt[l]; t < cnt[l + 1]; t += kSolverThreads) sptr.push_back(base + t);
             }
-            rlev[P] = (int)lptr.size();
-            lptr.push_back(n);
-            PF2_TRY(up(dir == 0 ? S->f_rlev : S->b_rlev, rlev));
-            PF2_TRY(up(dir == 0 ? S->f_lptr : S->b_lptr, lptr));
-            PF2_TRY(up(dir == 0 ? S->f_lord : S->b_lord, lord));
+            rstep[P] = (int)sptr.size();
+            sptr.push_back(n);
+            std::vector<int> rhs(n), dep((size_t)n * K, -1), pos((size_t)n * K, -1), dpos(n, -1);
+            for (int t = 0; t < n; ++t) {
+                const int i = srow[t];
+                rhs[t] = dir == 0 ? perm[i] : i;
+                int c = 0;
+                deps(dir, i, [&](int j, int k) {
+                    dep[(size_t)t * K + c] = j;
+                    pos[(size_t)t * K + c] = k;
+                    ++c;
+                });
+                dpos[t] = (dir == 1 || ic) ? bdiag[i] : -1;
+            }
+            PF2_TRY(up(H.rstep, rstep));
+            PF2_TRY(up(H.sptr, sptr));
+            PF2_TRY(up(H.row, srow));
+            PF2_TRY(up(H.rhs, rhs));
+            PF2_TRY(up(H.dep, dep));
+            PF2_TRY(up(H.pos, pos));
+            PF2_TRY(up(H.dpos, dpos));
+            PF2_TRY(H.val.alloc((size_t)n * K));
+            PF2_TRY(H.dinv.alloc(n));
+            if (S->opt.precision == PF2_PRECISION_MIXED) {
+                PF2_TRY(H.val32.alloc((size_t)n * K));
+                PF2_TRY(H.dinv32.alloc(n));
+            }
         }
         PF2_TRY(up(S->band_rs, rs));
         S->band_P = P;
         S->band_R = R;
+        S->band_K = K;
     }
     return PF2_OK;
 }
@@ -1080,8 +1173,10 @@ static Csr csr_of(const pf2_csr* A) {
 }
 
 static Tri tri_of(pf2_solver* S) {
-    const Band band{ S->band_P, S->band_R, S->band_rs.p, S->f_rlev.p, S->f_lptr.p, S->f_lord.p,
-                     S->b_rlev.p, S->b_lptr.p, S->b_lord.p };
+    auto dir = [&](BandHost& H) {
+        return BandDir{ H.rstep.p, H.sptr.p, H.row.p, H.rhs.p, H.dep.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p };
+    };
+    const Band band{ S->band_P, S->band_R, S->band_K, S->band_rs.p, dir(S->band[0]), dir(S->band[1]) };
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
                 S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
@@ -1104,6 +1199,24 @@ __global__ void k_gather_values(long long nnz, const double* __restrict__ val, c
 __global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __restrict__ diag, double* invd) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) invd[i] = 1.0 / val[diag[i]];
+}
+
+// Factor values and inverse diagonals of the banded plan's slots (after a factorisation).
+__global__ void k_band_values(long long nk, int n, const int* __restrict__ pos, const int* __restrict__ dpos,
+                              const double* __restrict__ fact, double* val, double* dinv, float* val32,
+                              float* dinv32) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nk; q += stride) {
+        const int p = pos[q];
+        const double v = p >= 0 ? fact[p] : 0.0;
+        val[q] = v;
+        if (val32) val32[q] = (float)v;
+    }
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int d = dpos[t];
+        dinv[t] = d >= 0 ? 1.0 / fact[d] : 1.0;
+        if (dinv32) dinv32[t] = d >= 0 ? 1.0f / (float)fact[d] : 1.0f;
+    }
 }
 
 static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
@@ -1132,6 +1245,14 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     PF2_LAUNCH_CHECK();
     k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
+    if (S->band_P) {
+        const long long nk = (long long)S->n * S->band_K;
+        for (BandHost& H : S->band) {
+            k_band_values<<<std::min((int)blocks_for(nk), num_sms() * 8), kThreads, 0, st>>>(
+                nk, S->n, H.pos.p, H.dpos.p, S->fact.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p);
+            PF2_LAUNCH_CHECK();
+        }
+    }
     if (mixed) {
         k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fact.p,
                                                                                         S->fact32.p);
@@ -1391,3 +1512,4 @@ pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream) 
 }
 
 }  // extern "C"
+
