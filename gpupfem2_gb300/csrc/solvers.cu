@@ -12,6 +12,7 @@
 // in level order; a row waits (bounded) until the rows it depends on are done.
 #include <algorithm>
 #include <cstdlib>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -1513,3 +1514,105 @@ pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream) 
 
 }  // extern "C"
 
+// ------------------------------------------------- allocation-free Jacobi-PCG
+namespace pf2 {
+
+constexpr int kStaticMaxRows = PF2_STATIC_MAX_ROWS;
+constexpr int kStaticMaxBlocks = 512;
+// r, z, p, q and the inverse diagonal (kStaticMaxRows each), 2 x 4 partial sums per block,
+// the solve record (4 doubles)
+constexpr size_t kStaticDoubles = 5ull * kStaticMaxRows + 8ull * kStaticMaxBlocks + 4;
+static __device__ __align__(256) double g_static_work[kStaticDoubles];
+// barrier count, barrier generation, error word, timeout record (5): all zeroed per call
+static __device__ __align__(256) unsigned g_static_words[8];
+
+struct StaticWork {
+    double* work = nullptr;
+    unsigned* words = nullptr;
+};
+static std::mutex g_static_mu;
+static StaticWork g_static[64];  // per device ordinal
+
+static pf2_status static_work(StaticWork& out) {
+    int dev = 0;
+    PF2_CUDA(cudaGetDevice(&dev));
+    PF2_REQUIRE(dev >= 0 && dev < 64, PF2_BAD_INPUT, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    StaticWork& w = g_static[dev];
+    if (!w.work) {
+        void* p = nullptr;
+        void* q = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_work);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(work)", __FILE__, __LINE__);
+        e = cudaGetSymbolAddress(&q, g_static_words);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(words)", __FILE__, __LINE__);
+        w.work = static_cast<double*>(p);
+        w.words = static_cast<unsigned*>(q);
+    }
+    out = w;
+    return PF2_OK;
+}
+
+}  // namespace pf2
+
+extern "C" pf2_status pf2_pcg_jacobi_static(const pf2_csr* A, double* x, const double* b, double tolerance,
+                                            int max_iterations, int criterion, pf2_solve_info* info,
+                                            void* stream) {
+    PF2_REQUIRE(A && x && b, PF2_BAD_INPUT, "null argument");
+    PF2_REQUIRE(A->n <= kStaticMaxRows, PF2_BAD_INPUT,
+                "pf2_pcg_jacobi_static: %d rows exceed its static work storage (%d rows); use pf2_solver_create",
+                A->n, kStaticMaxRows);
+    PF2_REQUIRE(max_iterations >= 0 && tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
+    PF2_REQUIRE(criterion == PF2_CRITERION_ABS || criterion == PF2_CRITERION_REL, PF2_BAD_INPUT,
+                "unknown criterion %d", criterion);
+    StaticWork w;
+    PF2_TRY(static_work(w));
+    cudaStream_t st = as_stream(stream);
+    // the block count of a pf2_solver_create Jacobi-CG solver (same partition, same bits)
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (void*)k_pcg, kSolverThreads, 0) != cudaSuccess ||
+        occ < 1)
+        return cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__);
+    int bps = kSolverBlocksPerSm;
+    if (const char* e = getenv("PF2_SOLVER_BLOCKS_PER_SM")) bps = std::max(1, atoi(e));
+    const int maxb = std::min(occ, bps) * num_sms();
+    const int blocks = std::max(1, std::min(std::min(maxb, kStaticMaxBlocks), (A->n + 511) / 512));
+    double* base = w.work;
+    KArgs a{};
+    a.A = csr_of(A);
+    a.precond = PF2_PRECOND_JACOBI;
+    a.x = x;
+    a.b = b;
+    a.r = base;
+    a.z = base + (size_t)kStaticMaxRows;
+    a.p = base + 2 * (size_t)kStaticMaxRows;
+    a.q = base + 3 * (size_t)kStaticMaxRows;
+    a.invd = base + 4 * (size_t)kStaticMaxRows;
+    a.partial = base + 5 * (size_t)kStaticMaxRows;
+    int* err = reinterpret_cast<int*>(w.words + 2);
+    a.bar = GridBarrier{ w.words, w.words + 1, err, a.partial, reinterpret_cast<int*>(w.words + 3) };
+    a.tol = tolerance;
+    a.maxit = max_iterations;
+    a.criterion = criterion;
+    a.out = reinterpret_cast<SolveOut*>(base + 5 * (size_t)kStaticMaxRows + 8 * (size_t)kStaticMaxBlocks);
+    PF2_CUDA(cudaMemsetAsync(w.words, 0, 8 * sizeof(unsigned), st));
+    void* args[] = { &a };
+    PF2_COOP_LAUNCH((void*)k_pcg, dim3(blocks), dim3(kSolverThreads), args, 0, st);
+    if (!info) return PF2_OK;
+    SolveOut o{};
+    int e = 0;
+    PF2_CUDA(cudaMemcpyAsync(&o, a.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaStreamSynchronize(st));
+    info->iterations = o.iterations;
+    info->converged = o.converged;
+    info->residual = o.residual;
+    info->outer_iterations = 1;
+    info->status = e ? e : o.status;
+    PF2_REQUIRE(e == 0, (pf2_status)e, "device-side wait timed out in the solver");
+    if (!info->converged) {
+        set_error("solver did not converge in %d iterations (residual %g)", info->iterations, info->residual);
+        return PF2_NOT_CONVERGED;
+    }
+    return PF2_OK;
+}

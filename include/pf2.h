@@ -255,6 +255,28 @@ pf2_status pf2_precond_apply(pf2_solver* s, double* dst, const double* src, void
  * (src/linear_algebra/linear_algebra.h:56-80). */
 pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream);
 
+/* Jacobi-preconditioned CG that allocates no memory (no reference counterpart): the same
+ * kernel and arithmetic as a PF2_SOLVER_CG / PF2_PRECOND_JACOBI solver from
+ * pf2_solver_create + pf2_solver_solve, with its work vectors in a fixed file-scope device
+ * array of the library sized for PF2_STATIC_MAX_ROWS rows (about 5.3 MB).  For callers
+ * that must not allocate device memory per solve: a loop of many small solves where a
+ * cudaMalloc/cudaFree pair per solve would dominate (and cudaFree synchronises the
+ * device, stalling work on other streams), or a program whose remaining device memory is
+ * held by its own pool so that a new allocation would fail.
+ * - A with more than PF2_STATIC_MAX_ROWS rows is rejected with PF2_BAD_INPUT.
+ * - The barrier, error and timeout words are zeroed by this call (cudaMemsetAsync on
+ *   `stream`) before the launch; nothing else needs to start at zero.  x is the initial
+ *   guess in, the solution out, as in pf2_solver_solve.
+ * - The storage is one per device: two calls whose work overlaps on one device (other
+ *   streams, other host threads) race on it and give undefined results; order them.
+ * - The first call on a device looks up the array's address (cudaGetSymbolAddress) and
+ *   caches it; make that first call before any stream capture.
+ * info may be NULL (no synchronisation); otherwise the call synchronises `stream` and
+ * fills it, returning PF2_NOT_CONVERGED when max_iterations is reached. */
+enum { PF2_STATIC_MAX_ROWS = 131072 };
+pf2_status pf2_pcg_jacobi_static(const pf2_csr* A, double* x, const double* b, double tolerance, int max_iterations,
+                                 int criterion, pf2_solve_info* info, void* stream);
+
 /* ------------------------------------------------------ ParticleHandler2D
  * Replaces ParticleHandler2D (src/particles/particle_handler_2d.cuh:9-54).  Velocity
  * fields are two device arrays (the reference passes a device array of two device
