@@ -149,6 +149,8 @@ struct pf2_mesh {
     pf2::DevBuf<double> area;
     pf2::DevBuf<double4_32a> invJ;     // row-major {(0,0),(0,1),(1,0),(1,1)}
     pf2::DevBuf<double2> v3;       // third vertex of each cell
+    pf2::DevBuf<float4> invJf;     // FP32 copies of invJ and v3 (cell-location pre-filter only)
+    pf2::DevBuf<float2> v3f;
     pf2::DevBuf<int> nb_off, nb_idx;
     pf2::DevBuf<int> edge_ids;     // int[3*nc]
     // node -> incident cells (ascending), packed (cell << 2 | local vertex)

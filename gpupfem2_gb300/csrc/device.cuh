@@ -51,13 +51,15 @@ __device__ __forceinline__ bool inside_unit(double l0, double l1, double l2) {
 }
 
 // Conservative single-precision test used to skip cells: false only when the point is
-// outside the cell by more than 0.01 in some barycentric coordinate, far beyond the
-// FP32 rounding of these O(10) quantities, so it never rejects a cell the exact FP64
-// test would accept.
-__device__ __forceinline__ bool maybe_inside_f32(double x, double y, const double4_32a J, const double2 v3) {
-    const float dx = (float)(x - v3.x), dy = (float)(y - v3.y);
-    const float l0 = (float)J.x * dx + (float)J.z * dy;
-    const float l1 = (float)J.y * dx + (float)J.w * dy;
+// outside the cell by more than 0.01 in some barycentric coordinate.  Position, vertex
+// and inverse Jacobian are FP32 roundings (relative error 6e-8 each): for coordinates
+// below ~8 the barycentric error is below 1e-6 / h, so for cells larger than ~1e-4 it
+// never rejects a cell the exact FP64 test would accept.  Pure FP32 arithmetic keeps
+// the candidates off GB300's small FP64 pipe.
+__device__ __forceinline__ bool maybe_inside_f32(float x, float y, const float4 J, const float2 v3) {
+    const float dx = x - v3.x, dy = y - v3.y;
+    const float l0 = J.x * dx + J.z * dy;
+    const float l1 = J.y * dx + J.w * dy;
     const float l2 = 1.0f - l0 - l1;
     const float m = 0.01f;
     return l0 > -m && l0 < 1.0f + m && l1 > -m && l1 < 1.0f + m && l2 > -m && l2 < 1.0f + m;

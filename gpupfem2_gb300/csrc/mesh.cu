@@ -17,7 +17,7 @@ namespace pf2 {
 // kCalculateCellArea / kCalculateInvJacobi (mesh_2d.cu:10-34) with
 // Matrix2x2::inverse (cuda_math.cuh:124-141).
 __global__ void k_geometry(int nc, const double2* __restrict__ xy, const int4* __restrict__ tri, double* area,
-                           double4_32a* invJ, double2* v3) {
+                           double4_32a* invJ, double2* v3, float4* invJf, float2* v3f) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nc) return;
     const int4 t = tri[c];
@@ -29,8 +29,12 @@ __global__ void k_geometry(int nc, const double2* __restrict__ xy, const int4* _
     const double d2 = __dsub_rn(B.x, D.x), d3 = __dsub_rn(B.y, D.y);
     const double det = __fma_rn(d0, d3, -__dmul_rn(d1, d2));
     const double inv = __ddiv_rn(1.0, det);
-    invJ[c] = make_double4_32a(__dmul_rn(d3, inv), __dmul_rn(-d1, inv), __dmul_rn(-d2, inv), __dmul_rn(d0, inv));
+    const double4_32a J = make_double4_32a(__dmul_rn(d3, inv), __dmul_rn(-d1, inv), __dmul_rn(-d2, inv),
+                                           __dmul_rn(d0, inv));
+    invJ[c] = J;
     v3[c] = D;
+    invJf[c] = make_float4((float)J.x, (float)J.y, (float)J.z, (float)J.w);
+    v3f[c] = make_float2((float)D.x, (float)D.y);
 }
 
 __global__ void k_tri4(int nc, const int* __restrict__ tri, int4* tri4, int nv, int* err) {
@@ -211,6 +215,8 @@ static pf2_status build_mesh(pf2_mesh* M, int nv, const double* xy, int nc, cons
     PF2_TRY(M->area.alloc(nc));
     PF2_TRY(M->invJ.alloc(nc));
     PF2_TRY(M->v3.alloc(nc));
+    PF2_TRY(M->invJf.alloc(nc));
+    PF2_TRY(M->v3f.alloc(nc));
     PF2_TRY(M->edge_ids.alloc(3 * (size_t)nc));
     DevBuf<int> err;
     PF2_TRY(err.alloc(1));
@@ -224,7 +230,8 @@ static pf2_status build_mesh(pf2_mesh* M, int nv, const double* xy, int nc, cons
     int h_err = 0;
     PF2_TRY(read_err(err.p, st, &h_err));
     PF2_REQUIRE(h_err == 0, PF2_BAD_INPUT, "triangle vertex index out of range or repeated");
-    k_geometry<<<bc, kThreads, 0, st>>>(nc, M->xy.p, M->tri4.p, M->area.p, M->invJ.p, M->v3.p);
+    k_geometry<<<bc, kThreads, 0, st>>>(nc, M->xy.p, M->tri4.p, M->area.p, M->invJ.p, M->v3.p, M->invJf.p,
+                                        M->v3f.p);
     PF2_LAUNCH_CHECK();
     // node incidence
     DevBuf<int> cnt, scratch;

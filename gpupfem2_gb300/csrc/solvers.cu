@@ -336,6 +336,42 @@ __device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, int* err
     return true;
 }
 
+// Sync-free triangular solve on the slot records in level order, for orderings with few
+// levels (multicolour): thread g solves slots g, g + T, ... (T threads in the grid) in
+// increasing order.  In a cooperative launch every thread is resident, so the lowest
+// unsolved slot always belongs to a thread that has reached it (its own earlier slots are
+// lower and solved) and whose dependencies, in lower levels, are solved: no tickets.
+template <class V>
+__device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err) {
+    const BandDir& D = dir == 0 ? T.band.f : T.band.b;
+    const int K = T.band.K;
+    const int n = T.B.n;
+    const V* vals = BandVals<V>::val(D);
+    const V* dinv = BandVals<V>::dinv(D);
+    const int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int row = __ldg(&D.row[t]);
+        const V in = __ldcg(&src[__ldg(&D.rhs[t])]);
+        const V di = __ldg(&dinv[t]);
+        V sum = V(0);
+        bool ok = true;
+        for (int k = 0; k < K; ++k) {
+            const int j = __ldg(&D.dep[(size_t)t * K + k]);
+            if (j < 0) break;
+            const V f = __ldg(&vals[(size_t)t * K + k]);
+            V xj;
+            if (!wait_value(dst, j, xj, err, T.rec, row)) {
+                ok = false;
+                break;
+            }
+            sum += f * xj;
+        }
+        if (!ok) return;
+        __stcg(&dst[row], (in - sum) * di);
+        if (dir == 1) __stcg(&src[row], Pending<V>::marker());
+    }
+}
+
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
 // per warp in level order, lane 0 working through the row.
 __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr, int* err) {
@@ -449,6 +485,10 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
             tri_solve_banded<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return false;
             tri_solve_banded<double>(a.T, 1, a.T.tmp, a.T.outB, a.bar.err);
+        } else if (a.T.band.K) {
+            tri_solve_slots<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve_slots<double>(a.T, 1, a.T.tmp, a.T.outB, a.bar.err);
         } else {
             tri_solve<double>(a.T, 0, const_cast<double*>(src), a.T.tmp, a.T.fact, &a.T.tickets[2 * apply],
                               a.bar.err);
@@ -770,6 +810,10 @@ __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, in
             tri_solve_banded<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return false;
             tri_solve_banded<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.bar.err);
+        } else if (a.T.band.K) {
+            tri_solve_slots<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return false;
+            tri_solve_slots<float>(a.T, 1, a.T.tmp32, a.T.outB32, a.bar.err);
         } else {
             tri_solve<float>(a.T, 0, const_cast<float*>(src), a.T.tmp32, a.T.fact32, &a.T.tickets[2 * apply],
                              a.bar.err);
@@ -1019,6 +1063,7 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
     PF2_TRY(S->fwd_order.alloc(n));
     PF2_CUDA(cudaMemcpy(S->fwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    const std::vector<int> fwd_h = order;
     // backward levels: 1 + max over the strictly upper entries (the pattern is symmetric)
     std::fill(lev.begin(), lev.end(), 0);
     nl = 0;
@@ -1033,6 +1078,7 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
     PF2_TRY(S->bwd_order.alloc(n));
     PF2_CUDA(cudaMemcpy(S->bwd_order.p, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    const std::vector<int> bwd_h = order;
     // rows of L^T: for each k, the entries l_ik with i > k as (row i, position in B)
     std::vector<int> off(n + 1, 0);
     for (int i = 0; i < n; ++i)
@@ -1095,9 +1141,12 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             deps(dir, i, [&](int, int) { ++c; });
             K = std::max(K, c);
         }
-    if (std::max(S->levels_fwd, S->levels_bwd) >= band_min && K <= kBandMaxDeps) {
-        const int R = std::min(n, band_rows);
-        const int P = (n + R - 1) / R;
+    // slot records (rows with at most kBandMaxDeps dependencies): in (range, step) order for
+    // the banded solve, in level order for the sync-free one
+    const bool banded = K <= kBandMaxDeps && std::max(S->levels_fwd, S->levels_bwd) >= band_min;
+    if (K <= kBandMaxDeps) {
+        const int R = banded ? std::min(n, band_rows) : n;
+        const int P = banded ? (n + R - 1) / R : 0;
         std::vector<int> rs(P + 1);
         for (int r = 0; r <= P; ++r) rs[r] = std::min(n, r * R);
         for (int dir = 0; dir < 2; ++dir) {
@@ -1105,6 +1154,7 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             std::vector<int> rstep(P + 1, 0), sptr, srow;
             srow.reserve(n);
             std::vector<int> loc(n, 0);
+            if (!banded) srow = dir == 0 ? fwd_h : bwd_h;
             for (int r = 0; r < P; ++r) {
                 const int r0 = rs[r], r1 = rs[r + 1];
                 int nl = 0;
@@ -1163,7 +1213,7 @@ static pf2_status build_tri_plan(pf2_solver* S) {
         }
         PF2_TRY(up(S->band_rs, rs));
         S->band_P = P;
-        S->band_R = R;
+        S->band_R = banded ? R : 0;
         S->band_K = K;
     }
     return PF2_OK;
@@ -1246,7 +1296,7 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     PF2_LAUNCH_CHECK();
     k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
-    if (S->band_P) {
+    if (S->band_K) {
         const long long nk = (long long)S->n * S->band_K;
         for (BandHost& H : S->band) {
             k_band_values<<<std::min((int)blocks_for(nk), num_sms() * 8), kThreads, 0, st>>>(
