@@ -404,10 +404,18 @@ def main():
     dominant = max(phase_ms, key=phase_ms.get)
     n = nv
     if dominant == "pressure_solve":
-        # per CG iteration: 12 nnz (values + columns) + 4 (n+1) row offsets + x, r, p, q, z
-        # read/written + D^-1: 8 doubles per row
-        algo = pres_iters * (12.0 * nnz + 4.0 * (n + 1) + 64.0 * n)
-        unit_desc = "bytes per CG iteration 12 nnz + 4 (n+1) + 64 n, x %d iterations" % pres_iters
+        # per CG iteration: SpMV 12 nnz (values + columns) + 4 (n+1) row offsets, vectors
+        # x, r, p, q, z read/written + D^-1: 8 doubles per row; ILU(0)/IC(0) adds two
+        # triangular sweeps over nnz_L = (nnz + n) / 2 entries (12 B each) plus 4 B of row
+        # data per row and sweep, and 32 B per row of vector traffic
+        per_it = 12.0 * nnz + 4.0 * (n + 1) + 64.0 * n
+        has_tri = prm["pressure_precond"] in (1, 2)
+        if has_tri:
+            per_it += 2.0 * (12.0 * (nnz + n) / 2.0 + 4.0 * n) + 32.0 * n
+        algo = pres_iters * per_it
+        unit_desc = ("bytes per CG iteration 12 nnz + 4 (n+1) + 64 n%s = %.0f, x %d iterations in %d solves"
+                     % (" + 12 (nnz + n) + 40 n (triangular sweeps)" if has_tri else "", per_it, pres_iters,
+                        prm["n_outer"]))
     elif dominant == "particles":
         # advect+locate 76 B/particle, scatter 12 B, gather 104 B (SoA 52 B moved in and out)
         algo = np_ * (76.0 + 12.0 + 104.0)
