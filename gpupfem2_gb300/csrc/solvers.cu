@@ -23,8 +23,7 @@
 
 namespace pf2 {
 
-constexpr int kSolverThreads = 256;
-constexpr int kGroup = 8;  // lanes per row in SpMV
+constexpr int kSolverThreads = 512;
 constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
@@ -40,30 +39,20 @@ struct Csr {
     const int* diag;  // position of a_ii
 };
 
-// y_i = sum_k a_ik x_k for the rows a group of kGroup lanes handles; x may be written
 // by other blocks during the kernel, so it is read through L2.
-// Every lane of the warp must call this the same number of times (the group shuffles use
-// the full warp mask): callers pass row -1 past the end of their rows.
-__device__ __forceinline__ double row_times(const Csr& A, int row, const double* x, int lane) {
-    const int s = row >= 0 ? __ldg(&A.rowptr[row]) : 0, e = row >= 0 ? __ldg(&A.rowptr[row + 1]) : 0;
+// Row i of A times x, one thread per row (rows of ~7 entries: a thread per row keeps the
+// most loads in flight); x may be written by other blocks during the kernel, so it is read
+// through L2.
+__device__ __forceinline__ double row_dot(const Csr& A, int row, const double* x) {
+    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
     double sum = 0.0;
-    for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&A.val[k]) * __ldcg(&x[__ldg(&A.col[k])]);
-#pragma unroll
-    for (int o = kGroup / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    for (int k = s; k < e; ++k) sum += __ldg(&A.val[k]) * __ldcg(&x[__ldg(&A.col[k])]);
     return sum;
 }
 
 __global__ void k_spmv(Csr A, const double* __restrict__ x, double* __restrict__ y) {
-    const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
-    const int lane = threadIdx.x % kGroup;
-    const int ngroups = gridDim.x * blockDim.x / kGroup;
-    const int wbase = gid - (threadIdx.x & 31) / kGroup;  // first group of this warp
-    for (int b = wbase; b < A.n; b += ngroups) {  // uniform over the warp
-        const int row = b + (threadIdx.x & 31) / kGroup;
-        const bool valid = row < A.n;
-        const double v = row_times(A, valid ? row : -1, x, lane);
-        if (valid && lane == 0) y[row] = v;
-    }
+    for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < A.n; row += gridDim.x * blockDim.x)
+        y[row] = row_dot(A, row, x);
 }
 
 // ------------------------------------------------------------ triangular data
@@ -518,18 +507,15 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     __shared__ double sh[kShDoubles];
     int r0, r1;
     row_range(a.A.n, r0, r1);
-    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     const bool rel = a.criterion == PF2_CRITERION_REL;
     // Jacobi: inverse diagonal (PreconditionerJacobi::initialize, preconditioners.cu:3-14)
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
     // r = b - A x
-    for (int rb = r0; rb < r1; rb += ngrp) {  // uniform over the block: full-warp shuffles
-        const int i = rb + grp;
-        const bool valid = i < r1;
-        const double v = row_times(a.A, valid ? i : -1, a.x, lane);
-        if (valid && lane == 0) a.r[i] = a.b[i] - v;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double v = row_dot(a.A, i, a.x);
+        a.r[i] = a.b[i] - v;
     }
     __syncthreads();
     int apply = 0;
@@ -556,11 +542,10 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
     while (!conv && it < a.maxit) {
         ++it;
         double pq[1] = { 0.0 };
-        for (int rb = r0; rb < r1; rb += ngrp) {
-            const int i = rb + grp;
-            const bool valid = i < r1;
-            const double v = row_times(a.A, valid ? i : -1, a.p, lane);
-            if (valid && lane == 0) { a.q[i] = v; pq[0] += a.p[i] * v; }
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double v = row_dot(a.A, i, a.p);
+            a.q[i] = v;
+            pq[0] += a.p[i] * v;
         }
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
@@ -653,7 +638,6 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const int n = a.A.n;
-    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
@@ -664,11 +648,9 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
     while (true) {
         // v0 = M^{-1}(b - A x), beta0 = ||v0||
         double* v0 = a.V;
-        for (int rb = r0; rb < r1; rb += ngrp) {
-            const int i = rb + grp;
-            const bool valid = i < r1;
-            const double v = row_times(a.A, valid ? i : -1, a.x, lane);
-            if (valid && lane == 0) a.r[i] = a.b[i] - v;
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double v = row_dot(a.A, i, a.x);
+            a.r[i] = a.b[i] - v;
         }
         __syncthreads();
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
@@ -693,11 +675,9 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
             ++total_it;
             double* vk = a.V + (size_t)k * n;
             double* vkp = a.V + (size_t)(k + 1) * n;
-            for (int rb = r0; rb < r1; rb += ngrp) {
-                const int i = rb + grp;
-                const bool valid = i < r1;
-                const double v = row_times(a.A, valid ? i : -1, vk, lane);
-                if (valid && lane == 0) a.q[i] = v;
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                const double v = row_dot(a.A, i, vk);
+                a.q[i] = v;
             }
             __syncthreads();
             if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
@@ -791,13 +771,10 @@ __global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
 
 // FP32 SpMV row (FP32 products summed in FP32 within the row; values read through L2
 // only where other blocks write them during the kernel).
-__device__ __forceinline__ float row_times32(const Csr& A, const float* __restrict__ val32, int row, const float* x,
-                                             int lane) {
-    const int s = row >= 0 ? __ldg(&A.rowptr[row]) : 0, e = row >= 0 ? __ldg(&A.rowptr[row + 1]) : 0;
+__device__ __forceinline__ float row_dot32(const Csr& A, const float* __restrict__ val32, int row, const float* x) {
+    const int s = __ldg(&A.rowptr[row]), e = __ldg(&A.rowptr[row + 1]);
     float sum = 0.0f;
-    for (int k = s + lane; k < e; k += kGroup) sum += __ldg(&val32[k]) * __ldcg(&x[__ldg(&A.col[k])]);
-#pragma unroll
-    for (int o = kGroup / 2; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    for (int k = s; k < e; ++k) sum += __ldg(&val32[k]) * __ldcg(&x[__ldg(&A.col[k])]);
     return sum;
 }
 
@@ -845,7 +822,6 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     __shared__ double sh[kShDoubles];
     int r0, r1;
     row_range(a.A.n, r0, r1);
-    const int lane = threadIdx.x % kGroup, grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
         a.invd32[i] = (a.precond == PF2_PRECOND_JACOBI) ? (float)(1.0 / a.A.val[a.A.diag[i]]) : 1.0f;
@@ -859,15 +835,11 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     while (true) {
         // r = b - A x in FP64
         double rr[1] = { 0.0 };
-        for (int rb = r0; rb < r1; rb += ngrp) {
-            const int i = rb + grp;
-            const bool valid = i < r1;
-            const double v = row_times(a.A, valid ? i : -1, a.x, lane);
-            if (valid && lane == 0) {
-                const double ri = a.b[i] - v;
-                a.r[i] = ri;
-                rr[0] += ri * ri;
-            }
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double v = row_dot(a.A, i, a.x);
+            const double ri = a.b[i] - v;
+            a.r[i] = ri;
+            rr[0] += ri * ri;
         }
         if (!grid_reduce<1>(a.bar, rr, sh)) return;
         rnorm = sqrt(rr[0]);
@@ -894,14 +866,10 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
         while (total < a.maxit) {
             ++total;
             double pq[1] = { 0.0 };
-            for (int rb = r0; rb < r1; rb += ngrp) {  // uniform over the block: full-warp shuffles
-                const int i = rb + grp;
-                const bool valid = i < r1;
-                const float v = row_times32(a.A, a.val32, valid ? i : -1, a.p32, lane);
-                if (valid && lane == 0) {
-                    a.q32[i] = v;
-                    pq[0] += (double)a.p32[i] * (double)v;
-                }
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                const float v = row_dot32(a.A, a.val32, i, a.p32);
+                a.q32[i] = v;
+                pq[0] += (double)a.p32[i] * (double)v;
             }
             if (!grid_reduce<1>(a.bar, pq, sh)) return;
             const float alpha = (float)(gamma / pq[0]);
@@ -1556,7 +1524,7 @@ pf2_status pf2_precond_apply(pf2_solver* S, double* dst, const double* src, void
 
 pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream) {
     PF2_REQUIRE(A && x && y, PF2_BAD_INPUT, "null argument");
-    const int blocks = std::min((int)blocks_for((long long)A->n * kGroup), num_sms() * 16);
+    const int blocks = std::min((int)blocks_for((long long)A->n), num_sms() * 8);
     k_spmv<<<std::max(blocks, 1), kThreads, 0, as_stream(stream)>>>(csr_of(A), x, y);
     PF2_LAUNCH_CHECK();
     return PF2_OK;
