@@ -330,6 +330,33 @@ __device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, int* err
 // increasing order.  In a cooperative launch every thread is resident, so the lowest
 // unsolved slot always belongs to a thread that has reached it (its own earlier slots are
 // lower and solved) and whose dependencies, in lower levels, are solved: no tickets.
+// sum_k f_k x_{j_k} over a slot's dependencies, four at a time: the four value loads are
+// issued together, then only the ones still pending are polled (one round trip instead
+// of four when the dependencies are already solved).  Terms are added in slot order.
+template <class V>
+__device__ __forceinline__ bool slot_dot(const V* dst, const int* dep, const V* val, int K, int row, int* err,
+                                         int* rec, V& sum) {
+    sum = V(0);
+    for (int k0 = 0; k0 < K; k0 += 4) {
+        int j[4];
+        V x[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) j[k] = k0 + k < K ? __ldg(&dep[k0 + k]) : -1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) x[k] = j[k] >= 0 ? *(volatile const V*)&dst[j[k]] : V(0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (j[k] >= 0 && Pending<V>::bits(x[k]) == Pending<V>::kBits &&
+                !wait_value(dst, j[k], x[k], err, rec, row))
+                return false;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (j[k] >= 0) sum += __ldg(&val[k0 + k]) * x[k];
+        if (j[3] < 0) break;
+    }
+    return true;
+}
+
 template <class V>
 __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err) {
     const BandDir& D = dir == 0 ? T.band.f : T.band.b;
@@ -342,20 +369,8 @@ __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err)
         const int row = __ldg(&D.row[t]);
         const V in = __ldcg(&src[__ldg(&D.rhs[t])]);
         const V di = __ldg(&dinv[t]);
-        V sum = V(0);
-        bool ok = true;
-        for (int k = 0; k < K; ++k) {
-            const int j = __ldg(&D.dep[(size_t)t * K + k]);
-            if (j < 0) break;
-            const V f = __ldg(&vals[(size_t)t * K + k]);
-            V xj;
-            if (!wait_value(dst, j, xj, err, T.rec, row)) {
-                ok = false;
-                break;
-            }
-            sum += f * xj;
-        }
-        if (!ok) return;
+        V sum;
+        if (!slot_dot(dst, D.dep + (size_t)t * K, vals + (size_t)t * K, K, row, err, T.rec, sum)) return;
         __stcg(&dst[row], (in - sum) * di);
         if (dir == 1) __stcg(&src[row], Pending<V>::marker());
     }
