@@ -613,8 +613,17 @@ __device__ __forceinline__ void block_dots(const double* V, int n, int K, const 
     const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int i = wq; i < K; i += nw) {
         const double* vi = V + (size_t)i * n;
-        double d = 0.0;
-        for (int j = r0 + lane; j < r1; j += 32) d += w[j] * vi[j];
+        // four independent partial sums keep four loads of each stream in flight
+        double d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0;
+        int j = r0 + lane;
+        for (; j + 96 < r1; j += 128) {
+            d0 += w[j] * vi[j];
+            d1 += w[j + 32] * vi[j + 32];
+            d2 += w[j + 64] * vi[j + 64];
+            d3 += w[j + 96] * vi[j + 96];
+        }
+        for (; j < r1; j += 32) d0 += w[j] * vi[j];
+        double d = (d0 + d1) + (d2 + d3);
         d = warp_sum(d);
         if (lane == 0) out[i] = d;
     }
