@@ -27,6 +27,7 @@ constexpr int kSolverThreads = 512;
 constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
+constexpr double kMixedInnerEta = 1e-4;  // inner FP32 solves stop at this fraction of the outer residual
 constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
 constexpr int kBandMinLevels = 128;
 constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)  // dependency chains at least this long use the banded solve
@@ -1349,7 +1350,8 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         a.q32 = S->q32.p;
         a.z32 = S->z32.p;
         a.invd32 = S->invd32.p;
-        a.inner_eta = 1e-4;
+        a.inner_eta = kMixedInnerEta;
+        if (const char* e = getenv("PF2_MIXED_INNER_ETA")) a.inner_eta = std::max(1e-12, atof(e));  // tuning
         a.max_outer = kMaxOuter;
     }
     const int applies = max_applies(S);
