@@ -27,7 +27,7 @@ constexpr int kSolverThreads = 512;
 constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
-constexpr double kMixedInnerEta = 1e-4;  // inner FP32 solves stop at this fraction of the outer residual
+constexpr double kMixedInnerEta = 0.1;  // mixed CG refines when the iterated residual drops by this factor
 constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
 constexpr int kBandMinLevels = 128;
 constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)  // dependency chains at least this long use the banded solve
@@ -836,11 +836,15 @@ __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, in
     return true;
 }
 
-// Mixed-precision iterative refinement (no reference counterpart): the outer loop keeps
-// x, r = b - A x (FP64 SpMV), the update x += d and the test ||r|| <= tol ||b|| in FP64;
-// each inner solve A d = r is a preconditioned CG (Jacobi, ILU(0) or IC(0)) whose SpMV,
-// preconditioner apply and vector updates are FP32 and whose dot products accumulate
-// FP32 products in FP64.
+// Mixed-precision CG with reliable updates (no reference counterpart).  The iteration
+// (SpMV, preconditioner, vector updates) runs in FP32; each thread's few dot-product
+// terms are summed in FP32 and the block and grid sums in FP64.  The solution lives in
+// FP64: the FP32 iterates accumulate the update d, and at a refinement point (the
+// iterated residual fell below kReliableDrop of its value at the last refinement, or
+// below the target) x += d, r = b - A x and the test ||r|| <= tol ||b|| run in FP64, and
+// the iteration continues from the true residual with its search direction kept, so the
+// Krylov space is not restarted.  On GB300 the FP32 iteration also stays off the small
+// FP64 pipe.  a.inner_eta is the refinement trigger (the drop of the iterated residual).
 __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
@@ -848,99 +852,119 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+    // r = b - A x (FP64), r32 = r, d = 0, inverse diagonal
+    double red[2] = { 0.0, 0.0 };  // b.b, r.r
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
         a.invd32[i] = (a.precond == PF2_PRECOND_JACOBI) ? (float)(1.0 / a.A.val[a.A.diag[i]]) : 1.0f;
-    double bb[1] = { 0.0 };
-    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) bb[0] += a.b[i] * a.b[i];
-    if (!grid_reduce<1>(a.bar, bb, sh)) return;
-    const double bnorm = sqrt(bb[0]);
-    int total = 0, outer = 0, apply = 0;
-    bool conv = false;
-    double rnorm = 0.0;
-    while (true) {
-        // r = b - A x in FP64
-        double rr[1] = { 0.0 };
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            const double v = row_dot(a.A, i, a.x);
-            const double ri = a.b[i] - v;
-            a.r[i] = ri;
-            rr[0] += ri * ri;
-        }
-        if (!grid_reduce<1>(a.bar, rr, sh)) return;
-        rnorm = sqrt(rr[0]);
-        if (rnorm <= a.tol * bnorm) { conv = true; break; }
-        if (outer >= a.max_outer || total >= a.maxit) break;
-        ++outer;
-        // inner CG in FP32: d = 0, r32 = r, z = M^{-1} r32, p = z
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            a.r32[i] = (float)a.r[i];
-            a.d32[i] = 0.0f;
-        }
-        __syncthreads();
+        const double ri = a.b[i] - row_dot(a.A, i, a.x);
+        a.r32[i] = (float)ri;
+        a.d32[i] = 0.0f;
+        red[0] += a.b[i] * a.b[i];
+        red[1] += ri * ri;
+    }
+    if (!grid_reduce<2>(a.bar, red, sh)) return;
+    const double bnorm = sqrt(red[0]);
+    const double target = a.tol * bnorm;
+    double rnorm = sqrt(red[1]);       // true (FP64) residual at the last refinement
+    double rlast = rnorm;              // iterated residual norm at the last refinement
+    int it = 0, refinements = 1, apply = 0;
+    bool conv = rnorm <= target;
+    if (!conv) {
+        // z = M^{-1} r32, p = z, gamma = r.z
         if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
         if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
-        double g[1] = { 0.0 };
+        float gl = 0.0f;
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const float zi = a.z32[i];
             a.p32[i] = zi;
-            g[0] += (double)a.r32[i] * (double)zi;
+            gl = fmaf(a.r32[i], zi, gl);
         }
+        double g[1] = { (double)gl };
         if (!grid_reduce<1>(a.bar, g, sh)) return;
         double gamma = g[0];
-        const double target = a.inner_eta * rnorm;
-        while (total < a.maxit) {
-            ++total;
-            double pq[1] = { 0.0 };
+        while (it < a.maxit) {
+            ++it;
+            // q = A p, p.q
+            float pql = 0.0f;
             for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
                 const float v = row_dot32(a.A, a.val32, i, a.p32);
                 a.q32[i] = v;
-                pq[0] += (double)a.p32[i] * (double)v;
+                pql = fmaf(a.p32[i], v, pql);
             }
+            double pq[1] = { (double)pql };
             if (!grid_reduce<1>(a.bar, pq, sh)) return;
             const float alpha = (float)(gamma / pq[0]);
-            double gn = 0.0, rn = 0.0;
+            // d += alpha p, r -= alpha q, z = M^{-1} r, r.z and r.r
+            float gl2 = 0.0f, rl2 = 0.0f;
             if (global_pc) {
                 for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-                    a.d32[i] += alpha * a.p32[i];
-                    const float ri = a.r32[i] - alpha * a.q32[i];
+                    a.d32[i] = fmaf(alpha, a.p32[i], a.d32[i]);
+                    const float ri = fmaf(-alpha, a.q32[i], a.r32[i]);
                     a.r32[i] = ri;
-                    rn += (double)ri * (double)ri;
+                    rl2 = fmaf(ri, ri, rl2);
                 }
                 __syncthreads();
                 if (!grid_sync(a.bar, gridDim.x)) return;
                 if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
-                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gn += (double)a.r32[i] * (double)a.z32[i];
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gl2 = fmaf(a.r32[i], a.z32[i], gl2);
             } else {
                 for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-                    a.d32[i] += alpha * a.p32[i];
-                    const float ri = a.r32[i] - alpha * a.q32[i];
+                    a.d32[i] = fmaf(alpha, a.p32[i], a.d32[i]);
+                    const float ri = fmaf(-alpha, a.q32[i], a.r32[i]);
                     const float zi = ri * a.invd32[i];
                     a.r32[i] = ri;
                     a.z32[i] = zi;
-                    gn += (double)ri * (double)zi;
-                    rn += (double)ri * (double)ri;
+                    gl2 = fmaf(ri, zi, gl2);
+                    rl2 = fmaf(ri, ri, rl2);
                 }
             }
-            double g2[2] = { gn, rn };
+            double g2[2] = { (double)gl2, (double)rl2 };
             if (!grid_reduce<2>(a.bar, g2, sh)) return;
-            const double gnew = g2[0];
-            const double rin = sqrt(g2[1]);
-            if (rin <= target) break;
+            double gnew = g2[0];
+            const double rit = sqrt(g2[1]);
+            if (rit <= a.inner_eta * rlast || rit <= target) {
+                // refinement: x += d (own rows), r = b - A x and the convergence test in FP64
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    a.x[i] += (double)a.d32[i];
+                    a.d32[i] = 0.0f;
+                }
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                double rr[1] = { 0.0 };
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    const double ri = a.b[i] - row_dot(a.A, i, a.x);
+                    a.r32[i] = (float)ri;
+                    rr[0] += ri * ri;
+                }
+                if (!grid_reduce<1>(a.bar, rr, sh)) return;
+                ++refinements;
+                rnorm = sqrt(rr[0]);
+                if (rnorm <= target) { conv = true; break; }
+                rlast = rnorm;
+                // continue from the true residual, keeping the search direction
+                if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
+                if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
+                float gl3 = 0.0f;
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gl3 = fmaf(a.r32[i], a.z32[i], gl3);
+                double g3[1] = { (double)gl3 };
+                if (!grid_reduce<1>(a.bar, g3, sh)) return;
+                gnew = g3[0];
+            }
             const float beta = (float)(gnew / gamma);
             gamma = gnew;
-            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p32[i] = a.z32[i] + beta * a.p32[i];
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p32[i] = fmaf(beta, a.p32[i], a.z32[i]);
             if (!grid_sync(a.bar, gridDim.x)) return;
         }
-        // x += d in FP64
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[i] += (double)a.d32[i];
-        if (!grid_sync(a.bar, gridDim.x)) return;
+        if (!conv) {
+            // iteration limit: keep the accumulated update
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[i] += (double)a.d32[i];
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.out->iterations = total;
+        a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
-        a.out->pad = outer;
+        a.out->pad = refinements;
     }
 }
 
