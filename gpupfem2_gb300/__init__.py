@@ -267,6 +267,14 @@ def body_loads(mesh, p, ux, uy, pres, center=(0.2, 0.2)):
     return out[0], out[1]
 
 
+def export_vtu(mesh, path, fields):
+    """DataExport::exportToVTK: the mesh and node fields ({name: device tensor}) as VTU."""
+    names = list(fields)
+    arr_n = (C.c_char_p * max(len(names), 1))(*[n.encode() for n in names])
+    arr_f = (C.c_void_p * max(len(names), 1))(*[_dev(fields[n]) for n in names])
+    _check(lib().pf2_export_vtu(mesh.h, str(path).encode(), len(names), arr_n, arr_f, _stream()), "pf2_export_vtu")
+
+
 def spmv(A, x, y):
     _check(lib().pf2_spmv(A.h, _dev(x), _dev(y), _stream()), "pf2_spmv")
 
@@ -350,6 +358,10 @@ class ParticleHandler2D:
         n = C.c_int()
         _check(lib().pf2_particles_count(self.h, C.byref(n)), "pf2_particles_count")
         return n.value
+
+    def export_vtu(self, path):
+        """DataExport::exportParticlesToVTK: positions and velocities as VTU vertices."""
+        _check(lib().pf2_export_particles_vtu(self.h, str(path).encode()), "pf2_export_particles_vtu")
 
     def download(self):
         n = self.count()

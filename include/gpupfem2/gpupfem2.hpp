@@ -262,8 +262,42 @@ public:
         return n;
     }
 
+    pf2_particles* handle() const { return h_; }
+
 private:
     pf2_particles* h_ = nullptr;
+};
+
+// DataExport (src/data_export.cuh:10-30): node fields registered by name, written with
+// the mesh as VTU; particles as VTU vertices.
+class DataExport {
+public:
+    explicit DataExport(const Mesh2D& mesh, const ParticleHandler2D* particleHandler = nullptr)
+        : mesh_(mesh), ph_(particleHandler) {}
+    void addScalarDataVector(const deviceVector<double>& dataVector, const std::string& fieldname) {
+        for (auto& f : fields_)
+            if (f.first == fieldname) { f.second = dataVector.data; return; }
+        fields_.emplace_back(fieldname, dataVector.data);
+    }
+    void exportToVTK(const std::string& filename) const {
+        std::vector<const char*> names;
+        std::vector<const double*> data;
+        for (const auto& f : fields_) {
+            names.push_back(f.first.c_str());
+            data.push_back(f.second);
+        }
+        check(pf2_export_vtu(mesh_.handle(), filename.c_str(), (int)names.size(), names.data(), data.data(), nullptr),
+              "pf2_export_vtu");
+    }
+    void exportParticlesToVTK(const std::string& filename) const {
+        if (!ph_) throw Error(PF2_BAD_INPUT, "DataExport has no particle handler");
+        check(pf2_export_particles_vtu(ph_->handle(), filename.c_str()), "pf2_export_particles_vtu");
+    }
+
+private:
+    const Mesh2D& mesh_;
+    const ParticleHandler2D* ph_;
+    std::vector<std::pair<std::string, const double*>> fields_;
 };
 
 }  // namespace gpupfem2

@@ -258,6 +258,16 @@ pf2_status pf2_precond_apply(pf2_solver* s, double* dst, const double* src, void
  * (src/linear_algebra/linear_algebra.h:56-80). */
 pf2_status pf2_spmv(const pf2_csr* A, const double* x, double* y, void* stream);
 
+/* ------------------------------------------------------------------ Output
+ * DataExport::exportToVTK (src/data_export.cu:17-122): the mesh and `nfields` node
+ * fields (device arrays of mesh nodes, named by `names`) as an ASCII VTU file in the
+ * reference's layout (Float32 points and data, triangles as VTK type 5).  Synchronises. */
+pf2_status pf2_export_vtu(const pf2_mesh* mesh, const char* path, int nfields, const char* const* names,
+                          const double* const* fields, void* stream);
+/* DataExport::exportParticlesToVTK (src/data_export.cu:124-171): particle positions as
+ * VTK vertices with their velocity.  Synchronises. */
+pf2_status pf2_export_particles_vtu(const pf2_particles* ph, const char* path);
+
 /* Jacobi-preconditioned CG that allocates no memory (no reference counterpart): the same
  * kernel and arithmetic as a PF2_SOLVER_CG / PF2_PRECOND_JACOBI solver from
  * pf2_solver_create + pf2_solver_solve, with its work vectors in a fixed file-scope device
