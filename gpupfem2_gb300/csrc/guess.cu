@@ -1,15 +1,14 @@
 // guess.cu - the learned initial guess of the pressure solve (no reference counterpart).
 //
 // Before the first pressure solve of a step the network (mpnn.cu) sees, per node,
-//   f = ((x - x0) / L, (y - y0) / L, b / s_b, p / s_p, p_prev / s_p)
-// (b the pressure right-hand side, p the previous-step pressure, p_prev the one before,
-// s_b = max |b|, s_p = max(|p|, |p_prev|)) and predicts y; the candidate start is
-//   x0 = p + (p - p_prev) + s_p y,
-// i.e. the network corrects the linear extrapolation.  The solver starts from x0 only if
-// ||b - A x0|| < ||b - A p|| (both computed on the device); otherwise from p, the
-// reference's start.  While training, after the step the target
-//   t = ((p_new - p) - (p - p_prev)) / s_p
-// drives one AdamW step on the same features.
+//   f = ((x - x0) / L, (y - y0) / L, b / s_b, p / s_p, (p - p_prev) / s_d)
+// (b the pressure right-hand side, p the previous-step pressure, p_prev the one before;
+// s_b = max |b|, s_p = max |p|, s_d = max |p - p_prev|) and predicts the increment
+// p_new - p in units of s_d; the candidate start is
+//   x0 = p + s_d y.
+// The solver starts from x0 only if ||b - A x0|| < ||b - A p|| (both computed on the
+// device); otherwise from p, the reference's start.  While training, after the step the
+// target t = (p_new - p) / s_d drives one AdamW step on the same features.
 #include <algorithm>
 #include <cmath>
 
@@ -26,7 +25,7 @@ struct Guess {
     double x0 = 0.0, y0 = 0.0, L = 1.0;
     DevBuf<float> feat, y, target;
     DevBuf<double> p_saved, p_prev, cand, part, res;
-    DevBuf<unsigned long long> scale_bits;  // max |b|, max |p| as ordered bit patterns
+    DevBuf<unsigned long long> scale_bits;  // max |b|, max |p|, max |p - p_prev| as ordered bit patterns
     DevBuf<int> flag;
     int blocks = 0;
 };
@@ -37,13 +36,15 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* slot, double 
 
 __global__ void k_guess_scales(int n, const double* __restrict__ b, const double* __restrict__ p,
                                const double* __restrict__ pp, unsigned long long* s) {
-    double mb = 0.0, mp = 0.0;
+    double mb = 0.0, mp = 0.0, md = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         mb = fmax(mb, fabs(b[i]));
-        mp = fmax(mp, fmax(fabs(p[i]), fabs(pp[i])));
+        mp = fmax(mp, fabs(p[i]));
+        md = fmax(md, fabs(p[i] - pp[i]));
     }
     atomic_max_abs(&s[0], mb);
     atomic_max_abs(&s[1], mp);
+    atomic_max_abs(&s[2], md);
 }
 
 __device__ __forceinline__ double scale_of(unsigned long long bits) {
@@ -57,21 +58,21 @@ __global__ void k_guess_features(int n, const double2* __restrict__ xy, double x
                                  double* p_saved) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double sb = scale_of(s[0]), sp = scale_of(s[1]);
+    const double sb = scale_of(s[0]), sp = scale_of(s[1]), sd = scale_of(s[2]);
     const double2 c = xy[i];
     f[5 * (size_t)i + 0] = (float)((c.x - x0) * invL);
     f[5 * (size_t)i + 1] = (float)((c.y - y0) * invL);
     f[5 * (size_t)i + 2] = (float)(b[i] / sb);
     f[5 * (size_t)i + 3] = (float)(p[i] / sp);
-    f[5 * (size_t)i + 4] = (float)(pp[i] / sp);
+    f[5 * (size_t)i + 4] = (float)((p[i] - pp[i]) / sd);
     p_saved[i] = p[i];
 }
 
-__global__ void k_guess_candidate(int n, const double* __restrict__ p, const double* __restrict__ pp,
-                                  const float* __restrict__ y, const unsigned long long* __restrict__ s, double* cand) {
+__global__ void k_guess_candidate(int n, const double* __restrict__ p, const float* __restrict__ y,
+                                  const unsigned long long* __restrict__ s, double* cand) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    cand[i] = p[i] + (p[i] - pp[i]) + scale_of(s[1]) * (double)y[i];
+    cand[i] = p[i] + scale_of(s[2]) * (double)y[i];
 }
 
 // per-block partials of ||b - A p||^2 and ||b - A cand||^2
@@ -116,11 +117,10 @@ __global__ void k_guess_select(int n, const int* __restrict__ flag, const double
 }
 
 __global__ void k_guess_target(int n, const double* __restrict__ pnew, const double* __restrict__ p,
-                               const double* __restrict__ pp, const unsigned long long* __restrict__ s, float* t,
-                               double* pp_out) {
+                               const unsigned long long* __restrict__ s, float* t, double* pp_out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    t[i] = (float)(((pnew[i] - p[i]) - (p[i] - pp[i])) / scale_of(s[1]));
+    t[i] = (float)((pnew[i] - p[i]) / scale_of(s[2]));
     pp_out[i] = p[i];  // p becomes the previous pressure of the next step
 }
 
@@ -145,7 +145,7 @@ pf2_status guess_create(const pf2_mesh* m, Guess** out) {
     const size_t n = G->n;
     if ((s = G->feat.alloc(5 * n)) || (s = G->y.alloc(n)) || (s = G->target.alloc(n)) || (s = G->p_saved.alloc(n)) ||
         (s = G->p_prev.alloc(n)) || (s = G->cand.alloc(n)) || (s = G->part.alloc(2 * (size_t)G->blocks)) ||
-        (s = G->res.alloc(2)) || (s = G->scale_bits.alloc(2)) || (s = G->flag.alloc(1)))
+        (s = G->res.alloc(2)) || (s = G->scale_bits.alloc(3)) || (s = G->flag.alloc(1)))
         return fail(s);
     if (cudaMemset(G->p_prev.p, 0, sizeof(double) * n) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "cudaMemset", __FILE__, __LINE__));
@@ -162,14 +162,14 @@ void guess_destroy(Guess* g) {
 pf2_status guess_apply(Guess* G, const pf2_csr* A, const double* b, double* x, const double* /*unused*/,
                        double* res_out, int* used_out, cudaStream_t st) {
     const int n = G->n;
-    PF2_CUDA(cudaMemsetAsync(G->scale_bits.p, 0, 2 * sizeof(unsigned long long), st));
+    PF2_CUDA(cudaMemsetAsync(G->scale_bits.p, 0, 3 * sizeof(unsigned long long), st));
     k_guess_scales<<<G->blocks, kThreads, 0, st>>>(n, b, x, G->p_prev.p, G->scale_bits.p);
     PF2_LAUNCH_CHECK();
     k_guess_features<<<blocks_for(n), kThreads, 0, st>>>(n, G->mesh->xy.p, G->x0, G->y0, 1.0 / G->L, b, x,
                                                          G->p_prev.p, G->scale_bits.p, G->feat.p, G->p_saved.p);
     PF2_LAUNCH_CHECK();
     PF2_TRY(pf2_mpnn_forward(G->net, G->feat.p, G->y.p, st));
-    k_guess_candidate<<<blocks_for(n), kThreads, 0, st>>>(n, x, G->p_prev.p, G->y.p, G->scale_bits.p, G->cand.p);
+    k_guess_candidate<<<blocks_for(n), kThreads, 0, st>>>(n, x, G->y.p, G->scale_bits.p, G->cand.p);
     PF2_LAUNCH_CHECK();
     k_guess_residuals<<<G->blocks, kThreads, 0, st>>>(n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, b, x,
                                                       G->cand.p, G->part.p);
@@ -185,8 +185,8 @@ pf2_status guess_apply(Guess* G, const pf2_csr* A, const double* b, double* x, c
 
 pf2_status guess_train(Guess* G, const double* p_new, float lr, cudaStream_t st) {
     const int n = G->n;
-    k_guess_target<<<blocks_for(n), kThreads, 0, st>>>(n, p_new, G->p_saved.p, G->p_prev.p, G->scale_bits.p,
-                                                       G->target.p, G->p_prev.p);
+    k_guess_target<<<blocks_for(n), kThreads, 0, st>>>(n, p_new, G->p_saved.p, G->scale_bits.p, G->target.p,
+                                                       G->p_prev.p);
     PF2_LAUNCH_CHECK();
     if (lr > 0.0f) PF2_TRY(pf2_mpnn_train_step(G->net, G->feat.p, G->target.p, lr, 1, nullptr, st));
     return PF2_OK;

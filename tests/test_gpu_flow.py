@@ -133,3 +133,28 @@ def test_body_loads_match_oracle(cuda):
     ref = np.zeros(2)
     O.lib().or_body_loads(tri.shape[0], xy, tri, invJ.ravel(), ids, O.C.byref(op), ux, uy, pr, ref)
     assert abs(cx - ref[0]) < 1e-12 * max(1.0, abs(ref[0])) and abs(cy - ref[1]) < 1e-12 * max(1.0, abs(ref[1]))
+
+
+def test_learned_guess_keeps_the_solution(cuda):
+    """Pressure solves started from the learned guess (trained online on the first
+    steps) reach the same converged fields as solves started from the previous
+    pressure: the solver, with its relative 1e-8 test, stays the judge."""
+    xy, tri, bu, bv, bp, p, op = _channel_case()
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(4.0, 1.0)
+    runs = {}
+    for x0 in (0, 1):
+        prm = g.default_params(rho=1.0, mu=0.01, dt=0.005, scheme=0, substeps=3, level=3, n_outer=2,
+                               pressure_precond=0, pressure_criterion=1, pressure_x0=x0, learn_steps=4,
+                               learn_rate=1e-3)
+        eng = g.FlowEngine(m, prm, bu, bv, bp)
+        eng.seed()
+        used = 0
+        for _ in range(8):
+            eng.step()
+            inf = eng.info()
+            assert inf.converged == 1 and inf.status == 0
+            used += inf.guess_used
+        runs[x0] = (eng.field("p"), eng.field("ux"), used)
+    assert rel_err(runs[1][0], runs[0][0]) < 1e-6 and rel_err(runs[1][1], runs[0][1]) < 1e-6
+    assert runs[0][2] == 0
