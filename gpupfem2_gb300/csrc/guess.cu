@@ -4,11 +4,16 @@
 //   f = ((x - x0) / L, (y - y0) / L, b / s_b, p / s_p, (p - p_prev) / s_d)
 // (b the pressure right-hand side, p the previous-step pressure, p_prev the one before;
 // s_b = max |b|, s_p = max |p|, s_d = max |p - p_prev|) and predicts the increment
-// p_new - p in units of s_d; the candidate start is
-//   x0 = p + s_d y.
-// The solver starts from x0 only if ||b - A x0|| < ||b - A p|| (both computed on the
-// device); otherwise from p, the reference's start.  While training, after the step the
-// target t = (p_new - p) / s_d drives one AdamW step on the same features.
+// p_new - p in units of s_d: d1 = s_d y.  With d2 = p - p_prev, the last increment, the
+// start is the Galerkin combination
+//   x0 = p + c1 d1 + c2 d2,  (D^T A D) c = D^T (b - A p),  D = [d1 d2],
+// the point of p + span{d1, d2} closest to the solution in the energy norm (A is SPD).
+// It lowers the energy norm of the error by h^T c >= 0 (h = D^T r0); a direction that
+// does not help gets a coefficient near 0, so the start is never worse than p in that
+// norm, the norm CG minimises.  (The residual norm is a poor test here: the Laplacian
+// amplifies any high-frequency error of a learned increment, so a useful increment can
+// still raise ||b - A x0||.)  While training, after the step the target
+// t = (p_new - p) / s_d drives one AdamW step on the same features.
 #include <algorithm>
 #include <cmath>
 
@@ -24,7 +29,7 @@ struct Guess {
     int n = 0;
     double x0 = 0.0, y0 = 0.0, L = 1.0;
     DevBuf<float> feat, y, target;
-    DevBuf<double> p_saved, p_prev, cand, part, res;
+    DevBuf<double> p_saved, p_prev, d1, d2, r0, a1, a2, coef, part, res;
     DevBuf<unsigned long long> scale_bits;  // max |b|, max |p|, max |p - p_prev| as ordered bit patterns
     DevBuf<int> flag;
     int blocks = 0;
@@ -68,52 +73,93 @@ __global__ void k_guess_features(int n, const double2* __restrict__ xy, double x
     p_saved[i] = p[i];
 }
 
-__global__ void k_guess_candidate(int n, const double* __restrict__ p, const float* __restrict__ y,
-                                  const unsigned long long* __restrict__ s, double* cand) {
+__global__ void k_guess_dirs(int n, const double* __restrict__ p, const double* __restrict__ pp,
+                             const float* __restrict__ y, const unsigned long long* __restrict__ s, double* d1,
+                             double* d2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    cand[i] = p[i] + scale_of(s[2]) * (double)y[i];
+    d1[i] = scale_of(s[2]) * (double)y[i];
+    d2[i] = p[i] - pp[i];
 }
 
-// per-block partials of ||b - A p||^2 and ||b - A cand||^2
-__global__ void k_guess_residuals(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                                  const double* __restrict__ val, const double* __restrict__ b,
-                                  const double* __restrict__ p, const double* __restrict__ cand, double* part) {
-    __shared__ double sh[40];
-    double r0 = 0.0, r1 = 0.0;
+// One pass over A: r0 = b - A p, A d1, A d2 per row; per-block partials of
+// d1.Ad1, d1.Ad2, d2.Ad2, d1.r0, d2.r0, r0.r0 (6 x blocks).
+__global__ void k_guess_project(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                                const double* __restrict__ val, const double* __restrict__ b,
+                                const double* __restrict__ p, const double* __restrict__ d1,
+                                const double* __restrict__ d2, double* r0, double* a1, double* a2, double* part) {
+    __shared__ double sh[33 * 6];
+    double acc[6] = { 0, 0, 0, 0, 0, 0 };
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double a0 = 0.0, a1 = 0.0;
+        double sp = 0.0, s1 = 0.0, s2 = 0.0;
         for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-            a0 += val[k] * p[col[k]];
-            a1 += val[k] * cand[col[k]];
+            const double v = val[k];
+            const int c = col[k];
+            sp += v * p[c];
+            s1 += v * d1[c];
+            s2 += v * d2[c];
         }
-        const double e0 = b[i] - a0, e1 = b[i] - a1;
-        r0 += e0 * e0;
-        r1 += e1 * e1;
+        const double ri = b[i] - sp;
+        r0[i] = ri;
+        a1[i] = s1;
+        a2[i] = s2;
+        acc[0] += d1[i] * s1;
+        acc[1] += d1[i] * s2;
+        acc[2] += d2[i] * s2;
+        acc[3] += d1[i] * ri;
+        acc[4] += d2[i] * ri;
+        acc[5] += ri * ri;
     }
-    r0 = block_sum(r0, sh);
-    r1 = block_sum(r1, sh);
-    if (threadIdx.x == 0) {
-        part[2 * blockIdx.x] = r0;
-        part[2 * blockIdx.x + 1] = r1;
-    }
+    block_sum_n<6>(acc, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = acc[k];
 }
 
-__global__ void k_guess_decide(int nb, const double* __restrict__ part, double* res, int* flag) {
-    double r0 = 0.0, r1 = 0.0;
-    for (int k = 0; k < nb; ++k) {
-        r0 += part[2 * k];
-        r1 += part[2 * k + 1];
+// Coefficients of the 2 x 2 Galerkin system (one thread, block partials in order);
+// coef = {c1, c2}, res[0] = ||b - A p||.
+__global__ void k_guess_solve(int nb, const double* __restrict__ part, double* coef, double* res, int* used) {
+    double t[6] = { 0, 0, 0, 0, 0, 0 };
+    for (int b = 0; b < nb; ++b)
+        for (int k = 0; k < 6; ++k) t[k] += part[6 * b + k];
+    const double g11 = t[0], g12 = t[1], g22 = t[2], h1 = t[3], h2 = t[4];
+    double c1 = 0.0, c2 = 0.0;
+    const double det = g11 * g22 - g12 * g12;
+    if (g11 > 0.0 && g22 > 0.0 && det > 1e-12 * g11 * g22) {
+        c1 = (g22 * h1 - g12 * h2) / det;
+        c2 = (g11 * h2 - g12 * h1) / det;
+    } else if (g11 > 0.0 && (g22 <= 0.0 || h1 * h1 / g11 >= h2 * h2 / g22)) {
+        c1 = h1 / g11;  // one usable direction: the better of the two
+    } else if (g22 > 0.0) {
+        c2 = h2 / g22;
     }
-    res[0] = sqrt(r0);
-    res[1] = sqrt(r1);
-    *flag = (r1 < r0) ? 1 : 0;
+    coef[0] = c1;
+    coef[1] = c2;
+    res[0] = sqrt(t[5]);
+    *used = c1 != 0.0 ? 1 : 0;
 }
 
-__global__ void k_guess_select(int n, const int* __restrict__ flag, const double* __restrict__ cand, double* x) {
-    if (!*flag) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] = cand[i];
+// x0 = p + c1 d1 + c2 d2 (x holds p); per-block partials of ||r0 - c1 A d1 - c2 A d2||^2,
+// the residual of the start.
+__global__ void k_guess_combine(int n, const double* __restrict__ coef, const double* __restrict__ d1,
+                                const double* __restrict__ d2, const double* __restrict__ r0,
+                                const double* __restrict__ a1, const double* __restrict__ a2, double* x,
+                                double* part) {
+    __shared__ double sh[40];
+    const double c1 = coef[0], c2 = coef[1];
+    double rr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        x[i] += c1 * d1[i] + c2 * d2[i];
+        const double ri = r0[i] - c1 * a1[i] - c2 * a2[i];
+        rr += ri * ri;
+    }
+    rr = block_sum(rr, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = rr;
+}
+
+__global__ void k_guess_res1(int nb, const double* __restrict__ part, double* res) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[b];
+    res[1] = sqrt(t);
 }
 
 __global__ void k_guess_target(int n, const double* __restrict__ pnew, const double* __restrict__ p,
@@ -144,7 +190,9 @@ pf2_status guess_create(const pf2_mesh* m, Guess** out) {
     G->blocks = std::min((int)blocks_for(G->n), num_sms() * 4);
     const size_t n = G->n;
     if ((s = G->feat.alloc(5 * n)) || (s = G->y.alloc(n)) || (s = G->target.alloc(n)) || (s = G->p_saved.alloc(n)) ||
-        (s = G->p_prev.alloc(n)) || (s = G->cand.alloc(n)) || (s = G->part.alloc(2 * (size_t)G->blocks)) ||
+        (s = G->p_prev.alloc(n)) || (s = G->d1.alloc(n)) || (s = G->d2.alloc(n)) || (s = G->r0.alloc(n)) ||
+        (s = G->a1.alloc(n)) || (s = G->a2.alloc(n)) || (s = G->coef.alloc(2)) ||
+        (s = G->part.alloc(6 * (size_t)G->blocks)) ||
         (s = G->res.alloc(2)) || (s = G->scale_bits.alloc(3)) || (s = G->flag.alloc(1)))
         return fail(s);
     if (cudaMemset(G->p_prev.p, 0, sizeof(double) * n) != cudaSuccess)
@@ -169,14 +217,17 @@ pf2_status guess_apply(Guess* G, const pf2_csr* A, const double* b, double* x, c
                                                          G->p_prev.p, G->scale_bits.p, G->feat.p, G->p_saved.p);
     PF2_LAUNCH_CHECK();
     PF2_TRY(pf2_mpnn_forward(G->net, G->feat.p, G->y.p, st));
-    k_guess_candidate<<<blocks_for(n), kThreads, 0, st>>>(n, x, G->y.p, G->scale_bits.p, G->cand.p);
+    k_guess_dirs<<<blocks_for(n), kThreads, 0, st>>>(n, x, G->p_prev.p, G->y.p, G->scale_bits.p, G->d1.p, G->d2.p);
     PF2_LAUNCH_CHECK();
-    k_guess_residuals<<<G->blocks, kThreads, 0, st>>>(n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, b, x,
-                                                      G->cand.p, G->part.p);
+    k_guess_project<<<G->blocks, kThreads, 0, st>>>(n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, b, x, G->d1.p,
+                                                    G->d2.p, G->r0.p, G->a1.p, G->a2.p, G->part.p);
     PF2_LAUNCH_CHECK();
-    k_guess_decide<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->res.p, G->flag.p);
+    k_guess_solve<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->coef.p, G->res.p, G->flag.p);
     PF2_LAUNCH_CHECK();
-    k_guess_select<<<blocks_for(n), kThreads, 0, st>>>(n, G->flag.p, G->cand.p, x);
+    k_guess_combine<<<G->blocks, kThreads, 0, st>>>(n, G->coef.p, G->d1.p, G->d2.p, G->r0.p, G->a1.p, G->a2.p, x,
+                                                    G->part.p);
+    PF2_LAUNCH_CHECK();
+    k_guess_res1<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->res.p);
     PF2_LAUNCH_CHECK();
     if (res_out) PF2_CUDA(cudaMemcpyAsync(res_out, G->res.p, 2 * sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (used_out) PF2_CUDA(cudaMemcpyAsync(used_out, G->flag.p, sizeof(int), cudaMemcpyDeviceToDevice, st));
