@@ -261,14 +261,18 @@ def study_learned(args):
     # IC(0) (multicolour order) pressure solves to ||b - A x|| <= 1e-8 ||b|| with an
     # iteration limit high enough for every variant to converge
     prm = dict(prm, max_iterations=20000)
+    # "untrained": the same start with a network that never trains, which isolates what
+    # the trained network adds to the projection onto the last increment
     variants = [("fp64_plain", dict(pressure_precision=0, pressure_x0=0)),
                 ("fp64_learned", dict(pressure_precision=0, pressure_x0=1)),
+                ("fp64_untrained", dict(pressure_precision=0, pressure_x0=1, learn_steps=0)),
                 ("mixed", dict(pressure_precision=1, pressure_x0=0)),
                 ("mixed_learned", dict(pressure_precision=1, pressure_x0=1))]
     L = g.lib()
     finals = {}
     for label, kw in variants:
-        prm2 = dict(prm, pressure_criterion=1, learn_steps=args.train, learn_rate=1e-3, **kw)
+        prm2 = dict(prm, pressure_criterion=1, learn_steps=args.train, learn_rate=1e-3)
+        prm2.update(kw)
         # particles accumulate where the flow converges: room for 4x the seeded count
         eng = g.FlowEngine(m, g.default_params(**prm2), bu, bv, bp, capacity_factor=4.0)
         eng.seed()
