@@ -222,7 +222,7 @@ static pf2_status step_body(pf2_flow* F, cudaStream_t st) {
                                   ux, uy, pr, F->loads.p, st));
     F->mark(st, PF2_PHASE_PARTICLE_CORRECTION);
     if (F->guess)
-        PF2_TRY(guess_train(F->guess, pr, F->steps_done < P.learn_steps ? P.learn_rate : 0.0f, st));
+        PF2_TRY(guess_train(F->guess, F->A[2], pr, F->steps_done < P.learn_steps ? P.learn_rate : 0.0f, st));
     ++F->steps_done;
     F->assembled = true;
     if (F->tmax && F->tsteps < F->tmax) ++F->tsteps;

@@ -4,16 +4,18 @@
 //   f = ((x - x0) / L, (y - y0) / L, b / s_b, p / s_p, (p - p_prev) / s_d)
 // (b the pressure right-hand side, p the previous-step pressure, p_prev the one before;
 // s_b = max |b|, s_p = max |p|, s_d = max |p - p_prev|) and predicts the increment
-// p_new - p in units of s_d: d1 = s_d y.  With d2 = p - p_prev, the last increment, the
-// start is the Galerkin combination
-//   x0 = p + c1 d1 + c2 d2,  (D^T A D) c = D^T (b - A p),  D = [d1 d2],
-// the point of p + span{d1, d2} closest to the solution in the energy norm (A is SPD).
-// It lowers the energy norm of the error by h^T c >= 0 (h = D^T r0); a direction that
-// does not help gets a coefficient near 0, so the start is never worse than p in that
-// norm, the norm CG minimises.  (The residual norm is a poor test here: the Laplacian
-// amplifies any high-frequency error of a learned increment, so a useful increment can
-// still raise ||b - A x0||.)  While training, after the step the target
-// t = (p_new - p) / s_d drives one AdamW step on the same features.
+// p_new - p in units of s_d: d0 = s_d y.  With the last kHistory pressure increments
+// h_1 .. h_K of the run (and their images A h_k, kept when they are stored), the start
+// is the Galerkin combination
+//   x0 = p + D c,  (D^T A D) c = D^T (b - A p),  D = [d0 h_1 .. h_K],
+// the point of p + span(D) closest to the solution in the energy norm (A is SPD).  It
+// lowers the energy norm of the error by c^T D^T r0 >= 0; directions that do not help get
+// coefficients near 0, so the start is never worse than p in that norm, the norm CG
+// minimises.  (The residual norm is a poor test here: the Laplacian amplifies any
+// high-frequency error of a learned increment, so a useful increment can still raise
+// ||b - A x0||.)  While training, after the step the target t = (p_new - p) / s_d drives
+// one AdamW step on the same features.  The history ring's state lives on the device, so
+// a replayed step graph keeps it up to date.
 #include <algorithm>
 #include <cmath>
 
@@ -23,13 +25,20 @@
 
 namespace pf2 {
 
+constexpr int kHistory = 8;                 // pressure increments kept for the projection
+constexpr int kDirs = kHistory + 1;         // the network's direction first
+constexpr int kDots = 2 * kDirs + 1;        // D^T r0, D^T A d0, r0^T r0
+
 struct Guess {
     const pf2_mesh* mesh = nullptr;
     pf2_mpnn* net = nullptr;
     int n = 0;
     double x0 = 0.0, y0 = 0.0, L = 1.0;
     DevBuf<float> feat, y, target;
-    DevBuf<double> p_saved, p_prev, d1, d2, r0, a1, a2, coef, part, res;
+    DevBuf<double> p_saved, p_prev, d0, r0, a0, coef, part, res;
+    DevBuf<double> hist, ahist;             // kHistory x n increments and their images under A
+    DevBuf<double> gram;                    // kHistory x kHistory, h_i^T A h_j
+    DevBuf<int> ring;                       // {count, head}
     DevBuf<unsigned long long> scale_bits;  // max |b|, max |p|, max |p - p_prev| as ordered bit patterns
     DevBuf<int> flag;
     int blocks = 0;
@@ -73,83 +82,147 @@ __global__ void k_guess_features(int n, const double2* __restrict__ xy, double x
     p_saved[i] = p[i];
 }
 
-__global__ void k_guess_dirs(int n, const double* __restrict__ p, const double* __restrict__ pp,
-                             const float* __restrict__ y, const unsigned long long* __restrict__ s, double* d1,
-                             double* d2) {
+__global__ void k_guess_dir(int n, const float* __restrict__ y, const unsigned long long* __restrict__ s,
+                            double* d0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    d1[i] = scale_of(s[2]) * (double)y[i];
-    d2[i] = p[i] - pp[i];
+    d0[i] = scale_of(s[2]) * (double)y[i];
 }
 
-// One pass over A: r0 = b - A p, A d1, A d2 per row; per-block partials of
-// d1.Ad1, d1.Ad2, d2.Ad2, d1.r0, d2.r0, r0.r0 (6 x blocks).
-__global__ void k_guess_project(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
-                                const double* __restrict__ val, const double* __restrict__ b,
-                                const double* __restrict__ p, const double* __restrict__ d1,
-                                const double* __restrict__ d2, double* r0, double* a1, double* a2, double* part) {
-    __shared__ double sh[33 * 6];
-    double acc[6] = { 0, 0, 0, 0, 0, 0 };
+// y1 = b - A x1 (or A x1 when b is null) and y2 = A x2 (when x2 is not null), one pass over A.
+__global__ void k_guess_spmv(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                             const double* __restrict__ val, const double* __restrict__ b,
+                             const double* __restrict__ x1, const double* __restrict__ x2, double* y1, double* y2) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        double sp = 0.0, s1 = 0.0, s2 = 0.0;
+        double s1 = 0.0, s2 = 0.0;
         for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) {
             const double v = val[k];
             const int c = col[k];
-            sp += v * p[c];
-            s1 += v * d1[c];
-            s2 += v * d2[c];
+            s1 += v * x1[c];
+            if (x2) s2 += v * x2[c];
         }
-        const double ri = b[i] - sp;
-        r0[i] = ri;
-        a1[i] = s1;
-        a2[i] = s2;
-        acc[0] += d1[i] * s1;
-        acc[1] += d1[i] * s2;
-        acc[2] += d2[i] * s2;
-        acc[3] += d1[i] * ri;
-        acc[4] += d2[i] * ri;
-        acc[5] += ri * ri;
+        y1[i] = b ? b[i] - s1 : s1;
+        if (x2) y2[i] = s2;
     }
-    block_sum_n<6>(acc, sh);
+}
+
+// Per-block partials of D_j . r0 and D_j . A d0 (j < kDirs; history slots beyond the
+// ring's count give 0) and of r0 . r0.
+__global__ void k_guess_dots(int n, const double* __restrict__ d0, const double* __restrict__ hist,
+                             const int* __restrict__ ring, const double* __restrict__ r0,
+                             const double* __restrict__ a0, double* part) {
+    __shared__ double sh[33 * kDots];
+    const int cnt = ring[0];
+    double acc[kDots];
+#pragma unroll
+    for (int j = 0; j < kDots; ++j) acc[j] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double r = r0[i], a = a0[i];
+        const double d = d0[i];
+        acc[0] += d * r;
+        acc[kDirs] += d * a;
+#pragma unroll
+        for (int k = 0; k < kHistory; ++k)
+            if (k < cnt) {
+                const double h = hist[(size_t)k * n + i];
+                acc[1 + k] += h * r;
+                acc[kDirs + 1 + k] += h * a;
+            }
+        acc[2 * kDirs] += r * r;
+    }
+    block_sum_n<kDots>(acc, sh);
     if (threadIdx.x == 0)
-        for (int k = 0; k < 6; ++k) part[6 * blockIdx.x + k] = acc[k];
+        for (int j = 0; j < kDots; ++j) part[(size_t)kDots * blockIdx.x + j] = acc[j];
 }
 
-// Coefficients of the 2 x 2 Galerkin system (one thread, block partials in order);
-// coef = {c1, c2}, res[0] = ||b - A p||.
-__global__ void k_guess_solve(int nb, const double* __restrict__ part, double* coef, double* res, int* used) {
-    double t[6] = { 0, 0, 0, 0, 0, 0 };
+// The (kDirs x kDirs) Galerkin system by a Cholesky factorisation with a small relative
+// diagonal shift, directions whose pivot vanishes dropped (one thread, partials summed
+// in block order).  coef[j] for D_j, res[0] = ||b - A p||, used = the network's
+// direction got a nonzero coefficient.
+__global__ void k_guess_solve(int nb, const double* __restrict__ part, const double* __restrict__ gram,
+                              const int* __restrict__ ring, double* coef, double* res, int* used) {
+    double t[kDots];
+    for (int j = 0; j < kDots; ++j) t[j] = 0.0;
     for (int b = 0; b < nb; ++b)
-        for (int k = 0; k < 6; ++k) t[k] += part[6 * b + k];
-    const double g11 = t[0], g12 = t[1], g22 = t[2], h1 = t[3], h2 = t[4];
-    double c1 = 0.0, c2 = 0.0;
-    const double det = g11 * g22 - g12 * g12;
-    if (g11 > 0.0 && g22 > 0.0 && det > 1e-12 * g11 * g22) {
-        c1 = (g22 * h1 - g12 * h2) / det;
-        c2 = (g11 * h2 - g12 * h1) / det;
-    } else if (g11 > 0.0 && (g22 <= 0.0 || h1 * h1 / g11 >= h2 * h2 / g22)) {
-        c1 = h1 / g11;  // one usable direction: the better of the two
-    } else if (g22 > 0.0) {
-        c2 = h2 / g22;
+        for (int j = 0; j < kDots; ++j) t[j] += part[(size_t)kDots * b + j];
+    const int cnt = ring[0];
+    const int m = 1 + cnt;
+    double G[kDirs][kDirs], h[kDirs], c[kDirs];
+    for (int i = 0; i < kDirs; ++i) {
+        h[i] = t[i];
+        c[i] = 0.0;
+        for (int j = 0; j < kDirs; ++j) G[i][j] = 0.0;
     }
-    coef[0] = c1;
-    coef[1] = c2;
-    res[0] = sqrt(t[5]);
-    *used = c1 != 0.0 ? 1 : 0;
+    G[0][0] = t[kDirs];
+    for (int k = 0; k < cnt; ++k) {
+        G[0][1 + k] = G[1 + k][0] = t[kDirs + 1 + k];
+        for (int l = 0; l < cnt; ++l) G[1 + k][1 + l] = gram[k * kHistory + l];
+    }
+    double dmax = 0.0;
+    for (int i = 0; i < m; ++i) dmax = fmax(dmax, G[i][i]);
+    bool keep[kDirs];
+    // Cholesky G = R^T R in place (upper triangle), dropping near-dependent directions
+    for (int i = 0; i < m; ++i) {
+        keep[i] = false;
+        if (!(dmax > 0.0)) continue;
+        double d = G[i][i] + 1e-12 * dmax;
+        for (int k = 0; k < i; ++k)
+            if (keep[k]) d -= G[k][i] * G[k][i];
+        if (!(d > 1e-10 * (G[i][i] + 1e-300))) continue;
+        keep[i] = true;
+        const double rii = sqrt(d);
+        G[i][i] = rii;
+        for (int j = i + 1; j < m; ++j) {
+            double v = G[i][j];
+            for (int k = 0; k < i; ++k)
+                if (keep[k]) v -= G[k][i] * G[k][j];
+            G[i][j] = v / rii;
+        }
+    }
+    // R^T z = h, R c = z over the kept directions
+    double z[kDirs];
+    for (int i = 0; i < m; ++i) {
+        z[i] = 0.0;
+        if (!keep[i]) continue;
+        double v = h[i];
+        for (int k = 0; k < i; ++k)
+            if (keep[k]) v -= G[k][i] * z[k];
+        z[i] = v / G[i][i];
+    }
+    for (int i = m - 1; i >= 0; --i) {
+        if (!keep[i]) continue;
+        double v = z[i];
+        for (int j = i + 1; j < m; ++j)
+            if (keep[j]) v -= G[i][j] * c[j];
+        c[i] = v / G[i][i];
+    }
+    for (int j = 0; j < kDirs; ++j) coef[j] = c[j];
+    res[0] = sqrt(t[2 * kDirs]);
+    *used = c[0] != 0.0 ? 1 : 0;
 }
 
-// x0 = p + c1 d1 + c2 d2 (x holds p); per-block partials of ||r0 - c1 A d1 - c2 A d2||^2,
-// the residual of the start.
-__global__ void k_guess_combine(int n, const double* __restrict__ coef, const double* __restrict__ d1,
-                                const double* __restrict__ d2, const double* __restrict__ r0,
-                                const double* __restrict__ a1, const double* __restrict__ a2, double* x,
-                                double* part) {
+// x0 = p + sum_j c_j D_j (x holds p); per-block partials of ||b - A x0||^2 =
+// ||r0 - c_0 A d0 - sum_k c_k A h_k||^2.
+__global__ void k_guess_combine(int n, const double* __restrict__ coef, const double* __restrict__ d0,
+                                const double* __restrict__ a0, const double* __restrict__ hist,
+                                const double* __restrict__ ahist, const int* __restrict__ ring,
+                                const double* __restrict__ r0, double* x, double* part) {
     __shared__ double sh[40];
-    const double c1 = coef[0], c2 = coef[1];
+    const int cnt = ring[0];
+    double c[kDirs];
+#pragma unroll
+    for (int j = 0; j < kDirs; ++j) c[j] = coef[j];
     double rr = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        x[i] += c1 * d1[i] + c2 * d2[i];
-        const double ri = r0[i] - c1 * a1[i] - c2 * a2[i];
+        double dx = c[0] * d0[i], dr = c[0] * a0[i];
+#pragma unroll
+        for (int k = 0; k < kHistory; ++k)
+            if (k < cnt) {
+                dx += c[1 + k] * hist[(size_t)k * n + i];
+                dr += c[1 + k] * ahist[(size_t)k * n + i];
+            }
+        x[i] += dx;
+        const double ri = r0[i] - dr;
         rr += ri * ri;
     }
     rr = block_sum(rr, sh);
@@ -160,6 +233,59 @@ __global__ void k_guess_res1(int nb, const double* __restrict__ part, double* re
     double t = 0.0;
     for (int b = 0; b < nb; ++b) t += part[b];
     res[1] = sqrt(t);
+}
+
+// After the step: the step's increment into the ring's head slot.
+__global__ void k_guess_increment(int n, const double* __restrict__ pnew, const double* __restrict__ p,
+                                  const int* __restrict__ ring, double* hist) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    hist[(size_t)ring[1] * n + i] = pnew[i] - p[i];
+}
+
+// Images under A of the head slot (pass 1 of the insertion): ahist[head] = A hist[head].
+__global__ void k_guess_ahead(int n, const int* __restrict__ rowptr, const int* __restrict__ col,
+                              const double* __restrict__ val, const int* __restrict__ ring,
+                              const double* __restrict__ hist, double* ahist) {
+    const double* h = hist + (size_t)ring[1] * n;
+    double* ah = ahist + (size_t)ring[1] * n;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k) s += val[k] * h[col[k]];
+        ah[i] = s;
+    }
+}
+
+// Per-block partials of hist_k . A hist[head] for all k (pass 2 of the insertion).
+__global__ void k_guess_gram_dots(int n, const double* __restrict__ hist, const double* __restrict__ ahist,
+                                  const int* __restrict__ ring, double* part) {
+    __shared__ double sh[33 * kHistory];
+    const double* ah = ahist + (size_t)ring[1] * n;
+    double acc[kHistory];
+#pragma unroll
+    for (int k = 0; k < kHistory; ++k) acc[k] = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double a = ah[i];
+#pragma unroll
+        for (int k = 0; k < kHistory; ++k) acc[k] += hist[(size_t)k * n + i] * a;
+    }
+    block_sum_n<kHistory>(acc, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < kHistory; ++k) part[(size_t)kHistory * blockIdx.x + k] = acc[k];
+}
+
+// Row and column of the head slot in the Gram matrix, then advance the ring (one thread).
+// Slots not yet written hold zeros (the ring's buffers start zeroed), so their dots are 0.
+__global__ void k_guess_insert(int nb, const double* __restrict__ part, double* gram, int* ring) {
+    const int head = ring[1];
+    for (int k = 0; k < kHistory; ++k) {
+        double t = 0.0;
+        for (int b = 0; b < nb; ++b) t += part[(size_t)kHistory * b + k];
+        gram[head * kHistory + k] = t;
+        gram[k * kHistory + head] = t;
+    }
+    ring[0] = min(ring[0] + 1, kHistory);
+    ring[1] = (head + 1) % kHistory;
 }
 
 __global__ void k_guess_target(int n, const double* __restrict__ pnew, const double* __restrict__ p,
@@ -190,12 +316,16 @@ pf2_status guess_create(const pf2_mesh* m, Guess** out) {
     G->blocks = std::min((int)blocks_for(G->n), num_sms() * 4);
     const size_t n = G->n;
     if ((s = G->feat.alloc(5 * n)) || (s = G->y.alloc(n)) || (s = G->target.alloc(n)) || (s = G->p_saved.alloc(n)) ||
-        (s = G->p_prev.alloc(n)) || (s = G->d1.alloc(n)) || (s = G->d2.alloc(n)) || (s = G->r0.alloc(n)) ||
-        (s = G->a1.alloc(n)) || (s = G->a2.alloc(n)) || (s = G->coef.alloc(2)) ||
-        (s = G->part.alloc(6 * (size_t)G->blocks)) ||
+        (s = G->p_prev.alloc(n)) || (s = G->d0.alloc(n)) || (s = G->r0.alloc(n)) || (s = G->a0.alloc(n)) ||
+        (s = G->coef.alloc(kDirs)) || (s = G->part.alloc((size_t)kDots * G->blocks)) ||
+        (s = G->hist.alloc((size_t)kHistory * n)) || (s = G->ahist.alloc((size_t)kHistory * n)) ||
+        (s = G->gram.alloc(kHistory * kHistory)) || (s = G->ring.alloc(2)) ||
         (s = G->res.alloc(2)) || (s = G->scale_bits.alloc(3)) || (s = G->flag.alloc(1)))
         return fail(s);
-    if (cudaMemset(G->p_prev.p, 0, sizeof(double) * n) != cudaSuccess)
+    if (cudaMemset(G->p_prev.p, 0, sizeof(double) * n) != cudaSuccess ||
+        cudaMemset(G->hist.p, 0, G->hist.bytes()) != cudaSuccess ||
+        cudaMemset(G->ahist.p, 0, G->ahist.bytes()) != cudaSuccess ||
+        cudaMemset(G->gram.p, 0, G->gram.bytes()) != cudaSuccess || cudaMemset(G->ring.p, 0, G->ring.bytes()) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "cudaMemset", __FILE__, __LINE__));
     *out = G;
     return PF2_OK;
@@ -217,15 +347,18 @@ pf2_status guess_apply(Guess* G, const pf2_csr* A, const double* b, double* x, c
                                                          G->p_prev.p, G->scale_bits.p, G->feat.p, G->p_saved.p);
     PF2_LAUNCH_CHECK();
     PF2_TRY(pf2_mpnn_forward(G->net, G->feat.p, G->y.p, st));
-    k_guess_dirs<<<blocks_for(n), kThreads, 0, st>>>(n, x, G->p_prev.p, G->y.p, G->scale_bits.p, G->d1.p, G->d2.p);
+    k_guess_dir<<<blocks_for(n), kThreads, 0, st>>>(n, G->y.p, G->scale_bits.p, G->d0.p);
     PF2_LAUNCH_CHECK();
-    k_guess_project<<<G->blocks, kThreads, 0, st>>>(n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, b, x, G->d1.p,
-                                                    G->d2.p, G->r0.p, G->a1.p, G->a2.p, G->part.p);
+    const int* rp = A->mesh->rowptr.p;
+    const int* cl = A->mesh->col.p;
+    k_guess_spmv<<<G->blocks, kThreads, 0, st>>>(n, rp, cl, A->val.p, b, x, G->d0.p, G->r0.p, G->a0.p);
     PF2_LAUNCH_CHECK();
-    k_guess_solve<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->coef.p, G->res.p, G->flag.p);
+    k_guess_dots<<<G->blocks, kThreads, 0, st>>>(n, G->d0.p, G->hist.p, G->ring.p, G->r0.p, G->a0.p, G->part.p);
     PF2_LAUNCH_CHECK();
-    k_guess_combine<<<G->blocks, kThreads, 0, st>>>(n, G->coef.p, G->d1.p, G->d2.p, G->r0.p, G->a1.p, G->a2.p, x,
-                                                    G->part.p);
+    k_guess_solve<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->gram.p, G->ring.p, G->coef.p, G->res.p, G->flag.p);
+    PF2_LAUNCH_CHECK();
+    k_guess_combine<<<G->blocks, kThreads, 0, st>>>(n, G->coef.p, G->d0.p, G->a0.p, G->hist.p, G->ahist.p, G->ring.p,
+                                                    G->r0.p, x, G->part.p);
     PF2_LAUNCH_CHECK();
     k_guess_res1<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->res.p);
     PF2_LAUNCH_CHECK();
@@ -234,8 +367,18 @@ pf2_status guess_apply(Guess* G, const pf2_csr* A, const double* b, double* x, c
     return PF2_OK;
 }
 
-pf2_status guess_train(Guess* G, const double* p_new, float lr, cudaStream_t st) {
+pf2_status guess_train(Guess* G, const pf2_csr* A, const double* p_new, float lr, cudaStream_t st) {
     const int n = G->n;
+    // the step's increment joins the history (before p_saved is consumed below)
+    k_guess_increment<<<blocks_for(n), kThreads, 0, st>>>(n, p_new, G->p_saved.p, G->ring.p, G->hist.p);
+    PF2_LAUNCH_CHECK();
+    k_guess_ahead<<<G->blocks, kThreads, 0, st>>>(n, A->mesh->rowptr.p, A->mesh->col.p, A->val.p, G->ring.p,
+                                                  G->hist.p, G->ahist.p);
+    PF2_LAUNCH_CHECK();
+    k_guess_gram_dots<<<G->blocks, kThreads, 0, st>>>(n, G->hist.p, G->ahist.p, G->ring.p, G->part.p);
+    PF2_LAUNCH_CHECK();
+    k_guess_insert<<<1, 1, 0, st>>>(G->blocks, G->part.p, G->gram.p, G->ring.p);
+    PF2_LAUNCH_CHECK();
     k_guess_target<<<blocks_for(n), kThreads, 0, st>>>(n, p_new, G->p_saved.p, G->scale_bits.p, G->target.p,
                                                        G->p_prev.p);
     PF2_LAUNCH_CHECK();

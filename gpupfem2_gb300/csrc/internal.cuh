@@ -52,11 +52,12 @@ struct Guess;
 pf2_status guess_create(const pf2_mesh* m, Guess** out);
 void guess_destroy(Guess* g);
 // Before the first pressure solve of a step: features from (x, y, b, p, p_prev), the
-// network's candidate x0, and x <- the candidate if its residual ||b - A x0|| is smaller
-// than that of x (the previous-step pressure).  Residuals go to res_out[2].
+// network's increment, and x <- the energy-norm Galerkin start over the network's
+// increment and the stored increments.  ||b - A p|| and ||b - A x0|| go to res_out[2].
 pf2_status guess_apply(Guess* g, const pf2_csr* A, const double* b, double* x, const double* p_prev,
                        double* res_out, int* used_out, cudaStream_t st);
-// After the step: one AdamW step on the target (p_new - p) of the features of guess_apply.
-pf2_status guess_train(Guess* g, const double* p_new, float lr, cudaStream_t st);
+// After the step: the step's increment p_new - p joins the history (with A times it), then
+// one AdamW step (lr > 0) on the target (p_new - p) of the features of guess_apply.
+pf2_status guess_train(Guess* g, const pf2_csr* A, const double* p_new, float lr, cudaStream_t st);
 
 }  // namespace pf2
