@@ -160,7 +160,9 @@ typedef struct pf2_params {
     double thickness, mean_velocity;
     double body_cx, body_cy; /* body centre for the load normals (0.2, 0.2 in Cylinder2D/main.cu:344) */
     int pressure_precision;  /* PF2_PRECISION_* for the pressure solve */
-    int pressure_x0;         /* PF2_X0_* for the pressure solve */
+    int pressure_x0;         /* PF2_X0_* for the pressure solve: GIVEN starts from the previous
+                                pressure p (the reference); LEARNED from the energy-norm Galerkin
+                                start over the network's increment and the last 8 increments */
     int gmres_restart;       /* Krylov dimension of the prediction GMRES, 0 = no restart */
     int pressure_criterion;  /* PF2_CRITERION_* of the pressure solve */
     int learn_steps;         /* PF2_X0_LEARNED: train the network on the first learn_steps steps */
@@ -366,8 +368,8 @@ typedef struct pf2_step_info {
     int converged;       /* all solves converged */
     int status;          /* first device-side error (pf2_status) */
     double cx, cy;       /* loads, when calculate_loads */
-    int guess_used;      /* PF2_X0_LEARNED: 1 if the network's guess started the pressure solve */
-    double guess_residual[2]; /* ||b - A x0|| of the previous-step guess and of the network's */
+    int guess_used;      /* PF2_X0_LEARNED: 1 if the network's increment got a nonzero coefficient */
+    double guess_residual[2]; /* ||b - A p|| of the previous pressure and ||b - A x0|| of the start */
 } pf2_step_info;
 /* Statistics of the last completed step. Synchronises. */
 pf2_status pf2_flow_step_info(pf2_flow* f, pf2_step_info* info);
