@@ -72,9 +72,8 @@ struct BandDir {
     const int* sptr;
     const int* row;    // [slot]
     const int* rhs;    // [slot] right-hand side index (A's numbering forward, B's backward)
-    const int* off;    // [slot + 1] start of the slot's dependencies
-    const int* dep;    // [off[slot] .. off[slot + 1]) dependency rows
-    double* val;       // factor values of the dependencies
+    const int* dep;    // [slot * K + k]
+    double* val;       // [slot * K + k] factor values
     double* dinv;      // [slot] 1 / dividing diagonal (1 for ILU forward)
     float* val32;      // FP32 copies (mixed precision)
     float* dinv32;
@@ -249,11 +248,10 @@ __device__ __forceinline__ void band_prefetch(const BandDir& D, int K, int t) {
     prefetch_l1(D.row + t);
     prefetch_l1(D.rhs + t);
     prefetch_l1(BandVals<V>::dinv(D) + t);
-    (void)K;
-    const int o = __ldg(&D.off[t]);
-    prefetch_l1(D.off + t + 1);
-    prefetch_l1(D.dep + o);
-    prefetch_l1(BandVals<V>::val(D) + o);
+    prefetch_l1(D.dep + (size_t)t * K);
+    prefetch_l1(D.dep + (size_t)t * K + K - 1);
+    prefetch_l1(BandVals<V>::val(D) + (size_t)t * K);
+    prefetch_l1(BandVals<V>::val(D) + (size_t)t * K + K - 1);
 }
 
 template <class V>
@@ -297,10 +295,10 @@ __device__ bool tri_solve_banded(const Tri& T, int dir, V* src, V* dst, int* err
                 const V di = __ldg(&dinv[t]);
                 V sum = V(0);
                 bool ok = true;
-                const int o0 = __ldg(&D.off[t]), o1 = __ldg(&D.off[t + 1]);
-                for (int k = o0; k < o1; ++k) {
-                    const int j = __ldg(&D.dep[k]);
-                    const V f = __ldg(&vals[k]);
+                for (int k = 0; k < K; ++k) {
+                    const int j = __ldg(&D.dep[(size_t)t * K + k]);
+                    if (j < 0) break;
+                    const V f = __ldg(&vals[(size_t)t * K + k]);
                     V xj;
                     if (j >= r0 && j < r1) {
                         xj = xs[j - r0];
@@ -373,8 +371,7 @@ __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err)
         const V in = __ldcg(&src[__ldg(&D.rhs[t])]);
         const V di = __ldg(&dinv[t]);
         V sum;
-        const int o0 = __ldg(&D.off[t]), o1 = __ldg(&D.off[t + 1]);
-        if (!slot_dot(dst, D.dep + o0, vals + o0, o1 - o0, row, err, T.rec, sum)) return;
+        if (!slot_dot(dst, D.dep + (size_t)t * K, vals + (size_t)t * K, K, row, err, T.rec, sum)) return;
         __stcg(&dst[row], (in - sum) * di);
         if (dir == 1) __stcg(&src[row], Pending<V>::marker());
     }
@@ -988,8 +985,7 @@ __global__ void k_precond_apply(KArgs a) {
 using namespace pf2;
 
 struct BandHost {
-    DevBuf<int> rstep, sptr, row, rhs, off, dep, pos, dpos;
-    long long nent = 0;  // dependency entries
+    DevBuf<int> rstep, sptr, row, rhs, dep, pos, dpos;
     DevBuf<double> val, dinv;
     DevBuf<float> val32, dinv32;
 };
@@ -1206,36 +1202,29 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             }
             rstep[P] = (int)sptr.size();
             sptr.push_back(n);
-            std::vector<int> rhs(n), off(n + 1, 0), dep, pos, dpos(n, -1);
-            dep.reserve((size_t)n * 4);
-            pos.reserve((size_t)n * 4);
+            std::vector<int> rhs(n), dep((size_t)n * K, -1), pos((size_t)n * K, -1), dpos(n, -1);
             for (int t = 0; t < n; ++t) {
                 const int i = srow[t];
                 rhs[t] = dir == 0 ? perm[i] : i;
+                int c = 0;
                 deps(dir, i, [&](int j, int k) {
-                    dep.push_back(j);
-                    pos.push_back(k);
+                    dep[(size_t)t * K + c] = j;
+                    pos[(size_t)t * K + c] = k;
+                    ++c;
                 });
-                off[t + 1] = (int)dep.size();
                 dpos[t] = (dir == 1 || ic) ? bdiag[i] : -1;
-            }
-            if (dep.empty()) {
-                dep.push_back(-1);
-                pos.push_back(-1);
             }
             PF2_TRY(up(H.rstep, rstep));
             PF2_TRY(up(H.sptr, sptr));
             PF2_TRY(up(H.row, srow));
             PF2_TRY(up(H.rhs, rhs));
-            PF2_TRY(up(H.off, off));
             PF2_TRY(up(H.dep, dep));
             PF2_TRY(up(H.pos, pos));
             PF2_TRY(up(H.dpos, dpos));
-            H.nent = (long long)dep.size();
-            PF2_TRY(H.val.alloc(dep.size()));
+            PF2_TRY(H.val.alloc((size_t)n * K));
             PF2_TRY(H.dinv.alloc(n));
             if (S->opt.precision == PF2_PRECISION_MIXED) {
-                PF2_TRY(H.val32.alloc(dep.size()));
+                PF2_TRY(H.val32.alloc((size_t)n * K));
                 PF2_TRY(H.dinv32.alloc(n));
             }
         }
@@ -1253,8 +1242,7 @@ static Csr csr_of(const pf2_csr* A) {
 
 static Tri tri_of(pf2_solver* S) {
     auto dir = [&](BandHost& H) {
-        return BandDir{ H.rstep.p, H.sptr.p, H.row.p, H.rhs.p, H.off.p, H.dep.p, H.val.p, H.dinv.p, H.val32.p,
-                        H.dinv32.p };
+        return BandDir{ H.rstep.p, H.sptr.p, H.row.p, H.rhs.p, H.dep.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p };
     };
     const Band band{ S->band_P, S->band_R, S->band_K, S->band_rs.p, dir(S->band[0]), dir(S->band[1]) };
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
@@ -1326,8 +1314,8 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 1);
     PF2_LAUNCH_CHECK();
     if (S->band_K) {
+        const long long nk = (long long)S->n * S->band_K;
         for (BandHost& H : S->band) {
-            const long long nk = H.nent;
             k_band_values<<<std::min((int)blocks_for(nk), num_sms() * 8), kThreads, 0, st>>>(
                 nk, S->n, H.pos.p, H.dpos.p, S->fact.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p);
             PF2_LAUNCH_CHECK();
