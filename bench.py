@@ -444,6 +444,15 @@ def main():
         unit_desc = dominant
     dom_ms = phase_ms[dominant]
     achieved = (algo / (dom_ms * 1e-3) / 1e9) if algo else None
+    # DRAM traffic of one launch of the dominant kernel, from the committed ncu capture
+    # (a smaller case of the same kernel, scaled by rows)
+    traffic, traffic_note = None, None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if dominant == "pressure_solve" and os.path.exists(tpath):
+        t = json.load(open(tpath)).get("pressure_solve")
+        if t:
+            traffic = t["dram_bytes_per_launch"] / t["rows"] * n
+            traffic_note = t["source"]
     line = {
         "metric": "ms per PFEM-2 step", "value": ms, "unit": "ms/step", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
@@ -472,7 +481,8 @@ def main():
             "pressure_ms_per_solve": phase_ms["pressure_solve"] / prm["n_outer"]},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel_phase": dominant, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "traffic_per": "bytes per launch (one pressure solve)", "traffic_source": traffic_note,
                      "peak_source": peak_kind, "algorithmic": unit_desc},
         "clocks": clocks.summary(),
     }
