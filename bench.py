@@ -280,16 +280,21 @@ def study_learned(args):
             eng.step()
         eng.info()
         g._check(L.pf2_flow_enable_timing(eng.h, args.eval), "timing")
-        its, used = [], 0
+        its, its_first, ratios, used = [], [], [], 0
         for _ in range(args.eval):
             eng.step()
             inf = eng.info()
             its.append(inf.it_pressure[0] + inf.it_pressure[1])
+            its_first.append(inf.it_pressure[0])
+            if inf.guess_residual[0] > 0:
+                ratios.append(inf.guess_residual[1] / inf.guess_residual[0])
             used += inf.guess_used
         ph = (ctypes.c_double * 9)()
         nst = ctypes.c_int()
         g._check(L.pf2_flow_phase_times(eng.h, ph, ctypes.byref(nst)), "phase times")
         res[label] = {"pressure_ms_per_step": ph[5] / max(nst.value, 1), "iterations_per_step": statistics.mean(its),
+                      "iterations_first_solve": statistics.mean(its_first),
+                      "start_residual_ratio": statistics.mean(ratios) if ratios else None,
                       "guess_used_steps": used, "cx": inf.cx, "cy": inf.cy, "particles": inf.particles}
         print(label, json.dumps(res[label]), file=sys.stderr, flush=True)
         finals[label] = (eng.field("p"), eng.field("ux"))
