@@ -377,6 +377,55 @@ __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err)
     }
 }
 
+// One CG iteration's preconditioner work on the slot path, fused with its vector
+// updates (FP64 PCG, few-level orderings): the forward sweep updates x and r of its row
+// (x += alpha p, r -= alpha q) before it solves with the new r, and resets the backward
+// vector; the backward sweep writes z in A's numbering and the terms of r.z.  Rows are
+// owned by slots here, not by block row ranges, so every vector crossing between the two
+// is read through L2.  Returns this thread's r.r (forward) or r.z (backward) terms.
+__device__ double slots_fwd_cg(const Tri& T, double alpha, double* r, const double* q, double* x, const double* p,
+                               int* err) {
+    const BandDir& D = T.band.f;
+    const int K = T.band.K;
+    const int n = T.B.n;
+    const int stride = gridDim.x * blockDim.x;
+    double rr = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int row = __ldg(&D.row[t]);
+        const int ai = __ldg(&D.rhs[t]);  // the row in A's numbering
+        const double ra = __ldcg(&r[ai]) - alpha * __ldcg(&q[ai]);
+        __stcg(&r[ai], ra);
+        __stcg(&x[ai], __ldcg(&x[ai]) + alpha * __ldcg(&p[ai]));
+        rr += ra * ra;
+        double sum;
+        if (!slot_dot(T.tmp, D.dep + (size_t)t * K, D.val + (size_t)t * K, K, row, err, T.rec, sum)) return rr;
+        __stcg(&T.tmp[row], (ra - sum) * __ldg(&D.dinv[t]));
+        __stcg(&T.outB[row], Pending<double>::marker());
+    }
+    return rr;
+}
+
+__device__ double slots_bwd_cg(const Tri& T, const double* r, double* z, int* err) {
+    const BandDir& D = T.band.b;
+    const int K = T.band.K;
+    const int n = T.B.n;
+    const int stride = gridDim.x * blockDim.x;
+    double rz = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int row = __ldg(&D.row[t]);
+        const double in = __ldcg(&T.tmp[row]);
+        double sum;
+        if (!slot_dot(T.outB, D.dep + (size_t)t * K, D.val + (size_t)t * K, K, row, err, T.rec, sum)) return rz;
+        const double v = (in - sum) * __ldg(&D.dinv[t]);
+        __stcg(&T.outB[row], v);
+        __stcg(&T.tmp[row], Pending<double>::marker());
+        const int ai = __ldg(&T.perm[row]);
+        __stcg(&z[ai], v);
+        rz += __ldcg(&r[ai]) * v;
+    }
+    return rz;
+}
+
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
 // per warp in level order, lane 0 working through the row.
 __global__ void k_factor(Tri T, const int* __restrict__ order, unsigned* ticket, const int* epoch_ptr, int* err) {
@@ -517,13 +566,14 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
 // SolverCG::solve (linear_solver.cu:440-515).  Per iteration: q = A p with p.q (one fused
 // barrier-reduction), x/r update, z = M^{-1} r with r.z (and r.r) (one fused
 // barrier-reduction), p = z + beta p (one barrier).
-__global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[kShDoubles];
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
+    const bool fused = global_pc && a.T.band.P == 0 && a.T.band.K > 0;  // slot sweeps fused with the updates
     const bool rel = a.criterion == PF2_CRITERION_REL;
     // Jacobi: inverse diagonal (PreconditionerJacobi::initialize, preconditioners.cu:3-14)
     if (a.precond == PF2_PRECOND_JACOBI)
@@ -566,7 +616,12 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
-        if (global_pc) {
+        if (fused) {
+            // 4 barriers per iteration: (p.q), forward -> backward, (r.z, r.r), p update
+            g2[1] = slots_fwd_cg(a.T, alpha, a.r, a.q, a.x, a.p, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            g2[0] = slots_bwd_cg(a.T, a.r, a.z, a.bar.err);
+        } else if (global_pc) {
             for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
                 a.x[i] += alpha * a.p[i];
                 a.r[i] -= alpha * a.q[i];
@@ -597,7 +652,7 @@ __global__ void __launch_bounds__(kSolverThreads) k_pcg(KArgs a) {
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
         const double beta = gnew / gamma;
         gamma = gnew;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = a.z[i] + beta * a.p[i];
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = __ldcg(&a.z[i]) + beta * a.p[i];
         if (!grid_sync(a.bar, gridDim.x)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -654,7 +709,7 @@ __device__ bool grid_reduce_vec(const KArgs& a, double* vals, int K, double* sh)
 // projections taken one after another on the updated vector, Givens rotations
 // (updateHcolumn :40-66), stop on |beta_k| < tol; x changes only on convergence.  With
 // m < maxit the Krylov space restarts every m iterations.
-__global__ void __launch_bounds__(kSolverThreads) k_gmres(KArgs a) {
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_gmres(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[kShDoubles];
@@ -845,7 +900,7 @@ __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, in
 // the iteration continues from the true residual with its search direction kept, so the
 // Krylov space is not restarted.  On GB300 the FP32 iteration also stays off the small
 // FP64 pipe.  a.inner_eta is the refinement trigger (the drop of the iterated residual).
-__global__ void __launch_bounds__(kSolverThreads) k_pcg_mixed(KArgs a) {
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixed(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[kShDoubles];
