@@ -383,47 +383,68 @@ __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err)
 // vector; the backward sweep writes z in A's numbering and the terms of r.z.  Rows are
 // owned by slots here, not by block row ranges, so every vector crossing between the two
 // is read through L2.  Returns this thread's r.r (forward) or r.z (backward) terms.
-__device__ double slots_fwd_cg(const Tri& T, double alpha, double* r, const double* q, double* x, const double* p,
-                               int* err) {
+template <class V> struct SlotVecs;
+template <> struct SlotVecs<double> {
+    __device__ static double* tmp(const Tri& T) { return T.tmp; }
+    __device__ static double* outB(const Tri& T) { return T.outB; }
+};
+template <> struct SlotVecs<float> {
+    __device__ static float* tmp(const Tri& T) { return T.tmp32; }
+    __device__ static float* outB(const Tri& T) { return T.outB32; }
+};
+
+// V = double for the FP64 PCG (x the solution), float for the mixed one (x the FP32
+// update d); the thread's terms are summed in V and returned in FP64.
+template <class V>
+__device__ double slots_fwd_cg(const Tri& T, V alpha, V* r, const V* q, V* x, const V* p, int* err) {
     const BandDir& D = T.band.f;
     const int K = T.band.K;
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
-    double rr = 0.0;
+    const V* vals = BandVals<V>::val(D);
+    const V* dinv = BandVals<V>::dinv(D);
+    V* tmp = SlotVecs<V>::tmp(T);
+    V* outB = SlotVecs<V>::outB(T);
+    V rr = V(0);
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
         const int row = __ldg(&D.row[t]);
         const int ai = __ldg(&D.rhs[t]);  // the row in A's numbering
-        const double ra = __ldcg(&r[ai]) - alpha * __ldcg(&q[ai]);
+        const V ra = __ldcg(&r[ai]) - alpha * __ldcg(&q[ai]);
         __stcg(&r[ai], ra);
         __stcg(&x[ai], __ldcg(&x[ai]) + alpha * __ldcg(&p[ai]));
         rr += ra * ra;
-        double sum;
-        if (!slot_dot(T.tmp, D.dep + (size_t)t * K, D.val + (size_t)t * K, K, row, err, T.rec, sum)) return rr;
-        __stcg(&T.tmp[row], (ra - sum) * __ldg(&D.dinv[t]));
-        __stcg(&T.outB[row], Pending<double>::marker());
+        V sum;
+        if (!slot_dot(tmp, D.dep + (size_t)t * K, vals + (size_t)t * K, K, row, err, T.rec, sum)) break;
+        __stcg(&tmp[row], (ra - sum) * __ldg(&dinv[t]));
+        __stcg(&outB[row], Pending<V>::marker());
     }
-    return rr;
+    return (double)rr;
 }
 
-__device__ double slots_bwd_cg(const Tri& T, const double* r, double* z, int* err) {
+template <class V>
+__device__ double slots_bwd_cg(const Tri& T, const V* r, V* z, int* err) {
     const BandDir& D = T.band.b;
     const int K = T.band.K;
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
-    double rz = 0.0;
+    const V* vals = BandVals<V>::val(D);
+    const V* dinv = BandVals<V>::dinv(D);
+    V* tmp = SlotVecs<V>::tmp(T);
+    V* outB = SlotVecs<V>::outB(T);
+    V rz = V(0);
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
         const int row = __ldg(&D.row[t]);
-        const double in = __ldcg(&T.tmp[row]);
-        double sum;
-        if (!slot_dot(T.outB, D.dep + (size_t)t * K, D.val + (size_t)t * K, K, row, err, T.rec, sum)) return rz;
-        const double v = (in - sum) * __ldg(&D.dinv[t]);
-        __stcg(&T.outB[row], v);
-        __stcg(&T.tmp[row], Pending<double>::marker());
+        const V in = __ldcg(&tmp[row]);
+        V sum;
+        if (!slot_dot(outB, D.dep + (size_t)t * K, vals + (size_t)t * K, K, row, err, T.rec, sum)) break;
+        const V v = (in - sum) * __ldg(&dinv[t]);
+        __stcg(&outB[row], v);
+        __stcg(&tmp[row], Pending<V>::marker());
         const int ai = __ldg(&T.perm[row]);
         __stcg(&z[ai], v);
         rz += __ldcg(&r[ai]) * v;
     }
-    return rz;
+    return (double)rz;
 }
 
 // Zero-fill factorisations on the CSR pattern (csrilu02 / csric02 semantics), one row
@@ -618,9 +639,9 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
         double g2[2] = { 0.0, 0.0 };
         if (fused) {
             // 4 barriers per iteration: (p.q), forward -> backward, (r.z, r.r), p update
-            g2[1] = slots_fwd_cg(a.T, alpha, a.r, a.q, a.x, a.p, a.bar.err);
+            g2[1] = slots_fwd_cg<double>(a.T, alpha, a.r, a.q, a.x, a.p, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return;
-            g2[0] = slots_bwd_cg(a.T, a.r, a.z, a.bar.err);
+            g2[0] = slots_bwd_cg<double>(a.T, a.r, a.z, a.bar.err);
         } else if (global_pc) {
             for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
                 a.x[i] += alpha * a.p[i];
@@ -907,6 +928,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixe
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
+    const bool fused = global_pc && a.T.band.P == 0 && a.T.band.K > 0;  // slot sweeps fused with the updates
     // r = b - A x (FP64), r32 = r, d = 0, inverse diagonal
     double red[2] = { 0.0, 0.0 };  // b.b, r.r
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -951,7 +973,12 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixe
             const float alpha = (float)(gamma / pq[0]);
             // d += alpha p, r -= alpha q, z = M^{-1} r, r.z and r.r
             float gl2 = 0.0f, rl2 = 0.0f;
-            if (global_pc) {
+            double g2[2] = { 0.0, 0.0 };
+            if (fused) {
+                g2[1] = slots_fwd_cg<float>(a.T, alpha, a.r32, a.q32, a.d32, a.p32, a.bar.err);
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                g2[0] = slots_bwd_cg<float>(a.T, a.r32, a.z32, a.bar.err);
+            } else if (global_pc) {
                 for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
                     a.d32[i] = fmaf(alpha, a.p32[i], a.d32[i]);
                     const float ri = fmaf(-alpha, a.q32[i], a.r32[i]);
@@ -973,15 +1000,18 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixe
                     rl2 = fmaf(ri, ri, rl2);
                 }
             }
-            double g2[2] = { (double)gl2, (double)rl2 };
+            if (!fused) {
+                g2[0] = (double)gl2;
+                g2[1] = (double)rl2;
+            }
             if (!grid_reduce<2>(a.bar, g2, sh)) return;
             double gnew = g2[0];
             const double rit = sqrt(g2[1]);
             if (rit <= a.inner_eta * rlast || rit <= target) {
                 // refinement: x += d (own rows), r = b - A x and the convergence test in FP64
                 for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-                    a.x[i] += (double)a.d32[i];
-                    a.d32[i] = 0.0f;
+                    a.x[i] += (double)__ldcg(&a.d32[i]);  // d may come from other blocks' slots
+                    __stcg(&a.d32[i], 0.0f);
                 }
                 if (!grid_sync(a.bar, gridDim.x)) return;
                 double rr[1] = { 0.0 };
@@ -999,19 +1029,19 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixe
                 if (global_pc && !grid_sync(a.bar, gridDim.x)) return;
                 if (!precond_apply32(a, a.r32, a.z32, r0, r1, apply++, ep_base)) return;
                 float gl3 = 0.0f;
-                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gl3 = fmaf(a.r32[i], a.z32[i], gl3);
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) gl3 = fmaf(a.r32[i], __ldcg(&a.z32[i]), gl3);
                 double g3[1] = { (double)gl3 };
                 if (!grid_reduce<1>(a.bar, g3, sh)) return;
                 gnew = g3[0];
             }
             const float beta = (float)(gnew / gamma);
             gamma = gnew;
-            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p32[i] = fmaf(beta, a.p32[i], a.z32[i]);
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p32[i] = fmaf(beta, a.p32[i], __ldcg(&a.z32[i]));
             if (!grid_sync(a.bar, gridDim.x)) return;
         }
         if (!conv) {
             // iteration limit: keep the accumulated update
-            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[i] += (double)a.d32[i];
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[i] += (double)__ldcg(&a.d32[i]);
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
