@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
 
 // out[i] = this block's part of w . V_i (rows r0..r1), i < K; warp q takes i = q, q + 8, ...
 __device__ __forceinline__ void block_dots(const double* V, int n, int K, const double* w, int r0, int r1,
-                                           double* out) {
+                                           double* out, bool with_norm = false) {
     const int lane = threadIdx.x & 31, wq = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int i = wq; i < K; i += nw) {
         const double* vi = V + (size_t)i * n;
@@ -703,6 +703,12 @@ __device__ __forceinline__ void block_dots(const double* V, int n, int K, const 
         double d = (d0 + d1) + (d2 + d3);
         d = warp_sum(d);
         if (lane == 0) out[i] = d;
+    }
+    if (with_norm && wq == K % nw) {  // out[K] = w . w
+        double d = 0.0;
+        for (int j = r0 + lane; j < r1; j += 32) d += w[j] * w[j];
+        d = warp_sum(d);
+        if (lane == 0) out[K] = d;
     }
     __syncthreads();
 }
@@ -785,17 +791,29 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_gmres(KA
             if (!precond_apply(a, a.q, vkp, r0, r1, apply++, ep_base)) return;
             __syncthreads();
             if (a.gs == PF2_GS_CLASSICAL_TWICE) {
-                // h = V^T v_{k+1}, v_{k+1} -= V h, twice; the second pass's h is added
+                // h = V^T v_{k+1}, v_{k+1} -= V h; a second pass (its h added) unless the
+                // first kept ||v_{k+1}|| above 0.7 of its value (the DGKS test: then one
+                // pass is already orthogonal to working accuracy)
                 for (int pass = 0; pass < 2; ++pass) {
                     double* hv = pass == 0 ? hcol : h2;
-                    block_dots(a.V, n, k + 1, vkp, r0, r1, hv);
-                    if (!grid_reduce_vec(a, hv, k + 1, sh)) return;
+                    block_dots(a.V, n, k + 1, vkp, r0, r1, hv, pass == 0);
+                    if (!grid_reduce_vec(a, hv, pass == 0 ? k + 2 : k + 1, sh)) return;
                     for (int j = r0 + threadIdx.x; j < r1; j += blockDim.x) {
                         double v = vkp[j];
                         for (int i = 0; i <= k; ++i) v -= hv[i] * a.V[(size_t)i * n + j];
                         vkp[j] = v;
                     }
                     __syncthreads();
+                    if (pass == 0) {
+                        double hh = 0.0;
+                        for (int i = 0; i <= k; ++i) hh += hv[i] * hv[i];
+                        const double ww = hv[k + 1];
+                        if (ww - hh > 0.49 * ww) {  // uniform: every block holds the same totals
+                            for (int i = threadIdx.x; i <= k; i += blockDim.x) h2[i] = 0.0;
+                            __syncthreads();
+                            break;
+                        }
+                    }
                 }
                 for (int i = threadIdx.x; i <= k; i += blockDim.x) hcol[i] += h2[i];
                 __syncthreads();
