@@ -372,6 +372,14 @@ class ParticleHandler2D:
         arr["cell"] = cell
         return arr
 
+    def save(self, path):
+        """Checkpoint of the particle state (pf2_particles_save)."""
+        _check(lib().pf2_particles_save(self.h, str(path).encode()), "pf2_particles_save")
+
+    def load(self, path):
+        """Restores a checkpoint written by save() for the same mesh and level."""
+        _check(lib().pf2_particles_load(self.h, str(path).encode()), "pf2_particles_load")
+
     def upload(self, P):
         n = int(P["cell"].size)
         a = {k: np.ascontiguousarray(P[k], dtype=np.float64) for k in self.FIELDS}
@@ -430,6 +438,15 @@ class FlowEngine:
     def set_graphs(self, enable):
         _check(lib().pf2_flow_set_graphs(self.h, int(enable)), "pf2_flow_set_graphs")
 
+    def save(self, path):
+        """Checkpoint between steps (pf2_flow_save)."""
+        _check(lib().pf2_flow_save(self.h, str(path).encode(), _stream()), "pf2_flow_save")
+
+    def load(self, path):
+        """Restores a checkpoint into an engine built with the same mesh, parameters and
+        Dirichlet sets; the following steps repeat the saved run's."""
+        _check(lib().pf2_flow_load(self.h, str(path).encode(), _stream()), "pf2_flow_load")
+
     def info(self):
         info = StepInfo()
         _check(lib().pf2_flow_step_info(self.h, C.byref(info)), "pf2_flow_step_info")
@@ -482,6 +499,12 @@ class LearnedGuess:
     def set_params(self, p):
         p = np.ascontiguousarray(p, dtype=np.float32)
         _check(lib().pf2_mpnn_set_params(self.h, p.ctypes.data_as(C.c_void_p)), "pf2_mpnn_set_params")
+
+    def save(self, path):
+        _check(lib().pf2_mpnn_save(self.h, str(path).encode()), "pf2_mpnn_save")
+
+    def load(self, path):
+        _check(lib().pf2_mpnn_load(self.h, str(path).encode()), "pf2_mpnn_load")
 
     def forward(self, feat, y):
         _check(lib().pf2_mpnn_forward(self.h, _dev(feat), _dev(y), _stream()), "pf2_mpnn_forward")

@@ -337,6 +337,54 @@ pf2_status pf2_flow_upload_field(pf2_flow* F, int which, const double* src) {
     return PF2_OK;
 }
 
+// Checkpoint sections: sizes and step count, the eight node fields, the boundary values
+// of the three Dirichlet sets, the particles, and the learned guess when there is one.
+// The matrices, right-hand sides and solver work are rebuilt by the next step from these
+// (assembly and solves are deterministic), so a run restarted from a checkpoint repeats
+// the uninterrupted run bit for bit.
+static pf2_status flow_checkpoint(pf2_flow* F, CkptFile& io, cudaStream_t st) {
+    const pf2_mesh* M = F->mesh;
+    long long meta[6] = { M->nv, M->nc, F->P.level, F->P.scheme, F->guess ? 1 : 0, F->steps_done };
+    const long long want[5] = { meta[0], meta[1], meta[2], meta[3], meta[4] };
+    PF2_TRY(io.host("fmeta", meta, sizeof(meta)));
+    for (int k = 0; k < 5; ++k)
+        PF2_REQUIRE(meta[k] == want[k], PF2_BAD_INPUT,
+                    "checkpoint flow (nodes %lld, cells %lld, level %lld, scheme %lld, learned guess %lld) does "
+                    "not match this engine (%lld, %lld, %lld, %lld, %lld)",
+                    meta[0], meta[1], meta[2], meta[3], meta[4], want[0], want[1], want[2], want[3], want[4]);
+    PF2_CUDA(cudaStreamSynchronize(st));
+    for (int k = 0; k < 8; ++k) {
+        char tag[8];
+        snprintf(tag, sizeof(tag), "field%d", k);
+        PF2_TRY(io.device(tag, F->f[k].p, sizeof(double) * M->nv, st));
+    }
+    for (int k = 0; k < 3; ++k) {
+        char tag[8];
+        snprintf(tag, sizeof(tag), "bcval%d", k);
+        PF2_TRY(io.device(tag, F->bc[k]->value.p, sizeof(double) * F->bc[k]->n_bc, st));
+    }
+    PF2_TRY(particles_checkpoint(F->ph, io, st));
+    if (F->guess) PF2_TRY(guess_checkpoint(F->guess, io, st));
+    if (!io.writing()) F->steps_done = meta[5];
+    return PF2_OK;
+}
+
+pf2_status pf2_flow_save(pf2_flow* F, const char* path, void* stream) {
+    PF2_REQUIRE(F && path, PF2_BAD_INPUT, "null argument");
+    CkptFile io;
+    PF2_TRY(io.open_write(path, CKPT_FLOW));
+    PF2_TRY(flow_checkpoint(F, io, as_stream(stream)));
+    return io.close();
+}
+
+pf2_status pf2_flow_load(pf2_flow* F, const char* path, void* stream) {
+    PF2_REQUIRE(F && path, PF2_BAD_INPUT, "null argument");
+    CkptFile io;
+    PF2_TRY(io.open_read(path, CKPT_FLOW));
+    PF2_TRY(flow_checkpoint(F, io, as_stream(stream)));
+    return io.close();
+}
+
 pf2_status pf2_flow_set_boundary_values(pf2_flow* F, int which, const double* values, void* stream) {
     PF2_REQUIRE(F && which >= 0 && which < 3, PF2_BAD_INPUT, "bad boundary set");
     return pf2_bc_set_values(F->bc[which], values, stream);

@@ -331,6 +331,21 @@ pf2_status guess_create(const pf2_mesh* m, Guess** out) {
     return PF2_OK;
 }
 
+// Sections: the previous pressure, the increment history with its images under A, their
+// Gram matrix and ring position, then the network.  The rest of the guess's buffers are
+// written before they are read within a step.
+pf2_status guess_checkpoint(Guess* G, CkptFile& io, cudaStream_t st) {
+    int n = G->n;
+    PF2_TRY(io.host("gmeta", &n, sizeof(n)));
+    PF2_REQUIRE(n == G->n, PF2_BAD_INPUT, "checkpoint guess has %d nodes, this mesh %d", n, G->n);
+    PF2_TRY(io.device("gpprev", G->p_prev.p, G->p_prev.bytes(), st));
+    PF2_TRY(io.device("ghist", G->hist.p, G->hist.bytes(), st));
+    PF2_TRY(io.device("gahist", G->ahist.p, G->ahist.bytes(), st));
+    PF2_TRY(io.device("ggram", G->gram.p, G->gram.bytes(), st));
+    PF2_TRY(io.device("gring", G->ring.p, G->ring.bytes(), st));
+    return mpnn_checkpoint(G->net, io, st);
+}
+
 void guess_destroy(Guess* g) {
     if (!g) return;
     pf2_mpnn_destroy(g->net);

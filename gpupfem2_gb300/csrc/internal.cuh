@@ -47,8 +47,47 @@ struct SolveRecord {
 pf2_status solver_solve_async(pf2_solver* s, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,
                               cudaStream_t st, bool refactor = true);
 
+// A checkpoint file (checkpoint.cu): a header (magic, format version, kind of object) and
+// tagged sections (8-byte tag, 8-byte length, payload) written and read in one order.
+// Reading checks each tag and length against what the reader expects, so a file of
+// another object, mesh or size is rejected with the section that differs.
+enum CkptKind : uint32_t { CKPT_PARTICLES = 1, CKPT_FLOW = 2, CKPT_MPNN = 3 };
+class CkptFile {
+public:
+    CkptFile() = default;
+    CkptFile(const CkptFile&) = delete;
+    CkptFile& operator=(const CkptFile&) = delete;
+    ~CkptFile();
+    pf2_status open_write(const char* path, CkptKind kind);
+    pf2_status open_read(const char* path, CkptKind kind);
+    // writing: flush and report any write error; reading: the file must end here
+    pf2_status close();
+    bool writing() const { return wr_; }
+    // host bytes: written, or read into p after the tag and length check
+    pf2_status host(const char* tag, void* p, size_t bytes);
+    // device bytes, staged through host memory (the stream is synchronised)
+    pf2_status device(const char* tag, void* d, size_t bytes, cudaStream_t st);
+
+private:
+    pf2_status header(const char* tag, size_t bytes);
+    FILE* f_ = nullptr;
+    bool wr_ = false;
+    std::string path_;
+    std::vector<unsigned char> stage_;
+};
+
+// The particle state (count, the SoA arrays of the current buffer, the cell words and
+// the cell segments) to or from a checkpoint.
+pf2_status particles_checkpoint(pf2_particles* H, CkptFile& io, cudaStream_t st);
+
+// The network's trained state (parameters, AdamW moments and step) to or from a checkpoint.
+pf2_status mpnn_checkpoint(pf2_mpnn* net, CkptFile& io, cudaStream_t st);
+
 // Learned initial guess of the pressure solve (guess.cu).
 struct Guess;
+// the guess's state across steps (previous pressure, increment history, network
+// parameters and AdamW moments) to or from a checkpoint
+pf2_status guess_checkpoint(Guess* g, CkptFile& io, cudaStream_t st);
 pf2_status guess_create(const pf2_mesh* m, Guess** out);
 void guess_destroy(Guess* g);
 // Before the first pressure solve of a step: features from (x, y, b, p, p_prev), the

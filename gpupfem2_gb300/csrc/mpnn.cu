@@ -420,6 +420,25 @@ struct pf2_mpnn {
 
 namespace pf2 {
 
+// Sections: the parameter count, the FP32 parameters, the AdamW moments and step count.
+// The BF16 weight copies follow from the parameters and are rebuilt on reading.
+pf2_status mpnn_checkpoint(pf2_mpnn* N, CkptFile& io, cudaStream_t st) {
+    int meta[2] = { kParams, N->step };
+    PF2_TRY(io.host("nmeta", meta, sizeof(meta)));
+    PF2_REQUIRE(meta[0] == kParams, PF2_BAD_INPUT, "checkpoint network has %d parameters, this one %d", meta[0],
+                kParams);
+    PF2_TRY(io.device("nparams", N->P.p, sizeof(float) * kParams, st));
+    PF2_TRY(io.device("nadam_m", N->am.p, sizeof(float) * kParams, st));
+    PF2_TRY(io.device("nadam_v", N->av.p, sizeof(float) * kParams, st));
+    if (!io.writing()) {
+        N->step = meta[1];
+        k_weights_bf16<<<blocks_for(ML * MH * MK), kThreads, 0, st>>>(N->P.p, N->Wb.p);
+        PF2_LAUNCH_CHECK();
+        PF2_CUDA(cudaStreamSynchronize(st));
+    }
+    return PF2_OK;
+}
+
 static pf2_status mpnn_forward(pf2_mpnn* N, cudaStream_t st) {
     const Graph G = N->graph();
     k_mpnn_encoder<<<blocks_for(N->n), kThreads, 0, st>>>(G, N->feat.p, N->P.p, N->Hl(0), N->maskl(0));
@@ -523,6 +542,22 @@ pf2_status pf2_mpnn_destroy(pf2_mpnn* N) {
 }
 
 int pf2_mpnn_param_count(void) { return kParams; }
+
+pf2_status pf2_mpnn_save(const pf2_mpnn* N, const char* path) {
+    PF2_REQUIRE(N && path, PF2_BAD_INPUT, "null argument");
+    CkptFile io;
+    PF2_TRY(io.open_write(path, CKPT_MPNN));
+    PF2_TRY(mpnn_checkpoint(const_cast<pf2_mpnn*>(N), io, nullptr));
+    return io.close();
+}
+
+pf2_status pf2_mpnn_load(pf2_mpnn* N, const char* path) {
+    PF2_REQUIRE(N && path, PF2_BAD_INPUT, "null argument");
+    CkptFile io;
+    PF2_TRY(io.open_read(path, CKPT_MPNN));
+    PF2_TRY(mpnn_checkpoint(N, io, nullptr));
+    return io.close();
+}
 
 pf2_status pf2_mpnn_set_params(pf2_mpnn* N, const float* params_host) {
     PF2_REQUIRE(N && params_host, PF2_BAD_INPUT, "null argument");

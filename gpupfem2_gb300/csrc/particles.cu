@@ -491,6 +491,41 @@ const int* particles_count_ptr(const pf2_particles* H) { return H->cnt.p; }
 int particles_parity(const pf2_particles* H) { return H->cur; }
 void particles_set_parity(pf2_particles* H, int parity) { H->cur = parity; }
 
+// Sections: sizes {cells, level, count, seeded}, the SoA arrays and cell words of the
+// current buffer, and the cell segments of the last sort (read by a projection that
+// comes before the next advection).  Between steps that is the whole particle state:
+// the per-cell counts and masks are zero and the other buffer is scratch.
+pf2_status particles_checkpoint(pf2_particles* H, CkptFile& io, cudaStream_t st) {
+    const int nc = H->mesh->nc;
+    int meta[4] = { nc, H->level, 0, H->seeded ? 1 : 0 };
+    if (io.writing()) {
+        PF2_TRY(particles_status(H, st));
+        PF2_CUDA(cudaMemcpyAsync(&meta[2], H->cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        PF2_CUDA(cudaStreamSynchronize(st));
+    }
+    PF2_TRY(io.host("pmeta", meta, sizeof(meta)));
+    if (!io.writing()) {
+        PF2_REQUIRE(meta[0] == nc && meta[1] == H->level, PF2_BAD_INPUT,
+                    "checkpoint particles: %d cells at level %d, these particles: %d cells at level %d", meta[0],
+                    meta[1], nc, H->level);
+        PF2_REQUIRE(meta[2] >= 0 && meta[2] <= H->cap, PF2_OVERFLOW,
+                    "checkpoint holds %d particles, the capacity is %lld", meta[2], H->cap);
+    }
+    const size_t n = (size_t)meta[2];
+    static const char* const tags[6] = { "px", "py", "pl0", "pl1", "pu", "pv" };
+    for (int k = 0; k < 6; ++k) PF2_TRY(io.device(tags[k], H->buf[H->cur][k].p, n * sizeof(double), st));
+    PF2_TRY(io.device("pcell", H->cw[H->cur].p, n * sizeof(int), st));
+    PF2_TRY(io.device("pseg", H->seg.p, (size_t)(nc + 1) * sizeof(int), st));
+    if (!io.writing()) {
+        const int h[2] = { meta[2], meta[2] };
+        PF2_CUDA(cudaMemcpyAsync(H->cnt.p, h, sizeof(h), cudaMemcpyHostToDevice, st));
+        PF2_CUDA(cudaStreamSynchronize(st));
+        H->partials_valid = false;
+        H->seeded = meta[3] != 0;
+    }
+    return PF2_OK;
+}
+
 }  // namespace pf2
 
 extern "C" {
@@ -601,6 +636,23 @@ pf2_status pf2_particles_download(const pf2_particles* Hc, double* x, double* y,
         }
     }
     return PF2_OK;
+}
+
+pf2_status pf2_particles_save(const pf2_particles* Hc, const char* path) {
+    PF2_REQUIRE(Hc && path, PF2_BAD_INPUT, "null argument");
+    pf2_particles* H = const_cast<pf2_particles*>(Hc);  // only read
+    CkptFile io;
+    PF2_TRY(io.open_write(path, CKPT_PARTICLES));
+    PF2_TRY(particles_checkpoint(H, io, nullptr));
+    return io.close();
+}
+
+pf2_status pf2_particles_load(pf2_particles* H, const char* path) {
+    PF2_REQUIRE(H && path, PF2_BAD_INPUT, "null argument");
+    CkptFile io;
+    PF2_TRY(io.open_read(path, CKPT_PARTICLES));
+    PF2_TRY(particles_checkpoint(H, io, nullptr));
+    return io.close();
 }
 
 pf2_status pf2_particles_upload(pf2_particles* H, int n, const double* x, const double* y, const double* l0,

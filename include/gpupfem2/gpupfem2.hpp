@@ -261,6 +261,12 @@ public:
         check(pf2_particles_count(h_, &n), "pf2_particles_count");
         return n;
     }
+    // checkpoint / restart (no reference counterpart): false if the file cannot be
+    // written or does not fit this handler (mesh, level, capacity)
+    bool saveCheckpoint(const std::string& filename) const {
+        return pf2_particles_save(h_, filename.c_str()) == PF2_OK;
+    }
+    bool loadCheckpoint(const std::string& filename) { return pf2_particles_load(h_, filename.c_str()) == PF2_OK; }
 
     pf2_particles* handle() const { return h_; }
 

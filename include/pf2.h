@@ -329,6 +329,19 @@ pf2_status pf2_particles_upload(pf2_particles* ph, int n, const double* x, const
                                 const double* l1, const double* l2, const double* u, const double* v,
                                 const int* cell);
 
+/* ---------------------------------------------------- Checkpoint / restart
+ * No reference counterpart (its drivers always start from the seed).  A checkpoint is a
+ * binary file: magic "PF2CKPT", format version, object kind, then tagged sections, each
+ * with its length.  Loading checks every section against the receiving object (mesh
+ * size, level, capacity, parameter count) and fails with PF2_BAD_INPUT naming the first
+ * section that differs (PF2_OVERFLOW: more particles than the capacity; PF2_IO_ERROR:
+ * the file cannot be opened).  A load that fails part-way leaves the object's state
+ * unspecified.  All synchronise.
+ * Particles: count, x, y, l0, l1, u, v, the cell words (with the sub-cell marks) and the
+ * cell segments of the last sort, so that a restored handler continues exactly. */
+pf2_status pf2_particles_save(const pf2_particles* ph, const char* path);
+pf2_status pf2_particles_load(pf2_particles* ph, const char* path);
+
 /* ------------------------------------------------------------- Flow engine
  * One PFEM-2 time step of the channel drivers (cases/Cylinder2D/main.cu:793-880): the
  * state (particles, velocity, prediction, pressure, matrices, solvers) lives on the
@@ -359,6 +372,13 @@ pf2_status pf2_flow_system(pf2_flow* f, int which, pf2_csr** A, double** rhs);
 /* New values for a Dirichlet set of the flow (0 velocity x, 1 velocity y, 2 pressure),
  * device double[n_bc] in the order the set was created with (a time-dependent inflow). */
 pf2_status pf2_flow_set_boundary_values(pf2_flow* f, int which, const double* values_dev, void* stream);
+/* Checkpoint of the flow between steps: step count, the eight node fields, the values of
+ * the three Dirichlet sets, the particles and (PF2_X0_LEARNED) the learned guess's
+ * history, network parameters and AdamW moments.  Load into an engine created with the
+ * same mesh, parameters and Dirichlet node sets; from there the steps repeat the
+ * uninterrupted run bit for bit. */
+pf2_status pf2_flow_save(pf2_flow* f, const char* path, void* stream);
+pf2_status pf2_flow_load(pf2_flow* f, const char* path, void* stream);
 
 typedef struct pf2_step_info {
     int particles;
@@ -407,6 +427,10 @@ pf2_status pf2_mpnn_forward(pf2_mpnn* net, const float* feat, float* y, void* st
  * be NULL; when not, the call synchronises to fill it. */
 pf2_status pf2_mpnn_train_step(pf2_mpnn* net, const float* feat, const float* target, float lr, int apply,
                                double* loss_host, void* stream);
+/* The network's trained state (parameters, AdamW moments and step count) to or from a
+ * checkpoint file. */
+pf2_status pf2_mpnn_save(const pf2_mpnn* net, const char* path);
+pf2_status pf2_mpnn_load(pf2_mpnn* net, const char* path);
 
 #ifdef __cplusplus
 }
