@@ -27,6 +27,7 @@ PRECOND = {"none": -1, "jacobi": 0, "ilu": 1, "ic": 2}
 CRITERION_ABS, CRITERION_REL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RHS_GAUSSIAN, RHS_SINSIN = 0, 1
+RHS3D_GAUSSIAN, RHS3D_SINSINSIN = 0, 1
 FIELDS = {"ux": 0, "uy": 1, "ux_old": 2, "uy_old": 3, "pred_x": 4, "pred_y": 5, "p": 6, "p_old": 7}
 MESH_FIELDS = {"xy": 0, "tri": 1, "area": 2, "inv_jacobi": 3, "neighbor_offsets": 4, "neighbor_indices": 5,
                "edge_ids": 6}
@@ -168,13 +169,64 @@ class Mesh2D:
                                                        C.c_double(r), _stream()), "pf2_mesh_set_channel_boundary_ids")
 
 
-class SparseMatrixCSR:
-    """SparseMatrixCSR (src/linear_algebra/sparse_matrix.cuh) on the mesh's pattern."""
+class Mesh3D:
+    """Mesh3D (src/mesh_3d.cuh): vertices, tetrahedra, volumes, inverse Jacobians,
+    face-sharing neighbour lists and the node graph's CSR pattern, built on the device."""
 
-    def __init__(self, mesh: Mesh2D):
+    FIELDS = {"xyz": 0, "tet": 1, "volume": 2, "inv_jacobi": 3, "neighbor_offsets": 4, "neighbor_indices": 5}
+
+    def __init__(self, handle):
+        self.h = handle
+        nv, nc, nn = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().pf2_mesh3d_sizes(self.h, C.byref(nv), C.byref(nc), C.byref(nn)), "pf2_mesh3d_sizes")
+        self.nv, self.nc, self.n_neighbor_entries = nv.value, nc.value, nn.value
+
+    @classmethod
+    def from_arrays(cls, xyz, tet, fill_neighbors=True):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        tet = np.ascontiguousarray(tet, dtype=np.int32)
+        h = C.c_void_p()
+        _check(lib().pf2_mesh3d_create(int(xyz.shape[0]), xyz.ctypes.data_as(C.c_void_p), int(tet.shape[0]),
+                                       tet.ctypes.data_as(C.c_void_p), int(fill_neighbors), None, C.byref(h)),
+               "pf2_mesh3d_create")
+        return cls(h)
+
+    @classmethod
+    def load_dat(cls, path, fill_neighbors=True, scale=1.0):
+        h = C.c_void_p()
+        _check(lib().pf2_mesh3d_load_dat(str(path).encode(), int(fill_neighbors), C.c_double(scale), None,
+                                         C.byref(h)), "pf2_mesh3d_load_dat")
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.pf2_mesh3d_destroy(self.h)
+            self.h = None
+
+    def download(self, field):
+        shapes = {"xyz": ((self.nv, 3), np.float64), "tet": ((self.nc, 4), np.int32),
+                  "volume": ((self.nc,), np.float64), "inv_jacobi": ((self.nc, 3, 3), np.float64),
+                  "neighbor_offsets": ((self.nc + 1,), np.int32),
+                  "neighbor_indices": ((max(self.n_neighbor_entries, 0),), np.int32)}
+        shape, dt = shapes[field]
+        out = np.empty(shape, dt)
+        if out.size:
+            _check(lib().pf2_mesh3d_download(self.h, self.FIELDS[field], out.ctypes.data_as(C.c_void_p)),
+                   "pf2_mesh3d_download")
+        return out
+
+
+class SparseMatrixCSR:
+    """SparseMatrixCSR (src/linear_algebra/sparse_matrix.cuh) on the mesh's pattern
+    (a Mesh2D or a Mesh3D)."""
+
+    def __init__(self, mesh):
         self.mesh = mesh
         self.h = C.c_void_p()
-        _check(lib().pf2_csr_create(mesh.h, C.byref(self.h)), "pf2_csr_create")
+        if isinstance(mesh, Mesh3D):
+            _check(lib().pf2_csr_create_3d(mesh.h, C.byref(self.h)), "pf2_csr_create_3d")
+        else:
+            _check(lib().pf2_csr_create(mesh.h, C.byref(self.h)), "pf2_csr_create")
         n, nnz = C.c_int(), C.c_int()
         _check(lib().pf2_csr_sizes(self.h, C.byref(n), C.byref(nnz)), "pf2_csr_sizes")
         self.rows, self.nnz = n.value, nnz.value
@@ -228,6 +280,13 @@ def assemble_poisson(mesh, A, rhs, rhs_kind=RHS_SINSIN, lam=1.0, bc=None):
                                       bc.h if bc is not None else None, _stream()), "pf2_assemble_poisson")
 
 
+def assemble_poisson_3d(mesh, A, rhs, rhs_kind=RHS3D_GAUSSIAN, lam=0.5, bc=None):
+    """PoissonIntegrator::assembleSystem of cases/Poisson3D/main.cu:79-85 (lambda 0.5
+    and the Gaussian rhs there), then the Dirichlet rule when bc is given."""
+    _check(lib().pf2_assemble_poisson_3d(mesh.h, A.h, _dev(rhs), int(rhs_kind), C.c_double(lam),
+                                         bc.h if bc is not None else None, _stream()), "pf2_assemble_poisson_3d")
+
+
 def assemble_velocity_prediction(mesh, p, ux, uy, uxo, uyo, pold, Ax, Ay, rx, ry, bcx=None, bcy=None):
     _check(lib().pf2_assemble_velocity_prediction(mesh.h, C.byref(p), _dev(ux), _dev(uy), _dev(uxo), _dev(uyo),
                                                   _dev(pold), Ax.h, Ay.h, _dev(rx), _dev(ry),
@@ -268,11 +327,17 @@ def body_loads(mesh, p, ux, uy, pres, center=(0.2, 0.2)):
 
 
 def export_vtu(mesh, path, fields):
-    """DataExport::exportToVTK: the mesh and node fields ({name: device tensor}) as VTU."""
+    """DataExport::exportToVTK / DataExport3D::exportToVTK: the mesh and node fields
+    ({name: device tensor}) as VTU."""
     names = list(fields)
     arr_n = (C.c_char_p * max(len(names), 1))(*[n.encode() for n in names])
     arr_f = (C.c_void_p * max(len(names), 1))(*[_dev(fields[n]) for n in names])
-    _check(lib().pf2_export_vtu(mesh.h, str(path).encode(), len(names), arr_n, arr_f, _stream()), "pf2_export_vtu")
+    if isinstance(mesh, Mesh3D):
+        _check(lib().pf2_export_vtu_3d(mesh.h, str(path).encode(), len(names), arr_n, arr_f, _stream()),
+               "pf2_export_vtu_3d")
+    else:
+        _check(lib().pf2_export_vtu(mesh.h, str(path).encode(), len(names), arr_n, arr_f, _stream()),
+               "pf2_export_vtu")
 
 
 def spmv(A, x, y):

@@ -123,7 +123,7 @@ constexpr int kMaxLevel = 4;         // cellDivisionLevel (src/common/constants.
 constexpr int kMaxPerCell = kMaxLevel * kMaxLevel;
 constexpr double kDoubleMin = 2e-6;  // CONSTANTS::DOUBLE_MIN (src/common/constants.h:5)
 
-// Cell word of a particle: bits 0..26 the cell, bits 27..31 = 1 + sub-cell index for a
+// Cell word of a particle: bits 0..25 the cell, bits 26..30 = 1 + sub-cell index for a
 // particle that still sits at a sub-cell centroid (seeded or reseeded and not yet
 // located), whose third barycentric coordinate is the centroid's stored one rather
 // than 1 - l0 - l1.
@@ -161,6 +161,24 @@ struct pf2_mesh {
     pf2::DevBuf<int> inc_pos;
     std::vector<double> h_xy;
     std::vector<int> h_tri;
+};
+
+// Mesh3D: linear tetrahedra.  The node graph's CSR pattern sits in `graph`, a pf2_mesh
+// with no cells of its own, so that matrices, boundary sets and solvers of 3D meshes use
+// the same objects as 2D ones.
+struct pf2_mesh3d {
+    int nv = 0, nc = 0, nnb = 0;
+    pf2::DevBuf<double4_32a> xyz;  // (x, y, z, 0)
+    pf2::DevBuf<int4> tet;
+    pf2::DevBuf<double> volume;
+    pf2::DevBuf<double> invJ;      // 9 per cell, row-major
+    pf2::DevBuf<int> nb_off, nb_idx;
+    // node -> incident cells (ascending), packed (cell << 2 | local vertex), and the
+    // positions in row i of the cell's four vertices, 4 x 8 bits
+    pf2::DevBuf<int> inc_off, inc, inc_pos;
+    pf2_mesh graph;
+    std::vector<double> h_xyz;
+    std::vector<int> h_tet;
 };
 
 struct pf2_csr {

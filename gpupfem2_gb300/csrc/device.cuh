@@ -13,6 +13,20 @@
 
 namespace pf2 {
 
+// Sorts buf[0, m) ascending in place and drops repeats; returns the unique count.
+__device__ __forceinline__ int sort_unique(int* buf, int m) {
+    for (int a = 1; a < m; ++a) {
+        const int x = buf[a];
+        int b = a - 1;
+        while (b >= 0 && buf[b] > x) { buf[b + 1] = buf[b]; --b; }
+        buf[b + 1] = x;
+    }
+    int u = 0;
+    for (int q = 0; q < m; ++q)
+        if (q == 0 || buf[q] != buf[q - 1]) buf[u++] = buf[q];
+    return u;
+}
+
 // Row-major invJ {d0, d1, d2, d3}.  shapeFuncGrad(i) mapped by invJ
 // (numerical_integrator_2d.cuh:8-20 with Matrix2x2::operator*, cuda_math.cuh:146-153):
 // grad N0 = (d0, d2), grad N1 = (d1, d3), grad N2 = (-d0 - d1, -d2 - d3).

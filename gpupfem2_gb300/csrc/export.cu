@@ -1,4 +1,4 @@
-// export.cu - VTU output of node fields and particles.
+// export.cu - VTU output of node fields (2D and 3D meshes) and particles.
 //
 // DataExport::exportToVTK / exportParticlesToVTK (src/data_export.cu:17-171): an ASCII
 // VTK UnstructuredGrid with the mesh (points, triangles as VTK type 5) and one Float32
@@ -70,6 +70,55 @@ pf2_status pf2_export_vtu(const pf2_mesh* m, const char* path, int nfields, cons
     fprintf(f, "\n        </DataArray>\n");
     fprintf(f, "        <DataArray type=\"UInt8\" Name=\"types\" Format=\"ascii\">\n          ");
     for (int c = 0; c < nc; ++c) fprintf(f, "5 ");
+    fprintf(f, "\n        </DataArray>\n");
+    fprintf(f, "      </Cells>\n");
+    if (nfields > 0) {
+        fprintf(f, "      <PointData Scalars=\"scalars\">\n");
+        for (int k = 0; k < nfields; ++k) {
+            fprintf(f, "        <DataArray type=\"Float32\" Name=\"%s\" Format=\"ascii\">\n        ", names[k]);
+            for (int i = 0; i < nv; ++i) fprintf(f, "%.9g  ", host[k][i]);
+            fprintf(f, "\n        </DataArray>\n");
+        }
+        fprintf(f, "      </PointData>\n");
+    }
+    footer(f);
+    PF2_REQUIRE(!ferror(f), PF2_IO_ERROR, "write error on %s", path);
+    return PF2_OK;
+}
+
+// DataExport3D::exportToVTK (src/data_export_3d.cu:15-93): the same document with
+// three coordinates per point and tetrahedra (VTK type 10).
+pf2_status pf2_export_vtu_3d(const pf2_mesh3d* m, const char* path, int nfields, const char* const* names,
+                             const double* const* fields, void* stream) {
+    PF2_REQUIRE(m && path && nfields >= 0 && (nfields == 0 || (names && fields)), PF2_BAD_INPUT, "null argument");
+    cudaStream_t st = as_stream(stream);
+    const int nv = m->nv, nc = m->nc;
+    std::vector<std::vector<double>> host(nfields, std::vector<double>(nv));
+    for (int k = 0; k < nfields; ++k) {
+        PF2_REQUIRE(names[k] && fields[k], PF2_BAD_INPUT, "field %d: null name or data", k);
+        PF2_CUDA(cudaMemcpyAsync(host[k].data(), fields[k], sizeof(double) * nv, cudaMemcpyDeviceToHost, st));
+    }
+    PF2_CUDA(cudaStreamSynchronize(st));
+    File out(path);
+    PF2_REQUIRE(out.f, PF2_IO_ERROR, "cannot open %s for writing", path);
+    FILE* f = out.f;
+    header(f, nv, nc);
+    fprintf(f, "      <Points>\n");
+    fprintf(f, "        <DataArray type=\"Float32\" NumberOfComponents=\"3\" Format=\"ascii\">\n");
+    for (int i = 0; i < nv; ++i)
+        fprintf(f, "        %.9g %.9g %.9g\n", m->h_xyz[3 * i], m->h_xyz[3 * i + 1], m->h_xyz[3 * i + 2]);
+    fprintf(f, "        </DataArray>\n");
+    fprintf(f, "      </Points>\n");
+    fprintf(f, "      <Cells>\n");
+    fprintf(f, "        <DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n          ");
+    for (int c = 0; c < nc; ++c)
+        fprintf(f, "%d %d %d %d ", m->h_tet[4 * c], m->h_tet[4 * c + 1], m->h_tet[4 * c + 2], m->h_tet[4 * c + 3]);
+    fprintf(f, "\n        </DataArray>\n");
+    fprintf(f, "        <DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n          ");
+    for (int c = 0; c < nc; ++c) fprintf(f, "%lld ", 4ll * (c + 1));
+    fprintf(f, "\n        </DataArray>\n");
+    fprintf(f, "        <DataArray type=\"UInt8\" Name=\"types\" Format=\"ascii\">\n          ");
+    for (int c = 0; c < nc; ++c) fprintf(f, "10 ");
     fprintf(f, "\n        </DataArray>\n");
     fprintf(f, "      </Cells>\n");
     if (nfields > 0) {

@@ -78,18 +78,6 @@ __global__ void k_inc_sort(int nv, const int* __restrict__ off, int* inc, int* e
     }
 }
 
-__device__ __forceinline__ int sort_unique(int* buf, int m) {
-    for (int a = 1; a < m; ++a) {
-        const int x = buf[a];
-        int b = a - 1;
-        while (b >= 0 && buf[b] > x) { buf[b + 1] = buf[b]; --b; }
-        buf[b + 1] = x;
-    }
-    int u = 0;
-    for (int q = 0; q < m; ++q)
-        if (q == 0 || buf[q] != buf[q - 1]) buf[u++] = buf[q];
-    return u;
-}
 
 // CSR rows: {i} U vertices of incident cells, sorted (sparse_matrix.cu:14-45)
 template <bool FILL>

@@ -303,3 +303,106 @@ def square_boundary_nodes(xy: np.ndarray, tol: float = 2e-6):
     x, y = xy[:, 0], xy[:, 1]
     on = (np.abs(x) < tol) | (np.abs(x - 1) < tol) | (np.abs(y) < tol) | (np.abs(y - 1) < tol)
     return [(int(i), 0.0) for i in np.nonzero(on)[0]]
+
+
+# ---- 3D (Mesh3D, Poisson3D) -----------------------------------------------------
+def box_tets(nx: int = 40, ny: int = 20, nz: int = 10, lo=(-1.0, 0.0, -0.25), hi=(1.0, 1.0, 0.25),
+             jitter: float = 0.2, seed: int = 0):
+    """Structured tetrahedral mesh of a box: nx x ny x nz hexahedra, each split into the
+    six tetrahedra around its (0,0,0)-(1,1,1) diagonal (conforming across hexahedra).
+    The default box is the Poisson3D case's [-1,1] x [0,1] x [-0.25,0.25]; interior
+    nodes move by at most ``jitter`` x the smallest spacing per axis (splitmix64 stream,
+    three uniforms per interior node in node order).  Returns (xyz, tet)."""
+    i, j, k = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    h = [(hi[a] - lo[a]) / n for a, n in enumerate((nx, ny, nz))]
+    xyz = np.stack([lo[0] + h[0] * i.ravel().astype(np.float64),
+                    lo[1] + h[1] * j.ravel().astype(np.float64),
+                    lo[2] + h[2] * k.ravel().astype(np.float64)], axis=1)
+    # exact end coordinates, so that boundary tests with a 2e-6 tolerance see them
+    for a, n in enumerate((nx, ny, nz)):
+        idx = (i, j, k)[a].ravel()
+        xyz[idx == n, a] = hi[a]
+    nid = (i * (ny + 1) + j) * (nz + 1) + k
+
+    def corner(dx, dy, dz):
+        return nid[dx:nx + dx, dy:ny + dy, dz:nz + dz].ravel()
+
+    tets = []
+    for a, b in ((0, 1), (0, 2), (1, 0), (1, 2), (2, 0), (2, 1)):
+        s1 = [0, 0, 0]
+        s1[a] = 1
+        s2 = list(s1)
+        s2[b] = 1
+        tets.append(np.stack([corner(0, 0, 0), corner(*s1), corner(*s2), corner(1, 1, 1)], axis=1))
+    tet = np.concatenate(tets, axis=0)
+    s = np.sort(tet, axis=1)
+    tet = tet[np.lexsort((s[:, 3], s[:, 2], s[:, 1], s[:, 0]))]
+    bnd = ((i == 0) | (i == nx) | (j == 0) | (j == ny) | (k == 0) | (k == nz)).ravel()
+    interior = np.nonzero(~bnd)[0]
+    if jitter and interior.size:
+        r = uniform_pm1(seed, 3 * interior.size).reshape(-1, 3)
+        xyz = xyz.copy()
+        xyz[interior] += jitter * r * np.array(h)[None, :]
+    return xyz, tet.astype(np.int32)
+
+
+def write_dat3(path: str, xyz: np.ndarray, tet: np.ndarray) -> None:
+    """Write a SALOME DAT mesh of tetrahedra (type 304, 1-based ids, no trailing newline)."""
+    nv, nt = xyz.shape[0], tet.shape[0]
+    lines = ["%d %d" % (nv, nt)]
+    lines += ["%d %.17g %.17g %.17g" % (k + 1, x, y, z) for k, (x, y, z) in enumerate(xyz)]
+    t1 = tet.astype(np.int64) + 1
+    lines += ["%d 304 %d %d %d %d" % (nv + 1 + k, a, b, c, d) for k, (a, b, c, d) in enumerate(t1)]
+    with open(path, "w") as f:
+        f.write("\n".join(lines))
+
+
+def read_dat3(path: str, scale: float = 1.0):
+    """Read a SALOME DAT mesh as Mesh3D::loadMeshFromFile (src/mesh_3d.cu:84-147) does:
+    tetrahedra (type 304) kept, other entities skipped, 1-based ids."""
+    with open(path) as f:
+        tok = f.read().split()
+    nv = int(tok[0])
+    p = 2
+    xyz = np.empty((nv, 3))
+    for q in range(nv):
+        for a in range(3):
+            xyz[q, a] = scale * float(tok[p + 1 + a])
+        p += 4
+    tets = []
+    n = len(tok)
+    while p + 1 < n:
+        typ = int(tok[p + 1])
+        if typ == 304:
+            tets.append(tuple(int(tok[p + 2 + a]) - 1 for a in range(4)))
+        p += 2 + typ % 100
+    return xyz, np.array(tets, dtype=np.int32).reshape(-1, 4)
+
+
+def box_boundary_nodes(xyz: np.ndarray, tol: float = 2e-6):
+    """Dirichlet nodes of the Poisson3D case (cases/Poisson3D/main.cu:111-126), tested
+    in its order: x = -1 -> -1, x = 1 -> 1, y = 0 -> 0, y = 1 -> 2, z = -0.25 -> 3,
+    z = 0.25 -> -2."""
+    out = []
+    for i, (x, y, z) in enumerate(xyz):
+        if abs(x - (-1.0)) < tol:
+            out.append((i, -1.0))
+        elif abs(x - 1.0) < tol:
+            out.append((i, 1.0))
+        elif abs(y) < tol:
+            out.append((i, 0.0))
+        elif abs(y - 1.0) < tol:
+            out.append((i, 2.0))
+        elif abs(z - (-0.25)) < tol:
+            out.append((i, 3.0))
+        elif abs(z - 0.25) < tol:
+            out.append((i, -2.0))
+    return out
+
+
+def cube_boundary_nodes(xyz: np.ndarray, tol: float = 2e-6):
+    """All nodes on the boundary of [0,1]^3 with value 0 (the sin-sin-sin problem)."""
+    on = np.zeros(xyz.shape[0], bool)
+    for a in range(3):
+        on |= (np.abs(xyz[:, a]) < tol) | (np.abs(xyz[:, a] - 1) < tol)
+    return [(int(i), 0.0) for i in np.nonzero(on)[0]]

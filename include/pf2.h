@@ -147,6 +147,50 @@ enum { PF2_RHS_GAUSSIAN = 0, /* exp(-(x^2+10y^2)), cases/Poisson2D/main.cu:24-26
 pf2_status pf2_assemble_poisson(const pf2_mesh* mesh, pf2_csr* A, double* rhs_dev, int rhs_kind, double lambda,
                                 const pf2_bc* bc, void* stream);
 
+/* ------------------------------------------------------- Mesh3D / Poisson3D
+ * Replaces Mesh3D (src/mesh_3d.cuh:11-70), SparseMatrixCSR(const Mesh3D&)
+ * (sparse_matrix.cu:56-97), the Poisson3D integrator (cases/Poisson3D/main.cu:26-85)
+ * and DataExport3D (src/data_export_3d.cuh:9-23): linear tetrahedra. */
+typedef struct pf2_mesh3d pf2_mesh3d;
+/* Mesh3D::loadMeshFromFile(path, fillNeighborLists, scale), mesh_3d.cu:84-147: DAT file
+ * with "nv ne", nv lines "id x y z", then entities "id type v..." of which type 304
+ * (tetrahedron, 1-based vertex ids) are kept; 102 and 203 entities are skipped. */
+pf2_status pf2_mesh3d_load_dat(const char* path, int fill_neighbors, double scale, void* stream, pf2_mesh3d** out);
+/* From host arrays: xyz double[3*nv], tet int[4*nc] (0-based).  Builds the cell volumes
+ * and inverse Jacobians (kCalculateCellVolume / kCalculateInvJacobi, mesh_3d.cu:12-35:
+ * J has rows v0 - v3, v1 - v3, v2 - v3), the face-sharing neighbour lists of
+ * fillCellNeighborIndices (mesh_3d.cu:37-82,198-227: cells sharing 3 vertices,
+ * ascending) when fill_neighbors != 0, and the CSR pattern of the node graph. */
+pf2_status pf2_mesh3d_create(int nv, const double* xyz, int nc, const int* tet, int fill_neighbors, void* stream,
+                             pf2_mesh3d** out);
+pf2_status pf2_mesh3d_destroy(pf2_mesh3d* mesh);
+pf2_status pf2_mesh3d_sizes(const pf2_mesh3d* mesh, int* nv, int* nc, int* n_neighbor_entries);
+enum { PF2_MESH3D_XYZ = 0,              /* double[3*nv] */
+       PF2_MESH3D_TET = 1,              /* int[4*nc] */
+       PF2_MESH3D_VOLUME = 2,           /* double[nc] */
+       PF2_MESH3D_INV_JACOBI = 3,       /* double[9*nc], row-major */
+       PF2_MESH3D_NEIGHBOR_OFFSETS = 4, /* int[nc+1] */
+       PF2_MESH3D_NEIGHBOR_INDICES = 5  /* int[n_neighbor_entries] */ };
+/* Copies one mesh array to host memory. Synchronises. */
+pf2_status pf2_mesh3d_download(const pf2_mesh3d* mesh, int field, void* host_dst);
+/* SparseMatrixCSR(const Mesh3D&): rows = nodes, columns = {i} U nodes sharing a
+ * tetrahedron with i, ascending; values zeroed.  Usable with every solver and with
+ * pf2_bc_apply. */
+pf2_status pf2_csr_create_3d(const pf2_mesh3d* mesh, pf2_csr** out);
+
+enum { PF2_RHS3D_GAUSSIAN = 0, /* exp(-(x^2+10y^2+z^2)), cases/Poisson3D/main.cu:22-24 */
+       PF2_RHS3D_SINSINSIN = 1 /* 3 pi^2 sin(pi x) sin(pi y) sin(pi z) */ };
+/* PoissonIntegrator::assembleSystem of cases/Poisson3D/main.cu:26-85: A_ij = lambda
+ * int grad N_i . grad N_j, b_i = int f N_i with the 6-point rule of
+ * createCellQuadratureFormula(1) (quadrature_formula_3d.cu); overwrites A's values and
+ * rhs; applies bc (pf2_bc_apply) when non-NULL. */
+pf2_status pf2_assemble_poisson_3d(const pf2_mesh3d* mesh, pf2_csr* A, double* rhs_dev, int rhs_kind, double lambda,
+                                   const pf2_bc* bc, void* stream);
+/* DataExport3D::exportToVTK (data_export_3d.cu:15-93): ASCII VTU, tetrahedra as VTK type
+ * 10, one Float32 point array per field (device double[nv]). */
+pf2_status pf2_export_vtu_3d(const pf2_mesh3d* mesh, const char* path, int nfields, const char* const* names,
+                             const double* const* fields_dev, void* stream);
+
 /* SimulationParameters, src/parameters.cuh:6-51 (the fields the step uses). */
 typedef struct pf2_params {
     double rho, mu, dt, tolerance;

@@ -112,6 +112,14 @@ def _declare(L):
     L.or_flow_csr_nnz.argtypes = [vp]
     L.or_flow_csr_nnz.restype = C.c_int
     L.or_flow_get_matrix.argtypes = [vp, C.c_int, _dp, _dp]
+    L.or_mesh3d_geometry.argtypes = [C.c_int, _dp, _ip, _dp, _dp]
+    L.or_mesh3d_neighbors.argtypes = [C.c_int, _ip, _ip, vp]
+    L.or_mesh3d_neighbors.restype = C.c_int
+    L.or_csr_structure_3d.argtypes = [C.c_int, C.c_int, _ip, _ip, vp]
+    L.or_csr_structure_3d.restype = C.c_int
+    L.or_cell_quadrature_3d.argtypes = [_dp, _dp]
+    L.or_cell_quadrature_3d.restype = C.c_int
+    L.or_assemble_poisson_3d.argtypes = [C.c_int, _dp, _ip, _dp, _dp, C.c_int, C.c_double, _ip, _ip, _dp, _dp]
 
 
 def _c(a, dt):
@@ -159,6 +167,50 @@ def node_cells(nv, tri):
     cells = np.empty(max(n, 1), I)
     lib().or_node_cells(nv, tri.shape[0], tri, off, _ptr(cells))
     return off, cells[:n]
+
+
+# ---- 3D mesh and Poisson3D ----------------------------------------------------
+def mesh3d_geometry(xyz, tet):
+    xyz, tet = _c(xyz, D), _c(tet, I)
+    nc = tet.shape[0]
+    vol = np.empty(nc, D)
+    invJ = np.empty((nc, 3, 3), D)
+    lib().or_mesh3d_geometry(nc, xyz, tet, vol, invJ)
+    return vol, invJ
+
+
+def mesh3d_neighbors(tet):
+    tet = _c(tet, I)
+    nc = tet.shape[0]
+    off = np.empty(nc + 1, I)
+    n = lib().or_mesh3d_neighbors(nc, tet, off, None)
+    idx = np.empty(max(n, 1), I)
+    lib().or_mesh3d_neighbors(nc, tet, off, _ptr(idx))
+    return off, idx[:n]
+
+
+def csr_structure_3d(nv, tet):
+    tet = _c(tet, I)
+    nc = tet.shape[0]
+    rp = np.empty(nv + 1, I)
+    n = lib().or_csr_structure_3d(nv, nc, tet, rp, None)
+    col = np.empty(max(n, 1), I)
+    lib().or_csr_structure_3d(nv, nc, tet, rp, _ptr(col))
+    return rp, col[:n]
+
+
+def cell_quadrature_3d():
+    c, w = np.empty(24, D), np.empty(6, D)
+    n = lib().or_cell_quadrature_3d(c, w)
+    return c.reshape(-1, 4)[:n], w[:n]
+
+
+def assemble_poisson_3d(xyz, tet, vol, invJ, rowptr, col, rhs_kind=0, lam=0.5):
+    val = np.zeros(col.size, D)
+    rhs = np.zeros(xyz.shape[0], D)
+    lib().or_assemble_poisson_3d(tet.shape[0], _c(xyz, D), _c(tet, I), _c(vol, D), _c(invJ, D), rhs_kind, lam,
+                                 _c(rowptr, I), _c(col, I), val, rhs)
+    return val, rhs
 
 
 def edge_boundary_ids(xy, tri, lx, ly, cylinder=None):

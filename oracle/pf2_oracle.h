@@ -163,6 +163,15 @@ double or_mpnn_backward(int n, const int* rowptr, const int* col, const double* 
 void or_adamw(int np, double* theta, const double* grad, double* m, double* v, int step, double lr, double b1,
               double b2, double eps, double wd);
 
+/* ---- 3D (pf2_oracle3d.c) ---- */
+void or_mesh3d_geometry(int nc, const double* xyz, const int* tet, double* volume, double* invJ);
+int or_mesh3d_neighbors(int nc, const int* tet, int* offsets, int* idx);   /* idx may be NULL */
+int or_csr_structure_3d(int nv, int nc, const int* tet, int* rowptr, int* col); /* col may be NULL */
+int or_cell_quadrature_3d(double* coords4, double* weights);
+void or_assemble_poisson_3d(int nc, const double* xyz, const int* tet, const double* volume, const double* invJ,
+                            int rhs_kind, double lambda, const int* rowptr, const int* col, double* val,
+                            double* rhs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -43,3 +43,14 @@ int cudaDeviceSynchronize(void) { return 0; }
 int cudaGetLastError(void) { return 0; }
 const char* cudaGetErrorName(int e) { (void)e; return "stub"; }
 const char* cudaGetErrorString(int e) { (void)e; return "stub"; }
+
+/* Referenced by the CUB scan in Mesh3D::fillCellNeighborIndices (mesh_3d.cu:198-227),
+ * which the 3D dump never calls (neighbour lists off): each reports an error. */
+int cudaGetDevice(int* d) { (void)d; return 1; }
+int cudaSetDevice(int d) { (void)d; return 1; }
+int cudaGetDeviceCount(int* n) { if (n) *n = 0; return 1; }
+int cudaDeviceGetAttribute(int* v, int attr, int dev) { (void)v; (void)attr; (void)dev; return 1; }
+int cudaFuncGetAttributes(void* a, const void* f) { (void)a; (void)f; return 1; }
+int cudaOccupancyMaxActiveBlocksPerMultiprocessorWithFlags(int* n, const void* f, int b, size_t s, unsigned fl)
+{ (void)n; (void)f; (void)b; (void)s; (void)fl; return 1; }
+int cudaPeekAtLastError(void) { return 0; }

@@ -1,4 +1,4 @@
-"""Generates tests/golden/reference_host.json from the reference's own host code.
+"""Generates tests/golden/reference_host.json from the reference's own host code (2D and 3D).
 
 Builds oracle/_ref/ref_host_dump with oracle/build_ref.sh (the reference's DAT reader,
 CSR pattern builder, vertex-sharing neighbour search, particle-handler constructor and
@@ -39,6 +39,12 @@ SHIPPED = ["cases/Poisson2D/TestProblem2.dat",
            "cases/PoiseuilleFlow2D/ChannelMesh.dat", "cases/Cylinder2D/CylinderMesh.dat",
            "cases/Cylinder2D/CylinderMesh3.dat"]
 ARRAYS = [("xy", "f64"), ("tri", "i32"), ("nboff", "i32"), ("nbidx", "i32"), ("rowptr", "i32"), ("col", "i32")]
+GENERATED3D = {
+    "box8x4x2": lambda: mg.box_tets(8, 4, 2),
+    "box40x20x10": lambda: mg.box_tets(),
+}
+SHIPPED3D = ["cases/Poisson3D/BoxMesh.dat", "cases/Poisson3D/BoxMesh2.dat"]
+ARRAYS3D = [("xyz", "f64"), ("tet", "i32"), ("rowptr", "i32"), ("col", "i32")]
 
 
 def digest(a: np.ndarray) -> str:
@@ -51,6 +57,16 @@ def run_dump(exe, dat, prefix):
         raise RuntimeError(r.stderr)
     out = {}
     for name, t in ARRAYS:
+        out[name] = np.fromfile(prefix + "." + name + "." + t, dtype=np.float64 if t == "f64" else np.int32)
+    return out
+
+
+def run_dump3d(exe, dat, prefix):
+    r = subprocess.run([exe, dat, prefix], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    out = {}
+    for name, t in ARRAYS3D + [("quad", "f64")]:
         out[name] = np.fromfile(prefix + "." + name + "." + t, dtype=np.float64 if t == "f64" else np.int32)
     return out
 
@@ -87,6 +103,31 @@ def main():
         q = np.fromfile(pre + ".quad.f64")
         fixtures["quadrature"] = {"face_index1_xyzw": [float(v).hex() for v in q[:12]],
                                   "edge_index1_cw": [float(v).hex() for v in q[12:]]}
+    exe3 = os.path.join(ROOT, "oracle", "_ref", "ref_host_dump3d")
+    fixtures["generator3d"] = ("reference host code (mesh_3d.cu:84-147, sparse_matrix.cu:56-97, "
+                               "quadrature_formula_3d.cu) via oracle/build_ref.sh")
+    fixtures["meshes3d"] = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        items = [(k, None) for k in GENERATED3D] + [(os.path.basename(s), os.path.join(ref, s)) for s in SHIPPED3D]
+        quad = None
+        for name, path in items:
+            if path is None:
+                xyz, tet = GENERATED3D[name]()
+                path = os.path.join(tmp, name + ".dat")
+                mg.write_dat3(path, xyz, tet)
+                kind = "generated"
+            else:
+                if not os.path.exists(path):
+                    continue
+                kind = "shipped"
+            a = run_dump3d(exe3, path, os.path.join(tmp, name))
+            quad = a.pop("quad")
+            rec = {"kind": kind, "nv": int(a["xyz"].size // 3), "nc": int(a["tet"].size // 4),
+                   "nnz": int(a["col"].size)}
+            rec.update({"sha256_" + k: digest(v) for k, v in a.items()})
+            fixtures["meshes3d"][name] = rec
+            print(name, rec["nv"], rec["nc"], rec["nnz"])
+        fixtures["quadrature3d"] = {"cell_index1_xyzw_weight": [float(v).hex() for v in quad]}
     with open(OUT, "w") as f:
         json.dump(fixtures, f, indent=1, sort_keys=True)
     print("wrote", OUT)

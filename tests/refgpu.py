@@ -27,6 +27,11 @@ PARTICLE = np.dtype({"names": ["id", "x", "y", "l0", "l1", "l2", "u", "v", "cell
 # GaussPoint2D {Point3 coordinates; double weight}, GaussPoint1D {double, double}
 GAUSS2D = np.dtype([("x", "<f8"), ("y", "<f8"), ("z", "<f8"), ("w", "<f8")])
 GAUSS1D = np.dtype([("c", "<f8"), ("w", "<f8")])
+# GaussPoint3D {Point4 coordinates (double4, 16-byte aligned); double weight}: 48 bytes;
+# GenericMatrix3x3 has a virtual operator(): vtable pointer, then 9 doubles (80 bytes)
+GAUSS3D = np.dtype({"names": ["x", "y", "z", "w", "weight"], "formats": ["<f8"] * 5,
+                    "offsets": [0, 8, 16, 24, 32], "itemsize": 48})
+MAT3 = np.dtype({"names": ["vptr", "m"], "formats": ["<u8", ("<f8", (9,))], "offsets": [0, 8], "itemsize": 80})
 # DirichletNode {unsigned nodeIdx; double bcValue}
 DNODE = np.dtype({"names": ["node", "value"], "formats": ["<u4", "<f8"], "offsets": [0, 8], "itemsize": 16})
 
@@ -45,6 +50,10 @@ def available():
                for f in ("ref_flow.cubin", "ref_poisson.cubin", "ref_kernels.names"))
 
 
+def available_3d():
+    return all(os.path.exists(os.path.join(REF_DIR, f)) for f in ("ref_poisson3d.cubin", "ref_kernels3d.names"))
+
+
 _cuda = None
 
 
@@ -61,13 +70,13 @@ def _ck(rc, what):
 
 
 class RefModule:
-    def __init__(self, cubin):
+    def __init__(self, cubin, names="ref_kernels.names"):
         torch.zeros(1, device="cuda")  # torch's primary context is current
         d = _drv()
         self.mod = C.c_void_p()
         _ck(d.cuModuleLoad(C.byref(self.mod), os.path.join(REF_DIR, cubin).encode()), "cuModuleLoad")
         self.names = {}
-        for line in open(os.path.join(REF_DIR, "ref_kernels.names")):
+        for line in open(os.path.join(REF_DIR, names)):
             _, base, mangled = line.split()
             self.names[base] = mangled
         self.fns = {}
