@@ -453,6 +453,20 @@ pf2_status pf2_mesh3d_sizes(const pf2_mesh3d* m, int* nv, int* nc, int* nnb) {
     return PF2_OK;
 }
 
+pf2_status pf2_mesh3d_view_get(const pf2_mesh3d* m, pf2_mesh3d_view* v) {
+    PF2_REQUIRE(m && v, PF2_BAD_INPUT, "null argument");
+    v->nv = m->nv;
+    v->nc = m->nc;
+    v->n_neighbor_entries = m->nnb;
+    v->xyz4 = reinterpret_cast<const double*>(m->xyz.p);
+    v->tet = reinterpret_cast<const int*>(m->tet.p);
+    v->volume = m->volume.p;
+    v->inv_jacobi = m->invJ.p;
+    v->neighbor_offsets = m->nb_off.p;
+    v->neighbor_indices = m->nb_idx.p;
+    return PF2_OK;
+}
+
 pf2_status pf2_mesh3d_download(const pf2_mesh3d* m, int field, void* dst) {
     PF2_REQUIRE(m && dst, PF2_BAD_INPUT, "null argument");
     PF2_CUDA(cudaDeviceSynchronize());

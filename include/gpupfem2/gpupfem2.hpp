@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <stdexcept>
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -104,10 +105,58 @@ private:
     std::vector<int3> hostCells_;
 };
 
+// Mesh3D (src/mesh_3d.cuh:11-70): linear tetrahedra.  Vertices on the device are
+// (x, y, z, 0) per vertex; the host copies keep the reference's element types.
+class Mesh3D {
+public:
+    Mesh3D() = default;
+    Mesh3D(const Mesh3D&) = delete;
+    Mesh3D& operator=(const Mesh3D&) = delete;
+    ~Mesh3D() { pf2_mesh3d_destroy(m_); }
+
+    bool loadMeshFromFile(const std::string& filename, bool fillNeighborLists = true, double scale = 1.0) {
+        pf2_mesh3d* m = nullptr;
+        if (pf2_mesh3d_load_dat(filename.c_str(), fillNeighborLists ? 1 : 0, scale, nullptr, &m) != PF2_OK)
+            return false;
+        pf2_mesh3d_destroy(m_);
+        m_ = m;
+        check(pf2_mesh3d_view_get(m_, &v_), "pf2_mesh3d_view_get");
+        hostVertices_.resize(v_.nv);
+        hostCells_.resize(v_.nc);
+        check(pf2_mesh3d_download(m_, PF2_MESH3D_XYZ, hostVertices_.data()), "pf2_mesh3d_download");
+        check(pf2_mesh3d_download(m_, PF2_MESH3D_TET, hostCells_.data()), "pf2_mesh3d_download");
+        return true;
+    }
+    int numVertices() const { return v_.nv; }
+    int numCells() const { return v_.nc; }
+    const double* getVertices() const { return v_.xyz4; }  // 4 doubles per vertex
+    const int4* getCells() const { return reinterpret_cast<const int4*>(v_.tet); }
+    const double* getCellVolume() const { return v_.volume; }
+    const double* getInvJacobi() const { return v_.inv_jacobi; }
+    const int* getCellNeighborsOffsets() const { return v_.neighbor_offsets; }
+    const int* getCellNeighborIndices() const { return v_.neighbor_indices; }
+    const std::vector<double3>& getHostVertices() const { return hostVertices_; }
+    const std::vector<int4>& getHostCells() const { return hostCells_; }
+    pf2_mesh3d* handle() const { return m_; }
+
+private:
+    pf2_mesh3d* m_ = nullptr;
+    pf2_mesh3d_view v_{};
+    std::vector<double3> hostVertices_;
+    std::vector<int4> hostCells_;
+};
+
 // SparseMatrixCSR (src/linear_algebra/sparse_matrix.cuh:9-58)
 class SparseMatrixCSR {
 public:
     explicit SparseMatrixCSR(const Mesh2D& mesh) { initialize(mesh); }
+    explicit SparseMatrixCSR(const Mesh3D& mesh) { initialize(mesh); }
+    void initialize(const Mesh3D& mesh) {
+        pf2_csr_destroy(a_);
+        check(pf2_csr_create_3d(mesh.handle(), &a_), "pf2_csr_create_3d");
+        check(pf2_csr_view(a_, &rp_, &col_, &val_), "pf2_csr_view");
+        check(pf2_csr_sizes(a_, &rows_, &nnz_), "pf2_csr_sizes");
+    }
     SparseMatrixCSR(const SparseMatrixCSR&) = delete;
     SparseMatrixCSR& operator=(const SparseMatrixCSR&) = delete;
     ~SparseMatrixCSR() { pf2_csr_destroy(a_); }
@@ -304,6 +353,31 @@ private:
     const Mesh2D& mesh_;
     const ParticleHandler2D* ph_;
     std::vector<std::pair<std::string, const double*>> fields_;
+};
+
+// DataExport3D (src/data_export_3d.cuh:9-23): node fields by name (written in name
+// order, as the reference's std::map), tetrahedra as VTK type 10.
+class DataExport3D {
+public:
+    explicit DataExport3D(const Mesh3D& mesh) : mesh_(mesh) {}
+    void addScalarDataVector(const deviceVector<double>& dataVector, const std::string& fieldname) {
+        fields_[fieldname] = dataVector.data;
+    }
+    void exportToVTK(const std::string& filename) const {
+        std::vector<const char*> names;
+        std::vector<const double*> data;
+        for (const auto& f : fields_) {
+            names.push_back(f.first.c_str());
+            data.push_back(f.second);
+        }
+        check(pf2_export_vtu_3d(mesh_.handle(), filename.c_str(), (int)names.size(), names.data(), data.data(),
+                                nullptr),
+              "pf2_export_vtu_3d");
+    }
+
+private:
+    const Mesh3D& mesh_;
+    std::map<std::string, const double*> fields_;
 };
 
 }  // namespace gpupfem2

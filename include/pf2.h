@@ -165,6 +165,19 @@ pf2_status pf2_mesh3d_create(int nv, const double* xyz, int nc, const int* tet, 
                              pf2_mesh3d** out);
 pf2_status pf2_mesh3d_destroy(pf2_mesh3d* mesh);
 pf2_status pf2_mesh3d_sizes(const pf2_mesh3d* mesh, int* nv, int* nc, int* n_neighbor_entries);
+/* Device arrays of the mesh (Mesh3D getters, mesh_3d.cuh:18-52).  xyz4 holds (x, y, z, 0)
+ * per vertex (a 32-byte stride, not the reference's 24-byte Point3); inv_jacobi holds 9
+ * doubles per cell, row-major (the reference's GenericMatrix3x3 adds a vtable slot). */
+typedef struct pf2_mesh3d_view {
+    int nv, nc, n_neighbor_entries;
+    const double* xyz4;
+    const int* tet;
+    const double* volume;
+    const double* inv_jacobi;
+    const int* neighbor_offsets;
+    const int* neighbor_indices;
+} pf2_mesh3d_view;
+pf2_status pf2_mesh3d_view_get(const pf2_mesh3d* mesh, pf2_mesh3d_view* out);
 enum { PF2_MESH3D_XYZ = 0,              /* double[3*nv] */
        PF2_MESH3D_TET = 1,              /* int[4*nc] */
        PF2_MESH3D_VOLUME = 2,           /* double[nc] */
