@@ -140,12 +140,15 @@ __global__ void k_poisson(int nv, RowMesh M, int kind, double lambda, double* __
 }
 
 // ------------------------------------------------------------- flow systems
+// `matrix` is a runtime flag, not a template parameter: the matrix values that feed the
+// elimination of a right-hand-side-only assembly then come from the same machine code
+// as a full assembly's, so both give the same bits (separate instantiations may fuse
+// the products differently).
 
 // kIntegrateVelocityPrediction, cases/Cylinder2D/main.cu:72-167.  Outlet edge term on
 // boundary id 1 with n = (1, 0); like the cell terms it is scaled by the cell area
 // (addLocalToGlobal).  Along an edge, sum_q w_q N_m(q) = 1 for both edge vertices.
-template <bool MATRIX>
-__global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __restrict__ ux,
+__global__ void k_prediction(bool matrix, int nv, RowMesh M, FlowCoef P, const double* __restrict__ ux,
                              const double* __restrict__ uy, const double* __restrict__ uxo,
                              const double* __restrict__ uyo, const double* __restrict__ pold,
                              double* __restrict__ valx, double* __restrict__ valy, double* __restrict__ rhsx,
@@ -153,11 +156,11 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const int s = M.rowptr[i], len = M.rowptr[i + 1] - s;
-    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, MATRIX);
-    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, MATRIX);
+    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, matrix);
+    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, matrix);
     if (bx && by) return;
     // the matrix rows are needed when written, or for the elimination of boundary columns
-    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
+    const bool need = matrix || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
     double v0[kMaxRow], v1[kMaxRow];
     if (need)
         for (int k = 0; k < len; ++k) { v0[k] = 0.0; v1[k] = 0.0; }
@@ -216,28 +219,27 @@ __global__ void k_prediction(int nv, RowMesh M, FlowCoef P, const double* __rest
     }
     if (!bx) {
         if (need) eliminate_row(i, s, len, M.col, v0, r0, bcx);
-        if (MATRIX)
+        if (matrix)
             for (int k = 0; k < len; ++k) valx[s + k] = v0[k];
         rhsx[i] = r0;
     }
     if (!by) {
         if (need) eliminate_row(i, s, len, M.col, v1, r1, bcy);
-        if (MATRIX)
+        if (matrix)
             for (int k = 0; k < len; ++k) valy[s + k] = v1[k];
         rhsy[i] = r1;
     }
 }
 
 // kIntegratePressureEquation, cases/Cylinder2D/main.cu:169-211
-template <bool MATRIX>
-__global__ void k_pressure(int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
+__global__ void k_pressure(bool matrix, int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
                            const double* __restrict__ py, const double* __restrict__ pold, double* __restrict__ val,
                            double* __restrict__ rhs, BcView bc) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const int s = M.rowptr[i], len = M.rowptr[i + 1] - s;
-    if (boundary_row(i, s, len, M.col, val, rhs, bc, MATRIX)) return;
-    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bc);
+    if (boundary_row(i, s, len, M.col, val, rhs, bc, matrix)) return;
+    const bool need = matrix || has_bc_column(i, s, len, M.col, bc);
     double v[kMaxRow];
     if (need)
         for (int k = 0; k < len; ++k) v[k] = 0.0;
@@ -261,24 +263,23 @@ __global__ void k_pressure(int nv, RowMesh M, FlowCoef P, const double* __restri
         r += (cr + fdiv * div) * A;
     }
     if (need) eliminate_row(i, s, len, M.col, v, r, bc);
-    if (MATRIX)
+    if (matrix)
         for (int k = 0; k < len; ++k) val[s + k] = v[k];
     rhs[i] = r;
 }
 
 // kIntegrateVelocityCorrection, cases/Cylinder2D/main.cu:213-259
-template <bool MATRIX>
-__global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
+__global__ void k_correction(bool matrix, int nv, RowMesh M, FlowCoef P, const double* __restrict__ px,
                              const double* __restrict__ py, const double* __restrict__ pres,
                              const double* __restrict__ pold, double* __restrict__ valx, double* __restrict__ valy,
                              double* __restrict__ rhsx, double* __restrict__ rhsy, BcView bcx, BcView bcy) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nv) return;
     const int s = M.rowptr[i], len = M.rowptr[i + 1] - s;
-    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, MATRIX);
-    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, MATRIX);
+    const bool bx = boundary_row(i, s, len, M.col, valx, rhsx, bcx, matrix);
+    const bool by = boundary_row(i, s, len, M.col, valy, rhsy, bcy, matrix);
     if (bx && by) return;
-    const bool need = MATRIX || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
+    const bool need = matrix || has_bc_column(i, s, len, M.col, bcx) || has_bc_column(i, s, len, M.col, bcy);
     double v[kMaxRow];
     if (need)
         for (int k = 0; k < len; ++k) v[k] = 0.0;
@@ -308,13 +309,13 @@ __global__ void k_correction(int nv, RowMesh M, FlowCoef P, const double* __rest
         for (int k = 0; k < len; ++k) w[k] = v[k];
     if (!bx) {
         if (need) eliminate_row(i, s, len, M.col, v, r0, bcx);
-        if (MATRIX)
+        if (matrix)
             for (int k = 0; k < len; ++k) valx[s + k] = v[k];
         rhsx[i] = r0;
     }
     if (!by) {
         if (need) eliminate_row(i, s, len, M.col, w, r1, bcy);
-        if (MATRIX)
+        if (matrix)
             for (int k = 0; k < len; ++k) valy[s + k] = w[k];
         rhsy[i] = r1;
     }
@@ -424,26 +425,16 @@ __global__ void k_body_loads(int nc, RowMesh M, FlowCoef P, int body_id, double 
 pf2_status launch_prediction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* ux, const double* uy,
                              const double* uxo, const double* uyo, const double* pold, double* valx, double* valy,
                              double* rhsx, double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st) {
-    if (matrix)
-        k_prediction<true><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, ux, uy, uxo, uyo, pold,
-                                                                     valx, valy, rhsx, rhsy, bc_view(bcx),
-                                                                     bc_view(bcy));
-    else
-        k_prediction<false><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, ux, uy, uxo, uyo, pold,
-                                                                      valx, valy, rhsx, rhsy, bc_view(bcx),
-                                                                      bc_view(bcy));
+    k_prediction<<<blocks_for(m->nv), kThreads, 0, st>>>(matrix, m->nv, row_mesh(m), P, ux, uy, uxo, uyo, pold, valx,
+                                                         valy, rhsx, rhsy, bc_view(bcx), bc_view(bcy));
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }
 
 pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                            const double* pold, double* val, double* rhs, const pf2_bc* bc, cudaStream_t st) {
-    if (matrix)
-        k_pressure<true><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pold, val, rhs,
-                                                                   bc_view(bc));
-    else
-        k_pressure<false><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pold, val, rhs,
-                                                                    bc_view(bc));
+    k_pressure<<<blocks_for(m->nv), kThreads, 0, st>>>(matrix, m->nv, row_mesh(m), P, px, py, pold, val, rhs,
+                                                       bc_view(bc));
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }
@@ -451,12 +442,8 @@ pf2_status launch_pressure(const pf2_mesh* m, const FlowCoef& P, bool matrix, co
 pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, bool matrix, const double* px, const double* py,
                              const double* pres, const double* pold, double* valx, double* valy, double* rhsx,
                              double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st) {
-    if (matrix)
-        k_correction<true><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pres, pold, valx,
-                                                                     valy, rhsx, rhsy, bc_view(bcx), bc_view(bcy));
-    else
-        k_correction<false><<<blocks_for(m->nv), kThreads, 0, st>>>(m->nv, row_mesh(m), P, px, py, pres, pold, valx,
-                                                                      valy, rhsx, rhsy, bc_view(bcx), bc_view(bcy));
+    k_correction<<<blocks_for(m->nv), kThreads, 0, st>>>(matrix, m->nv, row_mesh(m), P, px, py, pres, pold, valx, valy,
+                                                         rhsx, rhsy, bc_view(bcx), bc_view(bcy));
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }

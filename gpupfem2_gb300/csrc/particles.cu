@@ -202,6 +202,26 @@ __device__ __forceinline__ void add_partials(double acc[9], double l0, double l1
     acc[8] = __dadd_rn(acc[8], l2);
 }
 
+// The nine partial sums of one cell from its warp's per-lane sums (lane j holding the
+// cell's slots j, j + 32, ...), through shared memory R[9][33] of the warp: lane 3v + q
+// adds value v of lanes 11q .. 11q + 10, then the three parts are combined.  Fixed order
+// (about a quarter of the FP64 additions of nine butterfly reductions); every kernel
+// that forms partial sums goes through here, so they agree bit for bit.
+__device__ __forceinline__ void warp_partials_store(const double acc[9], int lane, double (*R)[33], Partials part,
+                                                    int c) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k][lane] = acc[k];
+    __syncwarp();
+    double sum = 0.0;
+    if (lane < 27) {
+        const int v = lane / 3, q0 = 11 * (lane % 3), q1 = min(32, q0 + 11);
+        for (int j = q0; j < q1; ++j) sum += R[v][j];
+    }
+    const double s1 = __shfl_down_sync(0xffffffffu, sum, 1);
+    const double s2 = __shfl_down_sync(0xffffffffu, sum, 2);
+    if (lane < 27 && lane % 3 == 0) part.s[(size_t)(lane / 3) * part.nc + c] = (sum + s1) + s2;
+}
+
 // Per cell, one warp: stable order, move, reseed (kAddParticlesToCell :197-236), partial
 // sums.  The cell's particles arrive in perm[s, s + n) in the order the atomics handed
 // out ranks; each lane ranks its particle by old index against all n (the old order is
@@ -280,36 +300,28 @@ __global__ void __launch_bounds__(256) k_gather(int nc, const int* __restrict__ 
         const double l0 = D.l0[o], l1 = D.l1[o];
         add_partials(acc, l0, l1, third_coord(w, l0, l1, C), D.u[o], D.v[o]);
     }
-    // nine sums over the 32 lanes through shared memory: lane 3v + q adds value v of
-    // lanes 11q .. 11q + 10, then the three parts are combined (fixed order; about a
-    // quarter of the FP64 additions of nine butterfly reductions)
     __shared__ double red[8][9][33];
-    double(*R)[33] = red[threadIdx.x >> 5];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) R[k][lane] = acc[k];
-    __syncwarp();
-    double sum = 0.0;
-    if (lane < 27) {
-        const int v = lane / 3, q0 = 11 * (lane % 3), q1 = min(32, q0 + 11);
-        for (int j = q0; j < q1; ++j) sum += R[v][j];
-    }
-    const double s1 = __shfl_down_sync(0xffffffffu, sum, 1);
-    const double s2 = __shfl_down_sync(0xffffffffu, sum, 2);
-    if (lane < 27 && lane % 3 == 0) part.s[(size_t)(lane / 3) * nc + c] = (sum + s1) + s2;
+    warp_partials_store(acc, lane, red[threadIdx.x >> 5], part, c);
 }
 
-// Partial sums of every cell from the current (cell-ordered) particles.
-__global__ void k_partials(int nc, const int* __restrict__ seg, PState S, Centers C, Partials part) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= nc) return;
+// Partial sums of every cell from the current (cell-ordered) particles: one warp per
+// cell with k_gather's lane assignment and reduction, so a projection gives the same bits
+// whether its partial sums came from the sort or from here.
+__global__ void __launch_bounds__(256) k_partials(int nc, const int* __restrict__ seg, PState S, Centers C,
+                                                  Partials part) {
+    const int lane = threadIdx.x & 31;
+    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    if (c >= nc) return;  // uniform over the warp
     double acc[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-    for (int p = seg[c]; p < seg[c + 1]; ++p) {
+    const int s = seg[c], tot = seg[c + 1] - s;
+    for (int k = lane; k < tot; k += 32) {
+        const int p = s + k;
         const int w = S.cw[p];
         const double l0 = S.l0[p], l1 = S.l1[p];
         add_partials(acc, l0, l1, third_coord(w, l0, l1, C), S.u[p], S.v[p]);
     }
-#pragma unroll
-    for (int k = 0; k < 9; ++k) part.s[(size_t)k * nc + c] = acc[k];
+    __shared__ double red[8][9][33];
+    warp_partials_store(acc, lane, red[threadIdx.x >> 5], part, c);
 }
 
 // kFinalizeVelocityProjection (:109-115): u_i = sum L v / sum L over the cells around
@@ -445,8 +457,8 @@ pf2_status particles_advect(pf2_particles* H, const double* ux, const double* uy
 pf2_status particles_project(pf2_particles* H, double* ux, double* uy, double* uxo, double* uyo, cudaStream_t st) {
     const pf2_mesh* M = H->mesh;
     if (!H->partials_valid) {
-        k_partials<<<blocks_for(M->nc), kThreads, 0, st>>>(M->nc, H->seg.p, H->state(H->cur), H->C,
-                                                           Partials{ H->part.p, M->nc });
+        k_partials<<<blocks_for((long long)M->nc * 32, 256), 256, 0, st>>>(M->nc, H->seg.p, H->state(H->cur),
+                                                                         H->C, Partials{ H->part.p, M->nc });
         PF2_LAUNCH_CHECK();
         H->partials_valid = true;
     }

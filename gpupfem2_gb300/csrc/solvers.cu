@@ -108,6 +108,14 @@ struct Tri {
     int* done_b;
     unsigned* tickets;     // one counter per (apply, direction)
     int* rec;              // where a wait gave up (GridBarrier::rec)
+    // FP64 CG on B itself (orderings without the banded plan): A's values in B's
+    // numbering, the factors as one array on B's pattern (row i: L to the left of the
+    // diagonal, the upper factor to the right, 1 / dividing diagonal on it) and x in B's
+    // numbering
+    int csr;
+    const double* bval;
+    const double* fsym;
+    double* xB;
 };
 
 __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, int* rec, int row, int dep) {
@@ -584,6 +592,219 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
     return true;
 }
 
+// q = A p over the block's rows r0..r1 with this thread's p.q terms: the thread's rows
+// (r0 + tid + u * blockDim, u = 0..3) walked together, so the loads of four rows are in
+// flight at once; each row sums its entries in order, as row_dot.
+__device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, double* q, int r0, int r1) {
+    double pq = 0.0;
+    for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * blockDim.x) {
+        int s[4], e[4];
+        double acc[4] = { 0.0, 0.0, 0.0, 0.0 };
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            s[u] = i < r1 ? __ldg(&A.rowptr[i]) : 0;
+            e[u] = i < r1 ? __ldg(&A.rowptr[i + 1]) : 0;
+        }
+        int len = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) len = max(len, e[u] - s[u]);
+        for (int k = 0; k < len; ++k) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (s[u] + k < e[u]) acc[u] += __ldg(&A.val[s[u] + k]) * __ldcg(&p[__ldg(&A.col[s[u] + k])]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i < r1) {
+                __stcg(&q[i], acc[u]);
+                pq += __ldcg(&p[i]) * acc[u];
+            }
+        }
+    }
+    return pq;
+}
+
+// p = z + beta p over the block's rows, four rows per pass with the loads first (z is
+// written by other blocks' threads in the sweeps: read through L2).
+__device__ __forceinline__ void p_update(double* p, const double* z, double beta, int r0, int r1) {
+    for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * blockDim.x) {
+        double zv[4], pv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            zv[u] = i < r1 ? __ldcg(&z[i]) : 0.0;
+            pv[u] = i < r1 ? __ldcg(&p[i]) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i < r1) __stcg(&p[i], zv[u] + beta * pv[u]);
+        }
+    }
+}
+
+// sum_k f_k x_{col_k} over the CSR entries [k0, k1) of a row whose x entries other
+// threads of the same sweep are still writing: four entries loaded together, only the
+// pending ones polled (bounded); terms added in entry order.
+__device__ __forceinline__ bool csr_dot_wait(const double* x, const int* __restrict__ col,
+                                             const double* __restrict__ f, int k0, int k1, int row, int* err,
+                                             int* rec, double& sum) {
+    sum = 0.0;
+    for (int k = k0; k < k1; k += 4) {
+        int j[4];
+        double v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = j[u] >= 0 ? *(volatile const double*)&x[j[u]] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (j[u] >= 0 && Pending<double>::bits(v[u]) == Pending<double>::kBits &&
+                !wait_value(x, j[u], v[u], err, rec, row))
+                return false;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (j[u] >= 0) sum += __ldg(&f[k + u]) * v[u];
+    }
+    return true;
+}
+
+// Forward sweep of one CG iteration on B (rows in B's order, thread t taking rows t,
+// t + T, ...: a row's dependencies are lower rows, so the lowest unsolved row always
+// belongs to a thread that has reached it).  With UPDATE it first applies x += alpha p,
+// r -= alpha q to its row.  Writes the forward result and resets the row of z to the
+// pending marker for the backward sweep.  Returns the thread's r.r terms.
+template <bool UPDATE>
+__device__ double csr_fwd(const Tri& T, double alpha, double* r, const double* q, double* x, const double* p,
+                          double* z, int* err) {
+    const int n = T.B.n;
+    const int stride = gridDim.x * blockDim.x;
+    const bool unit = T.kind != PF2_PRECOND_IC;  // ILU: L has a unit diagonal
+    double rr = 0.0;
+    // each row's pattern bounds are loaded one row ahead
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    int k0n = 0, dn = 0;
+    if (row < n) {
+        k0n = __ldg(&T.B.rowptr[row]);
+        dn = __ldg(&T.B.diag[row]);
+    }
+    for (; row < n; row += stride) {
+        const int k0 = k0n, d = dn;
+        if (row + stride < n) {
+            k0n = __ldg(&T.B.rowptr[row + stride]);
+            dn = __ldg(&T.B.diag[row + stride]);
+        }
+        double ra = __ldcg(&r[row]);
+        if (UPDATE) {
+            ra -= alpha * __ldcg(&q[row]);
+            __stcg(&r[row], ra);
+            __stcg(&x[row], __ldcg(&x[row]) + alpha * __ldcg(&p[row]));
+        }
+        rr += ra * ra;
+        double sum;
+        if (!csr_dot_wait(T.tmp, T.B.col, T.fsym, k0, d, row, err, T.rec, sum)) break;
+        const double v = unit ? ra - sum : (ra - sum) * __ldg(&T.fsym[d]);
+        __stcg(&T.tmp[row], v);
+        __stcg(&z[row], Pending<double>::marker());
+    }
+    return rr;
+}
+
+// Backward sweep (rows in reverse order): z = U^{-1} t, the forward result reset to the
+// marker; with p_init the first direction p = z is stored too.  Returns the r.z terms.
+__device__ double csr_bwd(const Tri& T, const double* r, double* z, double* p_init, int* err) {
+    const int n = T.B.n;
+    const int stride = gridDim.x * blockDim.x;
+    double rz = 0.0;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int dn = 0, k1n = 0;
+    if (t < n) {
+        dn = __ldg(&T.B.diag[n - 1 - t]);
+        k1n = __ldg(&T.B.rowptr[n - t]);
+    }
+    for (; t < n; t += stride) {
+        const int row = n - 1 - t;
+        const int d = dn, k1 = k1n;
+        if (t + stride < n) {
+            dn = __ldg(&T.B.diag[row - stride]);
+            k1n = __ldg(&T.B.rowptr[row - stride + 1]);
+        }
+        const double in = __ldcg(&T.tmp[row]);
+        double sum;
+        if (!csr_dot_wait(z, T.B.col, T.fsym, d + 1, k1, row, err, T.rec, sum)) break;
+        const double v = (in - sum) * __ldg(&T.fsym[d]);
+        __stcg(&z[row], v);
+        if (p_init) __stcg(&p_init[row], v);
+        __stcg(&T.tmp[row], Pending<double>::marker());
+        rz += __ldcg(&r[row]) * v;
+    }
+    return rz;
+}
+
+// PCG in B's numbering (the ordering's permuted system B = P A P^T, with b and x
+// permuted on the way in and out): the SpMV, the two sweeps and every vector run on
+// B's CSR arrays, so the whole iteration reads one compact set of arrays (A's values on
+// B's pattern, the factors, six vectors) that stays in L2 at a million rows.  Same
+// iteration as below: four barriers (p.q reduction, forward -> backward, r.z reduction,
+// p update).
+__device__ void pcg_csr(const KArgs& a, double* sh) {
+    const Tri& T = a.T;
+    const int n = a.A.n;
+    int r0, r1;
+    row_range(n, r0, r1);
+    const Csr B{ n, T.B.rowptr, T.B.col, T.bval, T.B.diag };
+    double* xB = T.xB;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) __stcg(&xB[i], a.x[__ldg(&T.perm[i])]);
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    double red[3] = { 0.0, 0.0, 0.0 };  // r.z, b.b, r.r
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double bi = a.b[__ldg(&T.perm[i])];
+        __stcg(&a.r[i], bi - row_dot(B, i, xB));
+        red[1] += bi * bi;
+    }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    red[2] = csr_fwd<false>(T, 0.0, a.r, nullptr, nullptr, nullptr, a.z, a.bar.err);
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    red[0] = csr_bwd(T, a.r, a.z, a.p, a.bar.err);
+    if (!grid_reduce<3>(a.bar, red, sh)) return;
+    double gamma = red[0];
+    const double bnorm = sqrt(red[1]);
+    double rr = red[2];
+    const double tol2 = a.tol * a.tol;
+    auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
+    int it = 0;
+    bool conv = done_test(gamma, rr);
+    while (!conv && it < a.maxit) {
+        ++it;
+        double pq[1] = { spmv_rows(B, a.p, a.q, r0, r1) };
+        if (!grid_reduce<1>(a.bar, pq, sh)) return;
+        const double alpha = gamma / pq[0];
+        double g2[2] = { 0.0, 0.0 };
+        g2[1] = csr_fwd<true>(T, alpha, a.r, a.q, xB, a.p, a.z, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        g2[0] = csr_bwd(T, a.r, a.z, nullptr, a.bar.err);
+        if (!grid_reduce<2>(a.bar, g2, sh)) return;
+        const double gnew = g2[0];
+        rr = g2[1];
+        if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
+        const double beta = gnew / gamma;
+        gamma = gnew;
+        p_update(a.p, a.z, beta, r0, r1);
+        if (!grid_sync(a.bar, gridDim.x)) return;
+    }
+    // every x update happened before the last reduction's barrier
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[__ldg(&T.perm[i])] = __ldcg(&xB[i]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
 // SolverCG::solve (linear_solver.cu:440-515).  Per iteration: q = A p with p.q (one fused
 // barrier-reduction), x/r update, z = M^{-1} r with r.z (and r.r) (one fused
 // barrier-reduction), p = z + beta p (one barrier).
@@ -596,6 +817,10 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
     const bool fused = global_pc && a.T.band.P == 0 && a.T.band.K > 0;  // slot sweeps fused with the updates
     const bool rel = a.criterion == PF2_CRITERION_REL;
+    if (global_pc && a.T.csr) {
+        pcg_csr(a, sh);
+        return;
+    }
     // Jacobi: inverse diagonal (PreconditionerJacobi::initialize, preconditioners.cu:3-14)
     if (a.precond == PF2_PRECOND_JACOBI)
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
@@ -628,12 +853,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
     bool conv = done_test(gamma, rr);
     while (!conv && it < a.maxit) {
         ++it;
-        double pq[1] = { 0.0 };
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-            const double v = row_dot(a.A, i, a.p);
-            a.q[i] = v;
-            pq[0] += a.p[i] * v;
-        }
+        double pq[1] = { spmv_rows(a.A, a.p, a.q, r0, r1) };
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
@@ -656,15 +876,32 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
                 g2[1] += ri * ri;
             }
         } else {
+            // two rows per pass, all loads issued before the stores
             const bool jac = a.precond == PF2_PRECOND_JACOBI;
-            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-                a.x[i] += alpha * a.p[i];
-                const double ri = a.r[i] - alpha * a.q[i];
-                const double zi = jac ? ri * a.invd[i] : ri;
-                a.r[i] = ri;
-                a.z[i] = zi;
-                g2[0] += ri * zi;
-                g2[1] += ri * ri;
+            for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 2 * blockDim.x) {
+                double xv[2], pv[2], rv[2], qv[2], dv[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int i = i0 + u * blockDim.x;
+                    const bool in = i < r1;
+                    xv[u] = in ? a.x[i] : 0.0;
+                    pv[u] = in ? a.p[i] : 0.0;
+                    rv[u] = in ? a.r[i] : 0.0;
+                    qv[u] = in ? a.q[i] : 0.0;
+                    dv[u] = in && jac ? a.invd[i] : 1.0;
+                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const int i = i0 + u * blockDim.x;
+                    if (i >= r1) continue;
+                    a.x[i] = xv[u] + alpha * pv[u];
+                    const double ri = rv[u] - alpha * qv[u];
+                    const double zi = jac ? ri * dv[u] : ri;
+                    a.r[i] = ri;
+                    a.z[i] = zi;
+                    g2[0] += ri * zi;
+                    g2[1] += ri * ri;
+                }
             }
         }
         if (!grid_reduce<2>(a.bar, g2, sh)) return;
@@ -673,7 +910,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
         const double beta = gnew / gamma;
         gamma = gnew;
-        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.p[i] = __ldcg(&a.z[i]) + beta * a.p[i];
+        p_update(a.p, a.z, beta, r0, r1);
         if (!grid_sync(a.bar, gridDim.x)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -1117,6 +1354,12 @@ struct pf2_solver {
     size_t smem = 0;  // dynamic shared memory of the solver kernels (banded window)
     DevBuf<double> outB;
     DevBuf<float> fact32, tmp32, outB32;  // mixed precision with ILU/IC
+    // FP64 CG on B (Tri::csr): A's values and the factors on B's pattern, x in B's
+    // numbering, and per entry of B the factor entry it takes (lower and ILU upper: its
+    // own; IC upper (i, j): l_ji; diagonal: -1 - position, stored as its inverse)
+    bool csr = false;
+    DevBuf<double> bval, fsym, xB;
+    DevBuf<int> tpos;
     int levels_fwd = 0, levels_bwd = 0, colors = 0;
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
@@ -1264,6 +1507,32 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     // slot records (rows with at most kBandMaxDeps dependencies): in (range, step) order for
     // the banded solve, in level order for the sync-free one
     const bool banded = K <= kBandMaxDeps && std::max(S->levels_fwd, S->levels_bwd) >= band_min;
+    // FP64 CG with few levels: the whole iteration on B's CSR arrays (pcg_csr)
+    S->csr = std::max(S->levels_fwd, S->levels_bwd) < band_min && S->opt.kind == PF2_SOLVER_CG &&
+             S->opt.precision == PF2_PRECISION_FP64;
+    if (const char* e = getenv("PF2_CG_SLOTS")) S->csr = S->csr && atoi(e) == 0;  // tuning: keep the slot sweeps
+    if (S->csr) {
+        std::vector<int> tpos(std::max(nnz, 1));
+        for (int r = 0; r < n; ++r)
+            for (int k = brp[r]; k < brp[r + 1]; ++k) tpos[k] = (k == bdiag[r]) ? -1 - k : k;
+        if (ic)  // upper entry (i, j) of row i takes l_ji, the lower entry (j, i) of row j
+            for (int j = 0; j < n; ++j)
+                for (int k = brp[j]; k < bdiag[j]; ++k) {
+                    const int i = bcol[k];
+                    const int* b0 = bcol.data() + bdiag[i] + 1;
+                    const int* b1 = bcol.data() + brp[i + 1];
+                    const int* f = std::lower_bound(b0, b1, j);
+                    if (f == b1 || *f != j) {
+                        set_error("pattern of B is not symmetric at (%d, %d)", i, j);
+                        return PF2_BAD_INPUT;
+                    }
+                    tpos[f - bcol.data()] = k;
+                }
+        PF2_TRY(up(S->tpos, tpos));
+        PF2_TRY(S->bval.alloc(nnz));
+        PF2_TRY(S->fsym.alloc(nnz));
+        PF2_TRY(S->xB.alloc(n));
+    }
     if (K <= kBandMaxDeps) {
         const int R = banded ? std::min(n, band_rows) : n;
         const int P = banded ? (n + R - 1) / R : 0;
@@ -1351,7 +1620,7 @@ static Tri tri_of(pf2_solver* S) {
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
                 S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
-                S->rec.p };
+                S->rec.p, S->csr ? 1 : 0, S->bval.p, S->fsym.p, S->xB.p };
 }
 
 static bool uses_tri(const pf2_solver* S) {
@@ -1390,6 +1659,14 @@ __global__ void k_band_values(long long nk, int n, const int* __restrict__ pos, 
     }
 }
 
+// The factors on B's pattern for the CSR sweeps (pf2_solver::tpos).
+__global__ void k_fsym(long long nnz, const int* __restrict__ tpos, const double* __restrict__ fact, double* fsym) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
+        const int t = tpos[k];
+        fsym[k] = t >= 0 ? fact[t] : 1.0 / fact[-1 - t];
+    }
+}
+
 static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
     S->last = A;
     const bool mixed = S->opt.precision == PF2_PRECISION_MIXED;
@@ -1423,6 +1700,11 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
                 nk, S->n, H.pos.p, H.dpos.p, S->fact.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p);
             PF2_LAUNCH_CHECK();
         }
+    }
+    if (S->csr) {
+        k_fsym<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->tpos.p, S->fact.p,
+                                                                                    S->fsym.p);
+        PF2_LAUNCH_CHECK();
     }
     if (mixed) {
         k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fact.p,
@@ -1482,6 +1764,11 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         a.max_outer = kMaxOuter;
     }
     const int applies = max_applies(S);
+    if (S->csr && !precond_only) {  // A's values in B's numbering, for this solve's matrix
+        k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
+            S->nnz, a.A.val, S->bmap.p, S->bval.p);
+        PF2_LAUNCH_CHECK();
+    }
     if (uses_tri(S)) {
         PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
         // triangular-solve vectors start as "pending" (all bits set)
