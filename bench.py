@@ -66,7 +66,7 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def build_case(name, precond=None, ordering=None, gs=None):
+def build_case(name, precond=None, ordering=None, gs=None, cg=None):
     w = WORKLOADS[name]
     xy, tri = w["mesh"]()
     bu, bv, bp = mg.channel_boundary_nodes(xy, w["lx"], w["ly"], 1.5, cylinder=w["cyl"])
@@ -77,6 +77,8 @@ def build_case(name, precond=None, ordering=None, gs=None):
         prm["pressure_ordering"] = ordering
     if gs is not None:
         prm["gmres_orthogonalization"] = gs
+    if cg is not None:
+        prm["cg_variant"] = cg
     return w, xy, tri, bu, bv, bp, prm
 
 
@@ -135,7 +137,8 @@ def cpu_baseline(name, precond, max_seconds=25.0):
     w, xy, tri, bu, bv, bp, prm = build_case(name, precond)
     # the oracle runs the reference's algorithm: natural-order ILU/IC, modified Gram-Schmidt
     kw = {k: v for k, v in prm.items() if k not in ("calculate_loads", "body_boundary_id", "mean_velocity",
-                                                    "thickness", "pressure_ordering", "gmres_orthogonalization")}
+                                                    "thickness", "pressure_ordering", "gmres_orthogonalization",
+                                                    "cg_variant")}
     cyl = w["cyl"]
     op = O.make_params(lx=w["lx"], ly=w["ly"], tol=1e-8, has_cylinder=int(cyl is not None),
                        cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
@@ -187,8 +190,8 @@ def _timed(fn):
 def study_solver(args):
     """Pressure solve to a 1e-8 relative residual on the flow's own pressure matrix after
     --record steps of the cylinder case, on the 994,240-triangle mesh and its 1:4
-    refinement (3,976,960 triangles): FP64 PCG and the mixed-precision refinement, with
-    Jacobi and IC(0) (natural and multicolour order).  b = A x* with x* uniform in
+    refinement (3,976,960 triangles): FP64 PCG (standard and one-reduction) and the
+    mixed-precision refinement, with Jacobi and IC(0) on the multicolour order.  b = A x* with x* uniform in
     [-1, 1] (splitmix64 seed 0), x0 = 0; median of 3 solves after one warm-up."""
     import torch
     import gpupfem2_gb300 as g
@@ -218,10 +221,12 @@ def study_solver(args):
         # sequential levels here and one apply costs milliseconds)
         cases = [("fp64_jacobi", dict(precond="jacobi")),
                  ("fp64_ic0_multicolour", dict(precond="ic", ordering=1)),
+                 ("fp64_jacobi_one_reduction", dict(precond="jacobi", cg_variant=g.CG_ONE_REDUCTION)),
+                 ("fp64_ic0_multicolour_one_reduction", dict(precond="ic", ordering=1, cg_variant=g.CG_ONE_REDUCTION)),
                  ("mixed_jacobi", dict(precond="jacobi", precision=g.PRECISION_MIXED)),
                  ("mixed_ic0_multicolour", dict(precond="ic", ordering=1, precision=g.PRECISION_MIXED))]
         if args.quick:
-            cases = cases[:2] + [c for c in cases[2:] if "jacobi" in c[0]]
+            cases = cases[:4]
         for label, kw in cases:
             s = g.LinearSolver(A, "cg", tol=1e-8, maxit=20000, criterion=g.CRITERION_REL, **kw)
             times, info, x0 = [], None, None
@@ -322,6 +327,7 @@ def main():
     ap.add_argument("--precond", type=int, default=None, help="pressure preconditioner override (0 J, 1 ILU, 2 IC)")
     ap.add_argument("--ordering", type=int, default=None, help="ILU/IC ordering override (0 natural, 1 multicolour)")
     ap.add_argument("--gs", type=int, default=None, help="GMRES Gram-Schmidt override (0 modified, 1 classical twice)")
+    ap.add_argument("--cg", type=int, default=None, help="CG variant override (0 standard, 1 one reduction)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--study", default=None, choices=["solver", "learned"])
@@ -349,7 +355,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond, args.ordering, args.gs)
+    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond, args.ordering, args.gs, args.cg)
     mesh = g.Mesh2D.from_arrays(xy, tri)
     mesh.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
     params = g.default_params(**prm)
@@ -466,6 +472,7 @@ def main():
                    "particles": int(np_), "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
                    "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
                    "gmres_gram_schmidt": ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)],
+                   "cg_variant": ["standard", "one_reduction"][prm.get("cg_variant", 0)],
                    "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
                    "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),
                    "iterations_last_step": {"prediction": [list(info.it_prediction[c])[:prm["n_outer"]]

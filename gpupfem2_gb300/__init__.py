@@ -28,6 +28,7 @@ CRITERION_ABS, CRITERION_REL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RHS_GAUSSIAN, RHS_SINSIN = 0, 1
 RHS3D_GAUSSIAN, RHS3D_SINSINSIN = 0, 1
+CG_STANDARD, CG_ONE_REDUCTION = 0, 1
 FIELDS = {"ux": 0, "uy": 1, "ux_old": 2, "uy_old": 3, "pred_x": 4, "pred_y": 5, "p": 6, "p_old": 7}
 MESH_FIELDS = {"xy": 0, "tri": 1, "area": 2, "inv_jacobi": 3, "neighbor_offsets": 4, "neighbor_indices": 5,
                "edge_ids": 6}
@@ -49,7 +50,7 @@ class Params(C.Structure):
                 ("body_cx", C.c_double), ("body_cy", C.c_double),
                 ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int),
                 ("pressure_criterion", C.c_int), ("learn_steps", C.c_int), ("learn_rate", C.c_float),
-                ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int)]
+                ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int), ("cg_variant", C.c_int)]
 
 
 class MeshView(C.Structure):
@@ -66,7 +67,7 @@ class DirichletNode(C.Structure):
 class SolverOptions(C.Structure):
     _fields_ = [("kind", C.c_int), ("precond", C.c_int), ("tolerance", C.c_double), ("max_iterations", C.c_int),
                 ("criterion", C.c_int), ("precision", C.c_int), ("restart", C.c_int), ("ordering", C.c_int),
-                ("orthogonalization", C.c_int)]
+                ("orthogonalization", C.c_int), ("cg_variant", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -349,7 +350,8 @@ class LinearSolver:
     preconditioner (preconditioners.cuh)."""
 
     def __init__(self, A: SparseMatrixCSR, kind="cg", precond="jacobi", tol=1e-8, maxit=1000,
-                 criterion=CRITERION_ABS, precision=PRECISION_FP64, restart=0, ordering=0, orthogonalization=0):
+                 criterion=CRITERION_ABS, precision=PRECISION_FP64, restart=0, ordering=0, orthogonalization=0,
+                 cg_variant=0):
         o = SolverOptions()
         o.kind = SOLVER_GMRES if kind == "gmres" else SOLVER_CG
         o.precond = PRECOND[precond] if isinstance(precond, str) else int(precond)
@@ -360,6 +362,7 @@ class LinearSolver:
         o.restart = restart
         o.ordering = ordering
         o.orthogonalization = orthogonalization
+        o.cg_variant = cg_variant
         self.h = C.c_void_p()
         _check(lib().pf2_solver_create(A.h, C.byref(o), C.byref(self.h)), "pf2_solver_create")
 

@@ -511,6 +511,7 @@ pf2_status pf2_params_default(pf2_params* p) {
     p->learn_rate = 1e-3f;
     p->pressure_ordering = PF2_ORDERING_NATURAL;
     p->gmres_orthogonalization = PF2_GS_MODIFIED;
+    p->cg_variant = PF2_CG_STANDARD;
     return PF2_OK;
 }
 

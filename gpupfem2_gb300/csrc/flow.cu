@@ -130,6 +130,7 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.kind = PF2_SOLVER_CG;
     o.restart = 0;
     o.orthogonalization = PF2_GS_MODIFIED;
+    o.cg_variant = p->cg_variant;
     o.precond = p->pressure_precond;
     o.precision = p->pressure_precision;
     o.criterion = p->pressure_criterion;

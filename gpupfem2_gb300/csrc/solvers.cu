@@ -531,6 +531,8 @@ struct KArgs {
     double* x;
     const double* b;
     double *r, *z, *p, *q, *invd;
+    double* s;        // one-reduction CG: s = A p
+    int variant;      // PF2_CG_*
     double* partial;  // 4 arrays of gridDim doubles
     GridBarrier bar;
     Tri T;
@@ -673,12 +675,14 @@ __device__ __forceinline__ bool csr_dot_wait(const double* x, const int* __restr
 
 // Forward sweep of one CG iteration on B (rows in B's order, thread t taking rows t,
 // t + T, ...: a row's dependencies are lower rows, so the lowest unsolved row always
-// belongs to a thread that has reached it).  With UPDATE it first applies x += alpha p,
-// r -= alpha q to its row.  Writes the forward result and resets the row of z to the
-// pending marker for the backward sweep.  Returns the thread's r.r terms.
-template <bool UPDATE>
-__device__ double csr_fwd(const Tri& T, double alpha, double* r, const double* q, double* x, const double* p,
-                          double* z, int* err) {
+// belongs to a thread that has reached it).  First the row's vector updates: MODE 1
+// x += alpha p, r -= alpha q (q = A p); MODE 2 (one-reduction CG, q = A z) p = z + beta p,
+// s = q + beta s, x += alpha p, r -= alpha s (first: p = z, s = q).  Writes the forward
+// result and resets the row of z to the pending marker for the backward sweep.  Returns
+// the thread's r.r terms.
+template <int MODE>
+__device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, double* r, const double* q, double* x,
+                          double* p, double* sv, double* z, int* err) {
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
     const bool unit = T.kind != PF2_PRECOND_IC;  // ILU: L has a unit diagonal
@@ -697,10 +701,19 @@ __device__ double csr_fwd(const Tri& T, double alpha, double* r, const double* q
             dn = __ldg(&T.B.diag[row + stride]);
         }
         double ra = __ldcg(&r[row]);
-        if (UPDATE) {
+        if (MODE == 1) {
             ra -= alpha * __ldcg(&q[row]);
             __stcg(&r[row], ra);
             __stcg(&x[row], __ldcg(&x[row]) + alpha * __ldcg(&p[row]));
+        } else if (MODE == 2) {
+            const double zr = __ldcg(&z[row]), wr = __ldcg(&q[row]);
+            const double pr = first ? zr : zr + beta * __ldcg(&p[row]);
+            const double sr = first ? wr : wr + beta * __ldcg(&sv[row]);
+            __stcg(&p[row], pr);
+            __stcg(&sv[row], sr);
+            __stcg(&x[row], __ldcg(&x[row]) + alpha * pr);
+            ra -= alpha * sr;
+            __stcg(&r[row], ra);
         }
         rr += ra * ra;
         double sum;
@@ -766,24 +779,57 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         red[1] += bi * bi;
     }
     if (!grid_sync(a.bar, gridDim.x)) return;
-    red[2] = csr_fwd<false>(T, 0.0, a.r, nullptr, nullptr, nullptr, a.z, a.bar.err);
+    red[2] = csr_fwd<0>(T, 0.0, 0.0, true, a.r, nullptr, nullptr, nullptr, nullptr, a.z, a.bar.err);
     if (!grid_sync(a.bar, gridDim.x)) return;
-    red[0] = csr_bwd(T, a.r, a.z, a.p, a.bar.err);
-    if (!grid_reduce<3>(a.bar, red, sh)) return;
-    double gamma = red[0];
-    const double bnorm = sqrt(red[1]);
-    double rr = red[2];
+    const bool one = a.variant == PF2_CG_ONE_REDUCTION;
+    red[0] = csr_bwd(T, a.r, a.z, one ? nullptr : a.p, a.bar.err);
+    double red4[4] = { red[0], red[1], red[2], 0.0 };
+    if (one) {  // w = B z and z.w join the first reduction
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        red4[3] = spmv_rows(B, a.z, a.q, r0, r1);
+        if (!grid_reduce<4>(a.bar, red4, sh)) return;
+    } else {
+        if (!grid_reduce<3>(a.bar, red, sh)) return;
+        red4[0] = red[0];
+        red4[1] = red[1];
+        red4[2] = red[2];
+    }
+    double gamma = red4[0];
+    const double bnorm = sqrt(red4[1]);
+    double rr = red4[2];
     const double tol2 = a.tol * a.tol;
     auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
     int it = 0;
     bool conv = done_test(gamma, rr);
+    if (one) {
+        // Chronopoulos-Gear: per iteration the forward sweep (with the p, s, x, r
+        // updates), the backward sweep, w = B z with z.w, and one reduction of r.z, z.w, r.r
+        double alpha = gamma / red4[3], beta = 0.0;
+        bool first = true;
+        while (!conv && it < a.maxit) {
+            ++it;
+            double g3[3] = { 0.0, 0.0, 0.0 };  // r.z, z.w, r.r
+            g3[2] = csr_fwd<2>(T, alpha, beta, first, a.r, a.q, xB, a.p, a.s, a.z, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            g3[0] = csr_bwd(T, a.r, a.z, nullptr, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            g3[1] = spmv_rows(B, a.z, a.q, r0, r1);
+            if (!grid_reduce<3>(a.bar, g3, sh)) return;
+            rr = g3[2];
+            if (done_test(g3[0], rr)) { gamma = g3[0]; conv = true; break; }
+            beta = g3[0] / gamma;
+            alpha = g3[0] / (g3[1] - beta * g3[0] / alpha);
+            gamma = g3[0];
+            first = false;
+        }
+    }
     while (!conv && it < a.maxit) {
         ++it;
         double pq[1] = { spmv_rows(B, a.p, a.q, r0, r1) };
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
-        g2[1] = csr_fwd<true>(T, alpha, a.r, a.q, xB, a.p, a.z, a.bar.err);
+        g2[1] = csr_fwd<1>(T, alpha, 0.0, false, a.r, a.q, xB, a.p, nullptr, a.z, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return;
         g2[0] = csr_bwd(T, a.r, a.z, nullptr, a.bar.err);
         if (!grid_reduce<2>(a.bar, g2, sh)) return;
@@ -803,6 +849,81 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
+}
+
+// One-reduction PCG (Chronopoulos-Gear) with the Jacobi or no preconditioner, on the
+// block's rows: per iteration the vector updates (p = z + beta p, s = w + beta s,
+// x += alpha p, r -= alpha s, z = M^{-1} r) with the r.z and r.r terms, one barrier, then
+// w = A z with the z.w terms and one fused reduction of the three: two grid-wide steps
+// instead of three.  alpha = gamma / (z.w - beta gamma / alpha_old).
+__device__ void pcg_one_reduction(const KArgs& a, double* sh) {
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    const bool jac = a.precond == PF2_PRECOND_JACOBI;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    if (jac)
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
+    double red[4] = { 0.0, 0.0, 0.0, 0.0 };  // r.z, b.b, r.r, z.w
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double bi = a.b[i];
+        const double ri = bi - row_dot(a.A, i, a.x);
+        const double zi = jac ? ri * a.invd[i] : ri;
+        a.r[i] = ri;
+        __stcg(&a.z[i], zi);
+        red[0] += ri * zi;
+        red[1] += bi * bi;
+        red[2] += ri * ri;
+    }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    red[3] = spmv_rows(a.A, a.z, a.q, r0, r1);
+    if (!grid_reduce<4>(a.bar, red, sh)) return;
+    double gamma = red[0];
+    const double bnorm = sqrt(red[1]);
+    double rr = red[2];
+    const double tol2 = a.tol * a.tol;
+    auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
+    int it = 0;
+    bool conv = done_test(gamma, rr);
+    double alpha = gamma / red[3], beta = 0.0;
+    bool first = true;
+    while (!conv && it < a.maxit) {
+        ++it;
+        double g3[3] = { 0.0, 0.0, 0.0 };  // r.z, z.w, r.r
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double zi = __ldcg(&a.z[i]), wi = __ldcg(&a.q[i]);
+            const double pi = first ? zi : zi + beta * a.p[i];
+            const double si = first ? wi : wi + beta * a.s[i];
+            a.p[i] = pi;
+            a.s[i] = si;
+            a.x[i] += alpha * pi;
+            const double ri = a.r[i] - alpha * si;
+            a.r[i] = ri;
+            const double zn = jac ? ri * a.invd[i] : ri;
+            __stcg(&a.z[i], zn);
+            g3[0] += ri * zn;
+            g3[2] += ri * ri;
+        }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        g3[1] = spmv_rows(a.A, a.z, a.q, r0, r1);
+        if (!grid_reduce<3>(a.bar, g3, sh)) return;
+        rr = g3[2];
+        if (done_test(g3[0], rr)) { gamma = g3[0]; conv = true; break; }
+        beta = g3[0] / gamma;
+        alpha = g3[0] / (g3[1] - beta * g3[0] / alpha);
+        gamma = g3[0];
+        first = false;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_one(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    pcg_one_reduction(a, sh);
 }
 
 // SolverCG::solve (linear_solver.cu:440-515).  Per iteration: q = A p with p.q (one fused
@@ -1334,7 +1455,7 @@ struct pf2_solver {
     pf2_solver_options opt{};
     const pf2_mesh* mesh = nullptr;
     int n = 0, nnz = 0, blocks = 0, m = 0;
-    DevBuf<double> r, z, p, q, invd, partial, V, H, vpart;
+    DevBuf<double> r, z, p, q, s, invd, partial, V, H, vpart;
     DevBuf<unsigned> bar;  // count, gen
     DevBuf<int> err;
     DevBuf<int> rec;  // where a device wait gave up (5 ints)
@@ -1725,6 +1846,16 @@ static int max_applies(const pf2_solver* S) {
     return it + 2;
 }
 
+// The kernel of a solve: GMRES, mixed CG, the one-reduction CG with a local (Jacobi or
+// no) preconditioner, or k_pcg (the standard iteration, and ILU/IC in either variant).
+static void* solve_kernel(const pf2_solver_options& o) {
+    if (o.kind == PF2_SOLVER_GMRES) return (void*)k_gmres;
+    if (o.precision == PF2_PRECISION_MIXED) return (void*)k_pcg_mixed;
+    if (o.cg_variant == PF2_CG_ONE_REDUCTION && o.precond != PF2_PRECOND_ILU && o.precond != PF2_PRECOND_IC)
+        return (void*)k_pcg_one;
+    return (void*)k_pcg;
+}
+
 static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, const double* b, cudaStream_t st,
                                 bool precond_only = false) {
     KArgs a{};
@@ -1736,6 +1867,8 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.z = S->z.p;
     a.p = S->p.p;
     a.q = S->q.p;
+    a.s = S->s.p;
+    a.variant = S->opt.cg_variant;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
     a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->rec.p };
@@ -1792,7 +1925,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         }
         return PF2_OK;
     }
-    void* fn = (S->opt.kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
+    void* fn = mixed ? (void*)k_pcg_mixed : solve_kernel(S->opt);
     PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, S->smem, st);
     if (uses_tri(S)) {
         k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 2 * applies + 2);
@@ -1815,6 +1948,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
                 "unknown ordering %d", opt->ordering);
     PF2_REQUIRE(opt->orthogonalization == PF2_GS_MODIFIED || opt->orthogonalization == PF2_GS_CLASSICAL_TWICE,
                 PF2_BAD_INPUT, "unknown orthogonalization %d", opt->orthogonalization);
+    PF2_REQUIRE(opt->cg_variant == PF2_CG_STANDARD || opt->cg_variant == PF2_CG_ONE_REDUCTION, PF2_BAD_INPUT,
+                "unknown CG variant %d", opt->cg_variant);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
     pf2_solver* S = new pf2_solver();
@@ -1831,7 +1966,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     if (uses_tri(S) && (s = build_tri_plan(S))) return fail(s);
     // the banded triangular solve keeps a range of the solution in shared memory
     S->smem = S->band_P ? sizeof(double) * (size_t)S->band_R : 0;
-    void* fn = (opt->kind == PF2_SOLVER_GMRES) ? (void*)k_gmres : (mixed ? (void*)k_pcg_mixed : (void*)k_pcg);
+    void* fn = solve_kernel(*opt);
     if (S->smem) {
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->smem) != cudaSuccess ||
             cudaFuncSetAttribute((void*)k_precond_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1854,6 +1989,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // at least ~512 rows per block keeps the barrier count per unit of work low
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
+        (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_ONE_REDUCTION && (s = S->s.alloc(S->n))) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
         return fail(s);

@@ -226,6 +226,7 @@ typedef struct pf2_params {
     float learn_rate;        /* AdamW learning rate of that training */
     int pressure_ordering;   /* PF2_ORDERING_* of an ILU(0)/IC(0) pressure preconditioner */
     int gmres_orthogonalization; /* PF2_GS_* of the prediction GMRES */
+    int cg_variant;          /* PF2_CG_* of the pressure and correction CG solves */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -272,10 +273,17 @@ enum { PF2_PRECISION_FP64 = 0,    /* the reference's FP64 PCG */
                                       the iterated residual drops tenfold; CG only */
 enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
 enum { PF2_ORDERING_NATURAL = 0,    /* ILU(0)/IC(0) on A as numbered (the reference's)     */
-       PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring: ~8 levels, a
-                                        different (weaker) preconditioner, parallel solves */
+       PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring (6 colours on the
+                                        cylinder meshes): a different preconditioner, parallel
+                                        triangular solves */
 enum { PF2_GS_MODIFIED = 0,           /* GMRES Gram-Schmidt as the reference (linear_solver.cu:480-487) */
        PF2_GS_CLASSICAL_TWICE = 1 };  /* classical Gram-Schmidt with one reorthogonalisation */
+enum { PF2_CG_STANDARD = 0,           /* PCG as the reference (linear_solver.cu:301-376): two
+                                         grid-wide reductions per iteration */
+       PF2_CG_ONE_REDUCTION = 1 };    /* Chronopoulos-Gear PCG: the same iterates in exact
+                                         arithmetic with r.z, (A z).z and r.r in one reduction;
+                                         FP64 with Jacobi/none, or ILU(0)/IC(0) on few-level
+                                         orderings (else the standard iteration runs) */
 
 typedef struct pf2_solver_options {
     int kind;          /* PF2_SOLVER_* */
@@ -288,6 +296,7 @@ typedef struct pf2_solver_options {
     int ordering;      /* PF2_ORDERING_* of ILU(0)/IC(0) */
     int orthogonalization; /* GMRES: PF2_GS_MODIFIED (the reference's, one reduction per basis
                               vector) or PF2_GS_CLASSICAL_TWICE (two batched reductions) */
+    int cg_variant;        /* CG: PF2_CG_* */
 } pf2_solver_options;
 
 typedef struct pf2_solve_info {

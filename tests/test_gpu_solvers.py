@@ -200,3 +200,38 @@ def test_banded_triangular_solves_match_oracle(cuda, pc, band_rows, monkeypatch)
     ox, oinfo = O.pcg(rp, col, val, rhs, tol=1e-8, maxit=2000, precond=pc)
     assert info.converged == 1 and abs(info.iterations - oinfo.iterations) <= 2
     assert rel_err(x.cpu().numpy(), ox) < 1e-6
+
+
+@pytest.mark.parametrize("pc,ordering", [("none", 0), ("jacobi", 0), ("ilu", 0), ("ic", 0), ("ic", 1)])
+@pytest.mark.parametrize("criterion", [g.CRITERION_ABS, g.CRITERION_REL])
+def test_one_reduction_cg_matches_standard(cuda, pc, ordering, criterion):
+    """Chronopoulos-Gear CG (one fused reduction per iteration) reaches the standard
+    iteration's solution within the solve tolerance in the same number of iterations, up
+    to rounding at the stopping test."""
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    res = {}
+    for variant in (g.CG_STANDARD, g.CG_ONE_REDUCTION):
+        x = torch.zeros_like(b)
+        s = g.LinearSolver(A, "cg", pc, tol=1e-8, maxit=2000, criterion=criterion, ordering=ordering,
+                           cg_variant=variant)
+        info = s.solve(A, x, b)
+        assert info.converged == 1 and info.status == 0
+        res[variant] = (x.cpu().numpy(), info.iterations)
+    assert abs(res[0][1] - res[1][1]) <= 2
+    assert rel_err(res[1][0], res[0][0]) < 1e-6
+    ox, _ = O.pcg(rp, col, val, rhs, tol=1e-8, maxit=2000, precond=pc)
+    assert rel_err(res[1][0], ox) < 1e-6
+
+
+def test_one_reduction_cg_stops_at_the_limit(cuda):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    s = g.LinearSolver(A, "cg", "jacobi", tol=1e-30, maxit=7, cg_variant=g.CG_ONE_REDUCTION)
+    info = s.solve(A, x, b, check=False)
+    assert info.converged == 0 and info.iterations == 7
+    # seven one-reduction iterations equal seven standard ones up to rounding
+    y = torch.zeros_like(b)
+    g.LinearSolver(A, "cg", "jacobi", tol=1e-30, maxit=7).solve(A, y, b, check=False)
+    assert rel_err(x.cpu().numpy(), y.cpu().numpy()) < 1e-10
