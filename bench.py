@@ -66,7 +66,7 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def build_case(name, precond=None, ordering=None, gs=None, cg=None):
+def build_case(name, precond=None, ordering=None, gs=None, cg=None, pred=None):
     w = WORKLOADS[name]
     xy, tri = w["mesh"]()
     bu, bv, bp = mg.channel_boundary_nodes(xy, w["lx"], w["ly"], 1.5, cylinder=w["cyl"])
@@ -79,6 +79,8 @@ def build_case(name, precond=None, ordering=None, gs=None, cg=None):
         prm["gmres_orthogonalization"] = gs
     if cg is not None:
         prm["cg_variant"] = cg
+    if pred is not None:
+        prm["prediction_solver"] = pred
     return w, xy, tri, bu, bv, bp, prm
 
 
@@ -138,7 +140,7 @@ def cpu_baseline(name, precond, max_seconds=25.0):
     # the oracle runs the reference's algorithm: natural-order ILU/IC, modified Gram-Schmidt
     kw = {k: v for k, v in prm.items() if k not in ("calculate_loads", "body_boundary_id", "mean_velocity",
                                                     "thickness", "pressure_ordering", "gmres_orthogonalization",
-                                                    "cg_variant")}
+                                                    "cg_variant", "prediction_solver")}
     cyl = w["cyl"]
     op = O.make_params(lx=w["lx"], ly=w["ly"], tol=1e-8, has_cylinder=int(cyl is not None),
                        cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
@@ -328,6 +330,7 @@ def main():
     ap.add_argument("--ordering", type=int, default=None, help="ILU/IC ordering override (0 natural, 1 multicolour)")
     ap.add_argument("--gs", type=int, default=None, help="GMRES Gram-Schmidt override (0 modified, 1 classical twice)")
     ap.add_argument("--cg", type=int, default=None, help="CG variant override (0 standard, 1 one reduction)")
+    ap.add_argument("--pred", type=int, default=None, help="prediction solver override (1 GMRES, 2 BiCGStab)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--study", default=None, choices=["solver", "learned"])
@@ -355,7 +358,7 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond, args.ordering, args.gs, args.cg)
+    w, xy, tri, bu, bv, bp, prm = build_case(args.workload, args.precond, args.ordering, args.gs, args.cg, args.pred)
     mesh = g.Mesh2D.from_arrays(xy, tri)
     mesh.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
     params = g.default_params(**prm)
@@ -473,6 +476,7 @@ def main():
                    "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
                    "gmres_gram_schmidt": ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)],
                    "cg_variant": ["standard", "one_reduction"][prm.get("cg_variant", 0)],
+                   "prediction_solver": {1: "gmres", 2: "bicgstab"}[prm.get("prediction_solver", 1)],
                    "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
                    "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),
                    "iterations_last_step": {"prediction": [list(info.it_prediction[c])[:prm["n_outer"]]

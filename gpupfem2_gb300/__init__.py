@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(_HERE, "_build", "libpf2.so")
 _lib = None
 
 OK, NOT_CONVERGED, BAD_INPUT, OVERFLOW, CUDA_ERROR, TIMEOUT, IO_ERROR = range(7)
-SOLVER_CG, SOLVER_GMRES = 0, 1
+SOLVER_CG, SOLVER_GMRES, SOLVER_BICGSTAB = 0, 1, 2
 PRECOND = {"none": -1, "jacobi": 0, "ilu": 1, "ic": 2}
 CRITERION_ABS, CRITERION_REL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
@@ -50,7 +50,8 @@ class Params(C.Structure):
                 ("body_cx", C.c_double), ("body_cy", C.c_double),
                 ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int),
                 ("pressure_criterion", C.c_int), ("learn_steps", C.c_int), ("learn_rate", C.c_float),
-                ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int), ("cg_variant", C.c_int)]
+                ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int), ("cg_variant", C.c_int),
+                ("prediction_solver", C.c_int)]
 
 
 class MeshView(C.Structure):
@@ -353,7 +354,7 @@ class LinearSolver:
                  criterion=CRITERION_ABS, precision=PRECISION_FP64, restart=0, ordering=0, orthogonalization=0,
                  cg_variant=0):
         o = SolverOptions()
-        o.kind = SOLVER_GMRES if kind == "gmres" else SOLVER_CG
+        o.kind = {"gmres": SOLVER_GMRES, "bicgstab": SOLVER_BICGSTAB}.get(kind, SOLVER_CG)
         o.precond = PRECOND[precond] if isinstance(precond, str) else int(precond)
         o.tolerance = tol
         o.max_iterations = maxit

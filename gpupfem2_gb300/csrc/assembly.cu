@@ -512,6 +512,7 @@ pf2_status pf2_params_default(pf2_params* p) {
     p->pressure_ordering = PF2_ORDERING_NATURAL;
     p->gmres_orthogonalization = PF2_GS_MODIFIED;
     p->cg_variant = PF2_CG_STANDARD;
+    p->prediction_solver = PF2_SOLVER_GMRES;
     return PF2_OK;
 }
 

@@ -96,6 +96,8 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     PF2_REQUIRE(p->substeps >= 1, PF2_BAD_INPUT, "substeps must be >= 1");
     PF2_REQUIRE(p->dt > 0 && p->rho > 0, PF2_BAD_INPUT, "dt and rho must be positive");
     PF2_REQUIRE(p->scheme == 0 || p->scheme == 1, PF2_BAD_INPUT, "scheme must be 0 (A) or 1 (B)");
+    PF2_REQUIRE(p->prediction_solver == PF2_SOLVER_GMRES || p->prediction_solver == PF2_SOLVER_BICGSTAB,
+                PF2_BAD_INPUT, "prediction_solver must be PF2_SOLVER_GMRES or PF2_SOLVER_BICGSTAB");
     pf2_flow* F = new pf2_flow();
     F->mesh = mesh;
     F->P = *p;
@@ -122,7 +124,7 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.max_iterations = p->max_iterations;
     o.criterion = PF2_CRITERION_ABS;
     o.precision = PF2_PRECISION_FP64;
-    o.kind = PF2_SOLVER_GMRES;
+    o.kind = p->prediction_solver == PF2_SOLVER_BICGSTAB ? PF2_SOLVER_BICGSTAB : PF2_SOLVER_GMRES;
     o.precond = PF2_PRECOND_JACOBI;
     o.restart = p->gmres_restart;
     o.orthogonalization = p->gmres_orthogonalization;

@@ -531,8 +531,9 @@ struct KArgs {
     double* x;
     const double* b;
     double *r, *z, *p, *q, *invd;
-    double* s;        // one-reduction CG: s = A p
+    double* s;        // one-reduction CG: s = A p; BiCGStab: s = r - alpha v
     int variant;      // PF2_CG_*
+    double *rhat, *y, *t;  // BiCGStab: shadow residual, M^{-1} p, A M^{-1} s
     double* partial;  // 4 arrays of gridDim doubles
     GridBarrier bar;
     Tri T;
@@ -917,6 +918,108 @@ __device__ void pcg_one_reduction(const KArgs& a, double* sh) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+// Right-preconditioned BiCGStab (van der Vorst 1992) with the Jacobi or no
+// preconditioner, on the block's rows: per iteration two SpMVs, two barriers and three
+// fused reductions.  Stops on ||M^{-1} r|| < tol (absolute: the preconditioned residual
+// that the reference's GMRES tests, linear_solver.cu:500-505) or ||r|| <= tol ||b||
+// (relative); a zero (rhat, v) or t.t ends the solve unconverged.  x changes every
+// iteration (x += alpha y + omega z).
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    int r0, r1;
+    row_range(a.A.n, r0, r1);
+    const bool jac = a.precond == PF2_PRECOND_JACOBI;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    if (jac)
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.invd[i] = 1.0 / a.A.val[a.A.diag[i]];
+    // r = rhat = b - A x; p = v = 0
+    double red[4] = { 0.0, 0.0, 0.0, 0.0 };  // rhat.r, r.r, |M^{-1} r|^2, b.b
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double bi = a.b[i];
+        const double ri = bi - row_dot(a.A, i, a.x);
+        const double di = jac ? a.invd[i] : 1.0;
+        a.r[i] = ri;
+        a.rhat[i] = ri;
+        a.p[i] = 0.0;
+        a.q[i] = 0.0;
+        red[0] += ri * ri;
+        red[1] += ri * ri;
+        red[2] += (ri * di) * (ri * di);
+        red[3] += bi * bi;
+    }
+    if (!grid_reduce<4>(a.bar, red, sh)) return;
+    const double bnorm = sqrt(red[3]);
+    auto done_test = [&](double rr, double mm) { return rel ? sqrt(rr) <= a.tol * bnorm : sqrt(mm) < a.tol; };
+    double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+    double rho = red[0], rr = red[1], mm = red[2];
+    int it = 0;
+    bool conv = done_test(rr, mm), broke = false;
+    while (!conv && it < a.maxit) {
+        ++it;
+        const double beta = (rho / rho_old) * (alpha / omega);
+        // p = r + beta (p - omega v); y = M^{-1} p
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double pi = a.r[i] + beta * (a.p[i] - omega * a.q[i]);
+            a.p[i] = pi;
+            __stcg(&a.y[i], jac ? pi * a.invd[i] : pi);
+        }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        // v = A y, rhat.v
+        double rv[1] = { 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double vi = row_dot(a.A, i, a.y);
+            a.q[i] = vi;
+            rv[0] += a.rhat[i] * vi;
+        }
+        if (!grid_reduce<1>(a.bar, rv, sh)) return;
+        if (rv[0] == 0.0) { broke = true; break; }
+        alpha = rho / rv[0];
+        // s = r - alpha v; z = M^{-1} s
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double si = a.r[i] - alpha * a.q[i];
+            a.s[i] = si;
+            __stcg(&a.z[i], jac ? si * a.invd[i] : si);
+        }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        // t = A z, t.s, t.t
+        double ts[2] = { 0.0, 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double ti = row_dot(a.A, i, a.z);
+            a.t[i] = ti;
+            ts[0] += ti * a.s[i];
+            ts[1] += ti * ti;
+        }
+        if (!grid_reduce<2>(a.bar, ts, sh)) return;
+        if (ts[1] == 0.0) { broke = true; break; }
+        omega = ts[0] / ts[1];
+        // x += alpha y + omega z; r = s - omega t; rhat.r, r.r, |M^{-1} r|^2
+        double g3[3] = { 0.0, 0.0, 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            a.x[i] += alpha * __ldcg(&a.y[i]) + omega * __ldcg(&a.z[i]);
+            const double ri = a.s[i] - omega * a.t[i];
+            const double di = jac ? a.invd[i] : 1.0;
+            a.r[i] = ri;
+            g3[0] += a.rhat[i] * ri;
+            g3[1] += ri * ri;
+            g3[2] += (ri * di) * (ri * di);
+        }
+        if (!grid_reduce<3>(a.bar, g3, sh)) return;
+        rho_old = rho;
+        rho = g3[0];
+        rr = g3[1];
+        mm = g3[2];
+        conv = done_test(rr, mm);
+        if (!conv && (rho == 0.0 || omega == 0.0)) { broke = true; break; }
+    }
+    (void)broke;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(mm);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1455,7 +1558,7 @@ struct pf2_solver {
     pf2_solver_options opt{};
     const pf2_mesh* mesh = nullptr;
     int n = 0, nnz = 0, blocks = 0, m = 0;
-    DevBuf<double> r, z, p, q, s, invd, partial, V, H, vpart;
+    DevBuf<double> r, z, p, q, s, invd, partial, V, H, vpart, rhat, yv, tv;
     DevBuf<unsigned> bar;  // count, gen
     DevBuf<int> err;
     DevBuf<int> rec;  // where a device wait gave up (5 ints)
@@ -1850,6 +1953,7 @@ static int max_applies(const pf2_solver* S) {
 // no) preconditioner, or k_pcg (the standard iteration, and ILU/IC in either variant).
 static void* solve_kernel(const pf2_solver_options& o) {
     if (o.kind == PF2_SOLVER_GMRES) return (void*)k_gmres;
+    if (o.kind == PF2_SOLVER_BICGSTAB) return (void*)k_bicgstab;
     if (o.precision == PF2_PRECISION_MIXED) return (void*)k_pcg_mixed;
     if (o.cg_variant == PF2_CG_ONE_REDUCTION && o.precond != PF2_PRECOND_ILU && o.precond != PF2_PRECOND_IC)
         return (void*)k_pcg_one;
@@ -1869,6 +1973,9 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.q = S->q.p;
     a.s = S->s.p;
     a.variant = S->opt.cg_variant;
+    a.rhat = S->rhat.p;
+    a.y = S->yv.p;
+    a.t = S->tv.p;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
     a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->rec.p };
@@ -1939,8 +2046,12 @@ extern "C" {
 pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf2_solver** out) {
     PF2_REQUIRE(A && opt && out, PF2_BAD_INPUT, "null argument");
     *out = nullptr;
-    PF2_REQUIRE(opt->kind == PF2_SOLVER_CG || opt->kind == PF2_SOLVER_GMRES, PF2_BAD_INPUT, "unknown solver kind %d",
-                opt->kind);
+    PF2_REQUIRE(opt->kind == PF2_SOLVER_CG || opt->kind == PF2_SOLVER_GMRES || opt->kind == PF2_SOLVER_BICGSTAB,
+                PF2_BAD_INPUT, "unknown solver kind %d", opt->kind);
+    PF2_REQUIRE(opt->kind != PF2_SOLVER_BICGSTAB ||
+                    (opt->precond != PF2_PRECOND_ILU && opt->precond != PF2_PRECOND_IC &&
+                     opt->precision == PF2_PRECISION_FP64),
+                PF2_BAD_INPUT, "BiCGStab takes the Jacobi or no preconditioner, in FP64");
     PF2_REQUIRE(opt->precond >= PF2_PRECOND_NONE && opt->precond <= PF2_PRECOND_IC, PF2_BAD_INPUT,
                 "unknown preconditioner %d", opt->precond);
     PF2_REQUIRE(opt->max_iterations >= 0 && opt->tolerance >= 0, PF2_BAD_INPUT, "bad tolerance or iteration limit");
@@ -1990,6 +2101,8 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
         (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_ONE_REDUCTION && (s = S->s.alloc(S->n))) ||
+        (opt->kind == PF2_SOLVER_BICGSTAB && ((s = S->s.alloc(S->n)) || (s = S->rhat.alloc(S->n)) ||
+                                               (s = S->yv.alloc(S->n)) || (s = S->tv.alloc(S->n)))) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
         return fail(s);

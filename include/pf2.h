@@ -227,6 +227,7 @@ typedef struct pf2_params {
     int pressure_ordering;   /* PF2_ORDERING_* of an ILU(0)/IC(0) pressure preconditioner */
     int gmres_orthogonalization; /* PF2_GS_* of the prediction GMRES */
     int cg_variant;          /* PF2_CG_* of the pressure and correction CG solves */
+    int prediction_solver;   /* PF2_SOLVER_GMRES (the reference's) or PF2_SOLVER_BICGSTAB */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -263,7 +264,9 @@ pf2_status pf2_body_loads(const pf2_mesh* mesh, const pf2_params* p, double cx, 
 /* ---------------------------------------------------------------- Solvers
  * Replaces LinearSolver/SolverCG/SolverGMRES (src/linear_algebra/linear_solver.cuh:15-137)
  * and Preconditioner{Jacobi,ILU,IC} (src/linear_algebra/preconditioners.cuh:9-106). */
-enum { PF2_SOLVER_CG = 0, PF2_SOLVER_GMRES = 1 };
+enum { PF2_SOLVER_CG = 0, PF2_SOLVER_GMRES = 1,
+       PF2_SOLVER_BICGSTAB = 2 /* no reference counterpart: right-preconditioned BiCGStab,
+                                  Jacobi or no preconditioner, FP64 */ };
 enum { PF2_PRECOND_NONE = -1, PF2_PRECOND_JACOBI = 0, PF2_PRECOND_ILU = 1, PF2_PRECOND_IC = 2 };
 enum { PF2_CRITERION_ABS = 0,   /* CG: r^T z < tol^2; GMRES: |beta_k| < tol (the reference's) */
        PF2_CRITERION_REL = 1 }; /* ||b - A x|| <= tol ||b|| */

@@ -158,3 +158,27 @@ def test_learned_guess_keeps_the_solution(cuda):
         runs[x0] = (eng.field("p"), eng.field("ux"), used)
     assert rel_err(runs[1][0], runs[0][0]) < 1e-6 and rel_err(runs[1][1], runs[0][1]) < 1e-6
     assert runs[0][2] == 0
+
+
+@pytest.mark.parametrize("option", ["bicgstab", "one_reduction"])
+def test_solver_options_keep_the_step(cuda, option):
+    """BiCGStab for the velocity prediction, or one-reduction CG for the pressure and
+    correction solves: the same fields as the reference's solvers to the solve tolerance."""
+    xy, tri, bu, bv, bp, p, op = _channel_case()
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(4.0, 1.0)
+    runs = []
+    for alt in (False, True):
+        kw = dict(rho=1.0, mu=0.01, dt=0.005, scheme=0, substeps=3, level=3, n_outer=2, pressure_precond=2,
+                  pressure_ordering=1)
+        if alt:
+            kw.update(prediction_solver=g.SOLVER_BICGSTAB if option == "bicgstab" else g.SOLVER_GMRES,
+                      cg_variant=g.CG_ONE_REDUCTION if option == "one_reduction" else g.CG_STANDARD)
+        eng = g.FlowEngine(m, g.default_params(**kw), bu, bv, bp)
+        eng.seed()
+        for _ in range(3):
+            eng.step()
+            assert eng.info().converged == 1
+        runs.append({f: eng.field(f) for f in ("ux", "uy", "p")})
+    for f in ("ux", "uy", "p"):
+        assert rel_err(runs[1][f], runs[0][f]) < FIELD_TOL, f

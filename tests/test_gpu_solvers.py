@@ -235,3 +235,55 @@ def test_one_reduction_cg_stops_at_the_limit(cuda):
     y = torch.zeros_like(b)
     g.LinearSolver(A, "cg", "jacobi", tol=1e-30, maxit=7).solve(A, y, b, check=False)
     assert rel_err(x.cpu().numpy(), y.cpu().numpy()) < 1e-10
+
+
+@pytest.mark.parametrize("pc", ["none", "jacobi"])
+@pytest.mark.parametrize("criterion", [g.CRITERION_ABS, g.CRITERION_REL])
+def test_bicgstab_matches_oracle(cuda, pc, criterion):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "bicgstab", pc, tol=1e-10, maxit=2000, criterion=criterion).solve(A, x, b)
+    assert info.converged == 1 and info.status == 0
+    ox, oinfo = O.pcg(rp, col, val, rhs, tol=1e-12, maxit=5000, precond="jacobi")
+    assert rel_err(x.cpu().numpy(), ox) < 1e-6
+    r = torch.empty_like(b)
+    g.spmv(A, x, r)
+    if criterion == g.CRITERION_REL:
+        assert float(torch.linalg.norm(b - r)) <= 1e-10 * float(torch.linalg.norm(b)) * (1 + 1e-6)
+
+
+def test_bicgstab_on_the_nonsymmetric_prediction_system(cuda):
+    """The velocity-prediction matrix (outlet edge term: not symmetric) of a flow step:
+    BiCGStab and GMRES reach the same solution."""
+    xy, tri = mg.channel(64, 16, 4.0, 1.0)
+    bu, bv, bp = mg.channel_boundary_nodes(xy, 4.0, 1.0)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(4.0, 1.0)
+    eng = g.FlowEngine(m, g.default_params(rho=1.0, mu=0.01, dt=0.005, level=2, n_outer=1), bu, bv, bp)
+    eng.seed()
+    eng.step()
+    A, _ = eng.system(0)
+    rp_, col_, val_ = A.download()
+    dense = np.zeros((rp_.size - 1,) * 2)
+    for i in range(rp_.size - 1):
+        dense[i, col_[rp_[i]:rp_[i + 1]]] = val_[rp_[i]:rp_[i + 1]]
+    assert np.abs(dense - dense.T).max() > 1e-12  # the outlet term breaks the symmetry
+    n = A.rows
+    b = torch.tensor(mg.uniform_pm1(3, n), device="cuda")
+    x1, x2 = torch.zeros_like(b), torch.zeros_like(b)
+    i1 = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-12, maxit=2000).solve(A, x1, b)
+    i2 = g.LinearSolver(A, "gmres", "jacobi", tol=1e-12, maxit=2000).solve(A, x2, b)
+    assert i1.converged == 1 and i2.converged == 1
+    assert rel_err(x1.cpu().numpy(), x2.cpu().numpy()) < 1e-8
+
+
+def test_bicgstab_stops_at_the_limit_and_rejects_triangular_preconditioners(cuda):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-30, maxit=5).solve(A, x, b, check=False)
+    assert info.converged == 0 and info.iterations == 5 and np.isfinite(x.cpu().numpy()).all()
+    with pytest.raises(g.Pf2Error) as e:
+        g.LinearSolver(A, "bicgstab", "ilu")
+    assert e.value.status == g.BAD_INPUT
