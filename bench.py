@@ -39,13 +39,15 @@ WORKLOADS = {
     "cylinder": dict(mesh=lambda: mg.cylinder_channel(), lx=2.2, ly=0.41, cyl=(0.2, 0.2, 0.05),
                      params=dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3,
                                  pressure_precond=2, calculate_loads=1, body_boundary_id=3, thickness=0.1,
-                                 mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1)),
+                                 mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1,
+                                 prediction_solver=2)),
     # the same case at a quarter of the cells (248,560 triangles): small captures under ncu
     "cylinder_quarter": dict(mesh=lambda: mg.cylinder_channel(nxh=350, nyh=400, nr=12), lx=2.2, ly=0.41,
                              cyl=(0.2, 0.2, 0.05),
                              params=dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3,
                                          pressure_precond=2, calculate_loads=1, body_boundary_id=3, thickness=0.1,
-                                         mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1)),
+                                         mean_velocity=1.0, pressure_ordering=1, gmres_orthogonalization=1,
+                                         prediction_solver=2)),
     "channel": dict(mesh=lambda: mg.channel(), lx=4.0, ly=1.0, cyl=None,
                     params=dict(rho=1.0, mu=0.01, dt=0.005, scheme=0, level=3, n_outer=2, substeps=3,
                                 pressure_precond=1)),
