@@ -116,6 +116,10 @@ struct Tri {
     const double* bval;
     const double* fsym;
     double* xB;
+    // B's rows in sweep groups: group g holds rows cstart[g] .. cstart[g + 1] (the colours
+    // of a multicolour order, or all rows), swept one group after the other
+    int ngroups;
+    const int* cstart;
 };
 
 __device__ __forceinline__ bool wait_flag(const int* flag, int epoch, int* err, int* rec, int row, int dep) {
@@ -674,9 +678,11 @@ __device__ __forceinline__ bool csr_dot_wait(const double* x, const int* __restr
     return true;
 }
 
-// Forward sweep of one CG iteration on B (rows in B's order, thread t taking rows t,
-// t + T, ...: a row's dependencies are lower rows, so the lowest unsolved row always
-// belongs to a thread that has reached it).  First the row's vector updates: MODE 1
+// Forward sweep of one CG iteration on B: group after group (a colour of a multicolour
+// order, so a group's rows depend only on earlier groups), thread t taking rows
+// g0 + t, g0 + t + T, ... of each.  Every thread's rows follow B's order and a row's
+// dependencies are lower rows, so the lowest unsolved row always belongs to a thread
+// that has reached it.  First the row's vector updates: MODE 1
 // x += alpha p, r -= alpha q (q = A p); MODE 2 (one-reduction CG, q = A z) p = z + beta p,
 // s = q + beta s, x += alpha p, r -= alpha s (first: p = z, s = q).  Writes the forward
 // result and resets the row of z to the pending marker for the backward sweep.  Returns
@@ -688,16 +694,20 @@ __device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, d
     const int stride = gridDim.x * blockDim.x;
     const bool unit = T.kind != PF2_PRECOND_IC;  // ILU: L has a unit diagonal
     double rr = 0.0;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    (void)n;
+    for (int gi = 0; gi < T.ngroups; ++gi) {
+    const int g0 = __ldg(&T.cstart[gi]), g1 = __ldg(&T.cstart[gi + 1]);
     // each row's pattern bounds are loaded one row ahead
-    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    int row = g0 + tid;
     int k0n = 0, dn = 0;
-    if (row < n) {
+    if (row < g1) {
         k0n = __ldg(&T.B.rowptr[row]);
         dn = __ldg(&T.B.diag[row]);
     }
-    for (; row < n; row += stride) {
+    for (; row < g1; row += stride) {
         const int k0 = k0n, d = dn;
-        if (row + stride < n) {
+        if (row + stride < g1) {
             k0n = __ldg(&T.B.rowptr[row + stride]);
             dn = __ldg(&T.B.diag[row + stride]);
         }
@@ -723,25 +733,30 @@ __device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, d
         __stcg(&T.tmp[row], v);
         __stcg(&z[row], Pending<double>::marker());
     }
+    }
     return rr;
 }
 
-// Backward sweep (rows in reverse order): z = U^{-1} t, the forward result reset to the
+// Backward sweep (groups and rows in reverse order): z = U^{-1} t, the forward result reset to the
 // marker; with p_init the first direction p = z is stored too.  Returns the r.z terms.
 __device__ double csr_bwd(const Tri& T, const double* r, double* z, double* p_init, int* err) {
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
     double rz = 0.0;
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    (void)n;
+    for (int gi = T.ngroups - 1; gi >= 0; --gi) {
+    // rows g1 - 1 - t, g1 - 1 - t - stride, ... of the group, highest first
+    const int g0 = __ldg(&T.cstart[gi]), g1 = __ldg(&T.cstart[gi + 1]);
+    int row = g1 - 1 - tid;
     int dn = 0, k1n = 0;
-    if (t < n) {
-        dn = __ldg(&T.B.diag[n - 1 - t]);
-        k1n = __ldg(&T.B.rowptr[n - t]);
+    if (row >= g0) {
+        dn = __ldg(&T.B.diag[row]);
+        k1n = __ldg(&T.B.rowptr[row + 1]);
     }
-    for (; t < n; t += stride) {
-        const int row = n - 1 - t;
+    for (; row >= g0; row -= stride) {
         const int d = dn, k1 = k1n;
-        if (t + stride < n) {
+        if (row - stride >= g0) {
             dn = __ldg(&T.B.diag[row - stride]);
             k1n = __ldg(&T.B.rowptr[row - stride + 1]);
         }
@@ -753,6 +768,7 @@ __device__ double csr_bwd(const Tri& T, const double* r, double* z, double* p_in
         if (p_init) __stcg(&p_init[row], v);
         __stcg(&T.tmp[row], Pending<double>::marker());
         rz += __ldcg(&r[row]) * v;
+    }
     }
     return rz;
 }
@@ -1584,10 +1600,90 @@ struct pf2_solver {
     bool csr = false;
     DevBuf<double> bval, fsym, xB;
     DevBuf<int> tpos;
+    int ngroups = 0;
+    DevBuf<int> cstart;
     int levels_fwd = 0, levels_bwd = 0, colors = 0;
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
 };
+
+// Greedy colouring leaves a thin tail of high colours (on the cylinder meshes 306 of
+// 499,288 nodes in colours 4 and 5), and each colour is one more dependency level of
+// both triangular sweeps.  Each tail node is moved below K (the first colour whose tail
+// holds under 0.2 % of the nodes) by a Kempe-chain swap: for colours a, b < K, swap a and
+// b in the (a, b)-components of v's a-coloured neighbours, provided none of those
+// components reaches a b-coloured neighbour of v; v then takes a.  Swaps keep the
+// colouring proper.  Nodes that no swap frees keep their colour; the search stops after
+// 64 n visited nodes.  Returns the number of colours.
+static int kempe_trim(int n, const std::vector<int>& rp, const std::vector<int>& col, std::vector<int>& color,
+                      int nc) {
+    std::vector<long long> size(nc, 0);
+    for (int i = 0; i < n; ++i) size[color[i]]++;
+    int K = nc;
+    long long tail = 0;
+    while (K > 1 && tail + size[K - 1] < std::max(1LL, (long long)n / 500)) tail += size[--K];
+    if (K == nc) return nc;
+    std::vector<int> mark(n, -1), comp, queue;
+    long long budget = 64LL * n;
+    int stamp = 0;
+    auto fix = [&](int v) {
+        for (int a = 0; a < K; ++a) {
+            bool has_a = false;
+            for (int k = rp[v]; k < rp[v + 1]; ++k) has_a |= col[k] != v && color[col[k]] == a;
+            if (!has_a) {
+                color[v] = a;
+                return true;
+            }
+            for (int b = 0; b < K; ++b) {
+                if (b == a) continue;
+                ++stamp;
+                comp.clear();
+                queue.clear();
+                for (int k = rp[v]; k < rp[v + 1]; ++k)
+                    if (col[k] != v && color[col[k]] == a && mark[col[k]] != stamp) {
+                        mark[col[k]] = stamp;
+                        queue.push_back(col[k]);
+                    }
+                bool ok = true;
+                for (size_t h = 0; h < queue.size() && ok; ++h) {
+                    const int x = queue[h];
+                    comp.push_back(x);
+                    if (--budget < 0) return false;
+                    for (int k = rp[x]; k < rp[x + 1]; ++k) {
+                        const int y = col[k];
+                        if (y == x || y == v || mark[y] == stamp) continue;
+                        if (color[y] != a && color[y] != b) continue;
+                        // a b-coloured neighbour of v inside the component: the swap would
+                        // give v an a-coloured neighbour again
+                        bool nb_of_v = false;
+                        for (int q = rp[v]; q < rp[v + 1]; ++q) nb_of_v |= col[q] == y;
+                        if (nb_of_v && color[y] == b) { ok = false; break; }
+                        mark[y] = stamp;
+                        queue.push_back(y);
+                    }
+                }
+                if (!ok) continue;
+                for (int x : comp) color[x] = color[x] == a ? b : a;
+                color[v] = a;
+                return true;
+            }
+        }
+        return false;
+    };
+    // a few passes: a swap for one node can free another node's colour
+    for (int pass = 0; pass < 4 && budget > 0; ++pass) {
+        int left = 0, fixed = 0;
+        for (int v = 0; v < n && budget > 0; ++v)
+            if (color[v] >= K) {
+                if (fix(v)) ++fixed;
+                else ++left;
+            }
+        if (left == 0 || fixed == 0) break;
+    }
+    int m = 0;
+    for (int i = 0; i < n; ++i) m = std::max(m, color[i] + 1);
+    return m;
+}
 
 static pf2_status build_tri_plan(pf2_solver* S) {
     const pf2_mesh* M = S->mesh;
@@ -1598,6 +1694,7 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     // ordering: natural (the reference's) or greedy multicolour in natural order, rows
     // of a colour kept in natural order
     std::vector<int> perm(n), iperm(n);
+    std::vector<int> groups{ 0, n };  // sweep groups of the CSR path: the colours, or all rows
     if (S->opt.ordering == PF2_ORDERING_MULTICOLOR) {
         std::vector<int> color(n, -1);
         int nc = 0;
@@ -1611,10 +1708,12 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             color[i] = c;
             nc = std::max(nc, c + 1);
         }
+        nc = kempe_trim(n, rp, col, color, nc);
         S->colors = nc;
         std::vector<int> cnt(nc + 1, 0);
         for (int i = 0; i < n; ++i) cnt[color[i] + 1]++;
         for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
+        groups = cnt;
         for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
     } else {
         for (int i = 0; i < n; ++i) perm[i] = i;
@@ -1753,6 +1852,8 @@ static pf2_status build_tri_plan(pf2_solver* S) {
                     tpos[f - bcol.data()] = k;
                 }
         PF2_TRY(up(S->tpos, tpos));
+        PF2_TRY(up(S->cstart, groups));
+        S->ngroups = (int)groups.size() - 1;
         PF2_TRY(S->bval.alloc(nnz));
         PF2_TRY(S->fsym.alloc(nnz));
         PF2_TRY(S->xB.alloc(n));
@@ -1844,7 +1945,7 @@ static Tri tri_of(pf2_solver* S) {
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
                 S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
-                S->rec.p, S->csr ? 1 : 0, S->bval.p, S->fsym.p, S->xB.p };
+                S->rec.p, S->csr ? 1 : 0, S->bval.p, S->fsym.p, S->xB.p, S->ngroups, S->cstart.p };
 }
 
 static bool uses_tri(const pf2_solver* S) {

@@ -276,9 +276,10 @@ enum { PF2_PRECISION_FP64 = 0,    /* the reference's FP64 PCG */
                                       the iterated residual drops tenfold; CG only */
 enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
 enum { PF2_ORDERING_NATURAL = 0,    /* ILU(0)/IC(0) on A as numbered (the reference's)     */
-       PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring (6 colours on the
-                                        cylinder meshes): a different preconditioner, parallel
-                                        triangular solves */
+       PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring whose thin tail of
+                                        high colours is moved down by Kempe-chain swaps (4
+                                        colours on the cylinder meshes): a different
+                                        preconditioner, parallel triangular solves */
 enum { PF2_GS_MODIFIED = 0,           /* GMRES Gram-Schmidt as the reference (linear_solver.cu:480-487) */
        PF2_GS_CLASSICAL_TWICE = 1 };  /* classical Gram-Schmidt with one reorthogonalisation */
 enum { PF2_CG_STANDARD = 0,           /* PCG as the reference (linear_solver.cu:301-376): two
