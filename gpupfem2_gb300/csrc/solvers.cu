@@ -77,6 +77,9 @@ struct BandDir {
     double* dinv;      // [slot] 1 / dividing diagonal (1 for ILU forward)
     float* val32;      // FP32 copies (mixed precision)
     float* dinv32;
+    // sync-free solve: the slots' level groups (slots gstart[g] .. gstart[g + 1])
+    int ngroups;
+    const int* gstart;
 };
 
 struct Band {
@@ -378,7 +381,10 @@ __device__ void tri_solve_slots(const Tri& T, int dir, V* src, V* dst, int* err)
     const V* vals = BandVals<V>::val(D);
     const V* dinv = BandVals<V>::dinv(D);
     const int stride = gridDim.x * blockDim.x;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    (void)n;
+    for (int gi = 0; gi < D.ngroups; ++gi)
+    for (int t = __ldg(&D.gstart[gi]) + blockIdx.x * blockDim.x + threadIdx.x, g1 = __ldg(&D.gstart[gi + 1]); t < g1;
+         t += stride) {
         const int row = __ldg(&D.row[t]);
         const V in = __ldcg(&src[__ldg(&D.rhs[t])]);
         const V di = __ldg(&dinv[t]);
@@ -418,7 +424,10 @@ __device__ double slots_fwd_cg(const Tri& T, V alpha, V* r, const V* q, V* x, co
     V* tmp = SlotVecs<V>::tmp(T);
     V* outB = SlotVecs<V>::outB(T);
     V rr = V(0);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    (void)n;
+    for (int gi = 0; gi < D.ngroups; ++gi)
+    for (int t = __ldg(&D.gstart[gi]) + blockIdx.x * blockDim.x + threadIdx.x, g1 = __ldg(&D.gstart[gi + 1]); t < g1;
+         t += stride) {
         const int row = __ldg(&D.row[t]);
         const int ai = __ldg(&D.rhs[t]);  // the row in A's numbering
         const V ra = __ldcg(&r[ai]) - alpha * __ldcg(&q[ai]);
@@ -444,7 +453,10 @@ __device__ double slots_bwd_cg(const Tri& T, const V* r, V* z, int* err) {
     V* tmp = SlotVecs<V>::tmp(T);
     V* outB = SlotVecs<V>::outB(T);
     V rz = V(0);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+    (void)n;
+    for (int gi = 0; gi < D.ngroups; ++gi)
+    for (int t = __ldg(&D.gstart[gi]) + blockIdx.x * blockDim.x + threadIdx.x, g1 = __ldg(&D.gstart[gi + 1]); t < g1;
+         t += stride) {
         const int row = __ldg(&D.row[t]);
         const V in = __ldcg(&tmp[row]);
         V sum;
@@ -1565,7 +1577,8 @@ __global__ void k_precond_apply(KArgs a) {
 using namespace pf2;
 
 struct BandHost {
-    DevBuf<int> rstep, sptr, row, rhs, dep, pos, dpos;
+    DevBuf<int> rstep, sptr, row, rhs, dep, pos, dpos, gstart;
+    int ngroups = 0;
     DevBuf<double> val, dinv;
     DevBuf<float> val32, dinv32;
 };
@@ -1744,6 +1757,10 @@ static pf2_status build_tri_plan(pf2_solver* S) {
         nl = std::max(nl, l + 1);
     }
     S->levels_fwd = nl;
+    std::vector<int> level_groups[2];
+    level_groups[0].assign(nl + 1, 0);
+    for (int i = 0; i < n; ++i) level_groups[0][lev[i] + 1]++;
+    for (int l = 0; l < nl; ++l) level_groups[0][l + 1] += level_groups[0][l];
     std::vector<int> order(n);
     for (int i = 0; i < n; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
@@ -1760,6 +1777,9 @@ static pf2_status build_tri_plan(pf2_solver* S) {
         nl = std::max(nl, l + 1);
     }
     S->levels_bwd = nl;
+    level_groups[1].assign(nl + 1, 0);
+    for (int i = 0; i < n; ++i) level_groups[1][lev[i] + 1]++;
+    for (int l = 0; l < nl; ++l) level_groups[1][l + 1] += level_groups[1][l];
     for (int i = 0; i < n; ++i) order[i] = n - 1 - i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lev[a] < lev[b]; });
     PF2_TRY(S->bwd_order.alloc(n));
@@ -1868,7 +1888,11 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             std::vector<int> rstep(P + 1, 0), sptr, srow;
             srow.reserve(n);
             std::vector<int> loc(n, 0);
-            if (!banded) srow = dir == 0 ? fwd_h : bwd_h;
+            if (!banded) {
+                srow = dir == 0 ? fwd_h : bwd_h;
+                PF2_TRY(up(H.gstart, level_groups[dir]));
+                H.ngroups = (int)level_groups[dir].size() - 1;
+            }
             for (int r = 0; r < P; ++r) {
                 const int r0 = rs[r], r1 = rs[r + 1];
                 int nl = 0;
@@ -1939,7 +1963,8 @@ static Csr csr_of(const pf2_csr* A) {
 
 static Tri tri_of(pf2_solver* S) {
     auto dir = [&](BandHost& H) {
-        return BandDir{ H.rstep.p, H.sptr.p, H.row.p, H.rhs.p, H.dep.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p };
+        return BandDir{ H.rstep.p, H.sptr.p, H.row.p, H.rhs.p, H.dep.p, H.val.p, H.dinv.p, H.val32.p, H.dinv32.p,
+                        H.ngroups, H.gstart.p };
     };
     const Band band{ S->band_P, S->band_R, S->band_K, S->band_rs.p, dir(S->band[0]), dir(S->band[1]) };
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
