@@ -1721,12 +1721,27 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             color[i] = c;
             nc = std::max(nc, c + 1);
         }
-        nc = kempe_trim(n, rp, col, color, nc);
+        // PF2_KEMPE=0 (tuning): keep the greedy colours and sweep the tail colours with the
+        // last main colour (same permutation as greedy, fewer sweep groups)
+        const char* ke = getenv("PF2_KEMPE");
+        const bool kempe = !ke || atoi(ke) != 0;
+        const int nc_greedy = nc;
+        if (kempe) nc = kempe_trim(n, rp, col, color, nc);
         S->colors = nc;
         std::vector<int> cnt(nc + 1, 0);
         for (int i = 0; i < n; ++i) cnt[color[i] + 1]++;
         for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
         groups = cnt;
+        if (!kempe) {  // merge the thin tail (under 0.2 % of the rows) into the group before it
+            int g = nc_greedy;
+            long long tail = 0;
+            while (g > 1 && tail + (cnt[g] - cnt[g - 1]) < std::max(1, n / 500)) {
+                tail += cnt[g] - cnt[g - 1];
+                --g;
+            }
+            groups.assign(cnt.begin(), cnt.begin() + g);
+            groups.push_back(n);
+        }
         for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
     } else {
         for (int i = 0; i < n; ++i) perm[i] = i;
