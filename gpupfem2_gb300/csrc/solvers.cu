@@ -1698,6 +1698,49 @@ static int kempe_trim(int n, const std::vector<int>& rp, const std::vector<int>&
     return m;
 }
 
+// Multicolour permutation of a symmetric pattern: greedy colouring in row order, then
+// (kempe) the thin tail of high colours moved down by kempe_trim.  perm[r] is the row of
+// A at position r of B (colour by colour, rows of a colour ascending); groups receives
+// the sweep groups (the colour starts and n), where without kempe the tail colours are
+// merged into the group before them.  Returns the number of colours.
+static int multicolour_order(int n, const int* rp, const int* col, bool kempe, std::vector<int>& perm,
+                             std::vector<int>& groups) {
+    std::vector<int> color(n, -1);
+    int nc = 0;
+    std::vector<char> used;
+    for (int i = 0; i < n; ++i) {
+        used.assign(nc + 1, 0);
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (col[k] < i) used[color[col[k]]] = 1;
+        int c = 0;
+        while (used[c]) ++c;
+        color[i] = c;
+        nc = std::max(nc, c + 1);
+    }
+    const int nc_greedy = nc;
+    if (kempe) {
+        const std::vector<int> rpv(rp, rp + n + 1), colv(col, col + rp[n]);
+        nc = kempe_trim(n, rpv, colv, color, nc);
+    }
+    std::vector<int> cnt(nc + 1, 0);
+    for (int i = 0; i < n; ++i) cnt[color[i] + 1]++;
+    for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
+    groups = cnt;
+    if (!kempe) {  // merge the thin tail (under 0.2 % of the rows) into the group before it
+        int g = nc_greedy;
+        long long tail = 0;
+        while (g > 1 && tail + (cnt[g] - cnt[g - 1]) < std::max(1, n / 500)) {
+            tail += cnt[g] - cnt[g - 1];
+            --g;
+        }
+        groups.assign(cnt.begin(), cnt.begin() + g);
+        groups.push_back(n);
+    }
+    perm.assign(n, 0);
+    for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
+    return nc;
+}
+
 static pf2_status build_tri_plan(pf2_solver* S) {
     const pf2_mesh* M = S->mesh;
     const int n = M->nv, nnz = M->nnz;
@@ -1709,40 +1752,10 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     std::vector<int> perm(n), iperm(n);
     std::vector<int> groups{ 0, n };  // sweep groups of the CSR path: the colours, or all rows
     if (S->opt.ordering == PF2_ORDERING_MULTICOLOR) {
-        std::vector<int> color(n, -1);
-        int nc = 0;
-        std::vector<char> used;
-        for (int i = 0; i < n; ++i) {
-            used.assign(nc + 1, 0);
-            for (int k = rp[i]; k < rp[i + 1]; ++k)
-                if (col[k] < i) used[color[col[k]]] = 1;
-            int c = 0;
-            while (used[c]) ++c;
-            color[i] = c;
-            nc = std::max(nc, c + 1);
-        }
         // PF2_KEMPE=0 (tuning): keep the greedy colours and sweep the tail colours with the
         // last main colour (same permutation as greedy, fewer sweep groups)
         const char* ke = getenv("PF2_KEMPE");
-        const bool kempe = !ke || atoi(ke) != 0;
-        const int nc_greedy = nc;
-        if (kempe) nc = kempe_trim(n, rp, col, color, nc);
-        S->colors = nc;
-        std::vector<int> cnt(nc + 1, 0);
-        for (int i = 0; i < n; ++i) cnt[color[i] + 1]++;
-        for (int c = 0; c < nc; ++c) cnt[c + 1] += cnt[c];
-        groups = cnt;
-        if (!kempe) {  // merge the thin tail (under 0.2 % of the rows) into the group before it
-            int g = nc_greedy;
-            long long tail = 0;
-            while (g > 1 && tail + (cnt[g] - cnt[g - 1]) < std::max(1, n / 500)) {
-                tail += cnt[g] - cnt[g - 1];
-                --g;
-            }
-            groups.assign(cnt.begin(), cnt.begin() + g);
-            groups.push_back(n);
-        }
-        for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
+        S->colors = multicolour_order(n, rp.data(), col.data(), !ke || atoi(ke) != 0, perm, groups);
     } else {
         for (int i = 0; i < n; ++i) perm[i] = i;
     }
@@ -2183,6 +2196,20 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
 }
 
 extern "C" {
+
+pf2_status pf2_multicolour_order(int n, const int* rowptr, const int* col, int kempe, int* perm, int* ncolours,
+                                 int* nstarts, int* starts) {
+    PF2_REQUIRE(n > 0 && rowptr && col && perm && ncolours && nstarts, PF2_BAD_INPUT, "null argument");
+    for (int i = 0; i < n; ++i)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            PF2_REQUIRE(col[k] >= 0 && col[k] < n, PF2_BAD_INPUT, "column %d of row %d out of range", col[k], i);
+    std::vector<int> p, groups;
+    *ncolours = multicolour_order(n, rowptr, col, kempe != 0, p, groups);
+    std::copy(p.begin(), p.end(), perm);
+    *nstarts = (int)groups.size();
+    if (starts) std::copy(groups.begin(), groups.end(), starts);
+    return PF2_OK;
+}
 
 pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf2_solver** out) {
     PF2_REQUIRE(A && opt && out, PF2_BAD_INPUT, "null argument");

@@ -303,6 +303,14 @@ typedef struct pf2_solver_options {
     int cg_variant;        /* CG: PF2_CG_* */
 } pf2_solver_options;
 
+/* The multicolour order of PF2_ORDERING_MULTICOLOR for a symmetric CSR pattern (host
+ * arrays; no GPU work): perm[r] = row of A at position r of P A P^T; starts receives
+ * *nstarts (<= n + 1) sweep-group starts ending with n (NULL: sizes only); kempe != 0
+ * moves greedy colouring's tail of high colours down by Kempe-chain swaps (the solver's
+ * choice), 0 keeps greedy's colours. */
+pf2_status pf2_multicolour_order(int n, const int* rowptr, const int* col, int kempe, int* perm, int* ncolours,
+                                 int* nstarts, int* starts);
+
 typedef struct pf2_solve_info {
     int iterations;      /* total inner iterations */
     int converged;
