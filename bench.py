@@ -364,7 +364,10 @@ def main():
     mesh = g.Mesh2D.from_arrays(xy, tri)
     mesh.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
     params = g.default_params(**prm)
-    eng = g.FlowEngine(mesh, params, bu, bv, bp, capacity_factor=2.0)
+    # reseeding only adds particles (the reference's population check), and they gather
+    # where the flow converges: room for 4x the seeded count covers about 150 steps of
+    # the cylinder case (2.8x after 80 steps)
+    eng = g.FlowEngine(mesh, params, bu, bv, bp, capacity_factor=4.0)
     eng.seed()
     for _ in range(args.warmup):
         eng.step()
