@@ -68,6 +68,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def replica_max(value, device):
+    """The slowest replica's value: with one independent replica per GPU (the step does
+    not shard), the job's ms per step is the maximum over the ranks."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def build_case(name, precond=None, ordering=None, gs=None, cg=None, pred=None):
     w = WORKLOADS[name]
     xy, tri = w["mesh"]()
@@ -393,9 +403,7 @@ def main():
     launches = L.pf2_kernel_launches() - n0
     ms = start.elapsed_time(end) / args.steps
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = replica_max(ms, "cuda")
     info = eng.info()
     phase = (__import__("ctypes").c_double * 9)()
     nst = __import__("ctypes").c_int()
