@@ -441,6 +441,10 @@ class ParticleHandler2D:
         arr["cell"] = cell
         return arr
 
+    def reserve(self, capacity):
+        """Grows the particle buffers to `capacity` particles, keeping the particles."""
+        _check(lib().pf2_particles_reserve(self.h, C.c_longlong(int(capacity))), "pf2_particles_reserve")
+
     def save(self, path):
         """Checkpoint of the particle state (pf2_particles_save)."""
         _check(lib().pf2_particles_save(self.h, str(path).encode()), "pf2_particles_save")

@@ -242,6 +242,20 @@ extern "C" {
 pf2_status pf2_flow_step(pf2_flow* F, void* stream) {
     PF2_REQUIRE(F, PF2_BAD_INPUT, "null flow");
     cudaStream_t st = as_stream(stream);
+    // reseeding only adds particles: once the last step left the buffers three quarters
+    // full, grow them by half (the step graphs hold the old buffers: recapture)
+    if (F->stepped) {
+        PF2_CUDA(cudaEventSynchronize(F->done));
+        const long long np = F->h_np.p[0], cap = particles_capacity(F->ph);
+        if (np > cap - cap / 4) {
+            PF2_TRY(particles_reserve(F->ph, std::max(cap + cap / 2, 2 * np), st));
+            for (auto& gx : F->gexec)
+                if (gx) {
+                    cudaGraphExecDestroy(gx);
+                    gx = nullptr;
+                }
+        }
+    }
     const bool learning = F->guess && F->steps_done < F->P.learn_steps;
     // graphs replay identical work: from the second step on (matrices assembled), and
     // not while phase timing records events

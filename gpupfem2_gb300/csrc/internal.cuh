@@ -34,6 +34,9 @@ const int* particles_count_ptr(const pf2_particles* H);
 // which of the two particle buffers holds the state (the cell sort alternates them)
 int particles_parity(const pf2_particles* H);
 void particles_set_parity(pf2_particles* H, int parity);
+long long particles_capacity(const pf2_particles* H);
+// grows the particle buffers to cap (no-op when already as large), keeping the particles
+pf2_status particles_reserve(pf2_particles* H, long long cap, cudaStream_t st);
 
 // Device-side record of one solve: copies of the solver's result and error word.
 struct SolveRecord {

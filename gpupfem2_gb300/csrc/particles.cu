@@ -501,6 +501,41 @@ pf2_status particles_status(pf2_particles* H, cudaStream_t st) {
 
 const int* particles_count_ptr(const pf2_particles* H) { return H->cnt.p; }
 int particles_parity(const pf2_particles* H) { return H->cur; }
+long long particles_capacity(const pf2_particles* H) { return H->cap; }
+
+// Larger particle buffers with the current particles copied over (the reference
+// reallocates its particle vector when reseeding outgrows it).  The second buffer of
+// the pair, the ranks and the permutation are scratch and are not copied.
+pf2_status particles_reserve(pf2_particles* H, long long cap, cudaStream_t st) {
+    if (cap <= H->cap) return PF2_OK;
+    PF2_REQUIRE(cap <= (long long)INT32_MAX - 1, PF2_OVERFLOW, "particle capacity %lld too large", cap);
+    int n = 0;
+    PF2_CUDA(cudaMemcpyAsync(&n, H->cnt.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaStreamSynchronize(st));
+    DevBuf<double> nb[2][6];
+    DevBuf<int> ncw[2], nrank, nperm;
+    for (int b = 0; b < 2; ++b) {
+        for (int k = 0; k < 6; ++k) PF2_TRY(nb[b][k].alloc(cap));
+        PF2_TRY(ncw[b].alloc(cap));
+    }
+    PF2_TRY(nrank.alloc(cap));
+    PF2_TRY(nperm.alloc(cap));
+    const int c = H->cur;
+    if (n > 0) {
+        for (int k = 0; k < 6; ++k)
+            PF2_CUDA(cudaMemcpyAsync(nb[c][k].p, H->buf[c][k].p, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        PF2_CUDA(cudaMemcpyAsync(ncw[c].p, H->cw[c].p, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    }
+    PF2_CUDA(cudaStreamSynchronize(st));
+    for (int b = 0; b < 2; ++b) {
+        for (int k = 0; k < 6; ++k) H->buf[b][k] = std::move(nb[b][k]);
+        H->cw[b] = std::move(ncw[b]);
+    }
+    H->rank = std::move(nrank);
+    H->perm = std::move(nperm);
+    H->cap = cap;
+    return PF2_OK;
+}
 void particles_set_parity(pf2_particles* H, int parity) { H->cur = parity; }
 
 // Sections: sizes {cells, level, count, seeded}, the SoA arrays and cell words of the
@@ -648,6 +683,12 @@ pf2_status pf2_particles_download(const pf2_particles* Hc, double* x, double* y,
         }
     }
     return PF2_OK;
+}
+
+pf2_status pf2_particles_reserve(pf2_particles* H, long long capacity) {
+    PF2_REQUIRE(H, PF2_BAD_INPUT, "null particles");
+    PF2_CUDA(cudaDeviceSynchronize());
+    return particles_reserve(H, capacity, nullptr);
 }
 
 pf2_status pf2_particles_save(const pf2_particles* Hc, const char* path) {

@@ -417,6 +417,11 @@ pf2_status pf2_particles_upload(pf2_particles* ph, int n, const double* x, const
  * unspecified.  All synchronise.
  * Particles: count, x, y, l0, l1, u, v, the cell words (with the sub-cell marks) and the
  * cell segments of the last sort, so that a restored handler continues exactly. */
+/* Grows the particle buffers to hold `capacity` particles, keeping the particles (the
+ * reference reallocates its particle vector when reseeding outgrows it).  The flow
+ * engine does this by itself before a step when the last step left them three
+ * quarters full. Synchronises. */
+pf2_status pf2_particles_reserve(pf2_particles* ph, long long capacity);
 pf2_status pf2_particles_save(const pf2_particles* ph, const char* path);
 pf2_status pf2_particles_load(pf2_particles* ph, const char* path);
 

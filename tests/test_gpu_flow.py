@@ -182,3 +182,37 @@ def test_solver_options_keep_the_step(cuda, option):
         runs.append({f: eng.field(f) for f in ("ux", "uy", "p")})
     for f in ("ux", "uy", "p"):
         assert rel_err(runs[1][f], runs[0][f]) < FIELD_TOL, f
+
+
+def test_particle_buffers_grow_with_the_flow(cuda):
+    """Reseeding only adds particles; an engine created with room for 1.1x the seeded
+    particles grows its buffers between steps and repeats, bit for bit, the run of an
+    engine created with room to spare."""
+    xy, tri, bu, bv, bp, p, op = _channel_case(level=3)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(4.0, 1.0)
+    out = []
+    for cap in (1.1, 8.0):
+        eng = g.FlowEngine(m, p, bu, bv, bp, capacity_factor=cap)
+        eng.seed()
+        for _ in range(6):
+            eng.step()
+            assert eng.info().status == 0
+        out.append((eng.particles.download(), eng.field("ux"), eng.field("p")))
+    (pa, ua, qa), (pb, ub, qb) = out
+    assert pa["cell"].size > 1.1 * 9 * tri.shape[0] * 0.75  # the small engine did have to grow
+    for k in pa:
+        assert np.array_equal(pa[k], pb[k]), k
+    assert np.array_equal(ua, ub) and np.array_equal(qa, qb)
+
+
+def test_particles_reserve_keeps_the_particles(cuda):
+    xy, tri = mg.channel(32, 8, 4.0, 1.0)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    h = g.ParticleHandler2D(m, 3, capacity_factor=1.1)
+    h.seed()
+    before = h.download()
+    h.reserve(10 * tri.shape[0] * 9)
+    after = h.download()
+    for k in before:
+        assert np.array_equal(before[k], after[k]), k
