@@ -162,13 +162,17 @@ __device__ __forceinline__ void block_sum_n(double (&v)[NV], double* sh) {
 }
 
 // ------------------------------------------------------------ grid barrier
-// Barrier over all blocks of a cooperative launch (all blocks co-resident).  The wait is
-// bounded: after `kBarrierPolls` polls it records DEV_TIMEOUT in *err (and where it gave up
-// in rec) and returns, and callers check the result after every barrier, so no block
-// waits forever.
+// Barrier over all blocks of a cooperative launch (all blocks co-resident).  Arrivals add
+// to one counter that only grows during a launch (zeroed before each launch): barrier k
+// is complete once the counter reaches (k + 1) * gridDim, so a block that arrives with the
+// counter at c waits for (c / gridDim + 1) * gridDim.  Thread 0 arrives with a gpu-scope
+// release after the block's __syncthreads and waits with gpu-scope acquire loads, which
+// orders every thread's writes before the barrier against every thread's reads after it.
+// The wait is bounded: after `kBarrierPolls` polls it records DEV_TIMEOUT in *err (and
+// where it gave up in rec) and returns, and callers check the result after every barrier,
+// so no block waits forever.
 struct GridBarrier {
-    unsigned int* count;  // zero-initialised
-    unsigned int* gen;
+    unsigned int* count;  // zero-initialised before each launch
     int* err;
     double* part;  // 2 x 4 x gridDim per-block partial sums (grid_reduce)
     int* rec;      // where a wait gave up: {kind, a, b, c, d}, kind 0 = none
@@ -188,86 +192,110 @@ __device__ __forceinline__ void record_timeout(int* rec, int kind, int a, int b,
     }
 }
 
-// Thread 0 waits until the barrier generation moves past g.
-__device__ __forceinline__ void wait_generation(const GridBarrier& b, unsigned g) {
-    volatile unsigned int* vgen = b.gen;
-    long long polls = 0;
-    while (*vgen == g) {
-        if (++polls > kBarrierPolls) {
-            atomicExch(b.err, (int)DEV_TIMEOUT);
-            record_timeout(b.rec, 1, (int)blockIdx.x, (int)g, (int)*(volatile unsigned*)b.count, 0);
-            break;
-        }
-        if (*(volatile int*)b.err != 0) break;
-    }
-    __threadfence();
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
 }
 
-// The error word is read once per block (thread 0) so that every thread of a block takes
-// the same branch afterwards.
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void arrive_release_gpu(unsigned* p) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" : : "l"(p) : "memory");
+}
+
+// Thread 0 arrives at barrier k (the counter read before arriving, c0, lies in
+// [k G, (k + 1) G)) and waits for the other blocks.  False on a timeout or an error.
+__device__ __forceinline__ bool arrive_and_wait(const GridBarrier& b, unsigned c0, unsigned nblocks) {
+    const unsigned target = (c0 / nblocks + 1) * nblocks;
+    arrive_release_gpu(b.count);
+    long long polls = 0;
+    unsigned c;
+    while ((int)((c = ld_acquire_gpu(b.count)) - target) < 0) {
+        if (++polls > kBarrierPolls) {
+            atomicExch(b.err, (int)DEV_TIMEOUT);
+            record_timeout(b.rec, 1, (int)blockIdx.x, (int)(c0 / nblocks), (int)c, 0);
+            return false;
+        }
+        if ((polls & 255) == 0 && *(volatile int*)b.err != 0) return false;
+    }
+    return *(volatile int*)b.err == 0;
+}
+
+// The counter is read before the block's __syncthreads, whose wait hides the load: the
+// value is at least k G (this thread saw it reach k G at the last barrier) and below
+// (k + 1) G (barrier k cannot complete before this block arrives).  The error word is
+// read once per block (thread 0) so that every thread of a block takes the same branch
+// afterwards.
 __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks) {
     __shared__ int s_ok;
+    unsigned c0 = 0;
+    if (threadIdx.x == 0) c0 = ld_relaxed_gpu(b.count);
     __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = b.gen;
-        const unsigned int g = *vgen;
-        __threadfence();
-        if (atomicAdd(b.count, 1u) == nblocks - 1) {
-            *b.count = 0;
-            __threadfence();
-            atomicAdd(b.gen, 1u);
-        } else {
-            wait_generation(b, g);
-        }
-        s_ok = *(volatile int*)b.err == 0;
-    }
+    if (threadIdx.x == 0) s_ok = arrive_and_wait(b, c0, nblocks) ? 1 : 0;
     __syncthreads();
     return s_ok != 0;
 }
 
-// Barrier fused with grid-wide sums of NV (<= 4) values.  Each block stores its block
-// sums in one of two partial arrays (chosen by the parity of the barrier generation) and
-// arrives; once released, every block adds all blocks' partials in block order, so all
-// blocks get the same bits whatever the arrival order.  Two arrays suffice: a block can
-// be at most one barrier ahead of the slowest reader of the other array.  On return v
-// holds the totals in every thread.  sh holds at least 33 * NV doubles; part holds
-// 2 x 4 x gridDim doubles.
+// Barrier fused with grid-wide sums of NV (<= 4) values.  The block sums (warp
+// butterflies, then warp 0 over the warp sums) are stored by thread 0 in one of two
+// partial arrays (chosen by the parity of the barrier index) before it arrives; once
+// released, warp 0 of every block adds all blocks' partials in the same fixed order
+// (lane l: partials l, l + 32, ... in increasing order, then a butterfly; lane 0's
+// total), so all blocks get the same bits whatever the arrival order.  Two arrays
+// suffice: a block can be at most one barrier ahead of the slowest reader of the other
+// array.  On return v holds the totals in every thread.  sh holds at least 33 * NV
+// doubles; part holds 2 x 4 x gridDim doubles.
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV], double* sh) {
     __shared__ int s_ok;
-    __shared__ unsigned s_gen;
-    block_sum_n<NV>(v, sh);
     const unsigned G = gridDim.x;
-    if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = b.gen;
-        const unsigned g = *vgen;
-        double* part = b.part + (size_t)(g & 1u) * 4 * G;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    unsigned c0 = 0;
+    if (threadIdx.x == 0) c0 = ld_relaxed_gpu(b.count);
 #pragma unroll
-        for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], v[j]);
-        __threadfence();
-        if (atomicAdd(b.count, 1u) == G - 1) {
-            *b.count = 0;
-            __threadfence();
-            atomicAdd(b.gen, 1u);
-        } else {
-            wait_generation(b, g);
-        }
-        s_gen = g;
-        s_ok = *(volatile int*)b.err == 0;
+    for (int j = 0; j < NV; ++j) v[j] = warp_sum(v[j]);
+    __syncthreads();  // the previous call's readers of sh are done
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) sh[32 * j + w] = v[j];
     }
     __syncthreads();
-    const double* part = b.part + (size_t)(s_gen & 1u) * 4 * G;
-    double t[NV];
+    if (w == 0) {
+        double t[NV];
 #pragma unroll
-    for (int j = 0; j < NV; ++j) t[j] = 0.0;
-    // thread k adds partials k, k + blockDim, ... in increasing order, then a fixed tree
-    for (unsigned k = threadIdx.x; k < G; k += blockDim.x) {
+        for (int j = 0; j < NV; ++j) t[j] = warp_sum(lane < nw ? sh[32 * j + lane] : 0.0);
+        const unsigned k = __shfl_sync(0xffffffffu, c0, 0) / G;
+        double* part = b.part + (size_t)(k & 1u) * 4 * G;
+        int ok = 1;
+        if (lane == 0) {
 #pragma unroll
-        for (int j = 0; j < NV; ++j) t[j] += __ldcg(&part[j * G + k]);
+            for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], t[j]);
+            ok = arrive_and_wait(b, c0, G) ? 1 : 0;
+        }
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        __syncwarp();  // lane 0's acquire orders the other lanes' reads of the partials
+#pragma unroll
+        for (int j = 0; j < NV; ++j) t[j] = 0.0;
+        for (unsigned q = lane; q < G; q += 32) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) t[j] += __ldcg(&part[j * G + q]);
+        }
+#pragma unroll
+        for (int j = 0; j < NV; ++j) t[j] = warp_sum(t[j]);
+        if (lane == 0) {
+#pragma unroll
+            for (int j = 0; j < NV; ++j) sh[32 * NV + j] = t[j];
+            s_ok = ok;
+        }
     }
-    block_sum_n<NV>(t, sh);
+    __syncthreads();
 #pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = t[j];
+    for (int j = 0; j < NV; ++j) v[j] = sh[32 * NV + j];
     return s_ok != 0;
 }
 

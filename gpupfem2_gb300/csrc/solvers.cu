@@ -111,7 +111,7 @@ struct Tri {
     int* done_b;
     unsigned* tickets;     // one counter per (apply, direction)
     int* rec;              // where a wait gave up (GridBarrier::rec)
-    // FP64 CG on B itself (orderings without the banded plan): A's values in B's
+    // CG on B itself (orderings without the banded plan): A's values in B's
     // numbering, the factors as one array on B's pattern (row i: L to the left of the
     // diagonal, the upper factor to the right, 1 / dividing diagonal on it) and x in B's
     // numbering
@@ -119,6 +119,8 @@ struct Tri {
     const double* bval;
     const double* fsym;
     double* xB;
+    const float* bval32;   // mixed precision: FP32 copies of bval and fsym
+    const float* fsym32;
     // B's rows in sweep groups: group g holds rows cstart[g] .. cstart[g + 1] (the colours
     // of a multicolour order, or all rows), swept one group after the other
     int ngroups;
@@ -611,14 +613,16 @@ __device__ bool precond_apply(const KArgs& a, const double* src, double* dst, in
     return true;
 }
 
-// q = A p over the block's rows r0..r1 with this thread's p.q terms: the thread's rows
+// q = A p over the block's rows r0..r1 with this thread's p.q terms (values val, which
+// may be A's or an FP32 copy): the thread's rows
 // (r0 + tid + u * blockDim, u = 0..3) walked together, so the loads of four rows are in
 // flight at once; each row sums its entries in order, as row_dot.
-__device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, double* q, int r0, int r1) {
-    double pq = 0.0;
+template <class V>
+__device__ __forceinline__ V spmv_rows(const Csr& A, const V* __restrict__ val, const V* p, V* q, int r0, int r1) {
+    V pq = V(0);
     for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * blockDim.x) {
         int s[4], e[4];
-        double acc[4] = { 0.0, 0.0, 0.0, 0.0 };
+        V acc[4] = { V(0), V(0), V(0), V(0) };
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int i = i0 + u * blockDim.x;
@@ -631,7 +635,7 @@ __device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, doubl
         for (int k = 0; k < len; ++k) {
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (s[u] + k < e[u]) acc[u] += __ldg(&A.val[s[u] + k]) * __ldcg(&p[__ldg(&A.col[s[u] + k])]);
+                if (s[u] + k < e[u]) acc[u] += __ldg(&val[s[u] + k]) * __ldcg(&p[__ldg(&A.col[s[u] + k])]);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -645,16 +649,21 @@ __device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, doubl
     return pq;
 }
 
+__device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, double* q, int r0, int r1) {
+    return spmv_rows<double>(A, A.val, p, q, r0, r1);
+}
+
 // p = z + beta p over the block's rows, four rows per pass with the loads first (z is
 // written by other blocks' threads in the sweeps: read through L2).
-__device__ __forceinline__ void p_update(double* p, const double* z, double beta, int r0, int r1) {
+template <class V>
+__device__ __forceinline__ void p_update(V* p, const V* z, V beta, int r0, int r1) {
     for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * blockDim.x) {
-        double zv[4], pv[4];
+        V zv[4], pv[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const int i = i0 + u * blockDim.x;
-            zv[u] = i < r1 ? __ldcg(&z[i]) : 0.0;
-            pv[u] = i < r1 ? __ldcg(&p[i]) : 0.0;
+            zv[u] = i < r1 ? __ldcg(&z[i]) : V(0);
+            pv[u] = i < r1 ? __ldcg(&p[i]) : V(0);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -667,20 +676,20 @@ __device__ __forceinline__ void p_update(double* p, const double* z, double beta
 // sum_k f_k x_{col_k} over the CSR entries [k0, k1) of a row whose x entries other
 // threads of the same sweep are still writing: four entries loaded together, only the
 // pending ones polled (bounded); terms added in entry order.
-__device__ __forceinline__ bool csr_dot_wait(const double* x, const int* __restrict__ col,
-                                             const double* __restrict__ f, int k0, int k1, int row, int* err,
-                                             int* rec, double& sum) {
-    sum = 0.0;
+template <class V>
+__device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__ col, const V* __restrict__ f,
+                                             int k0, int k1, int row, int* err, int* rec, V& sum) {
+    sum = V(0);
     for (int k = k0; k < k1; k += 4) {
         int j[4];
-        double v[4];
+        V v[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = j[u] >= 0 ? *(volatile const double*)&x[j[u]] : 0.0;
+        for (int u = 0; u < 4; ++u) v[u] = j[u] >= 0 ? *(volatile const V*)&x[j[u]] : V(0);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-            if (j[u] >= 0 && Pending<double>::bits(v[u]) == Pending<double>::kBits &&
+            if (j[u] >= 0 && Pending<V>::bits(v[u]) == Pending<V>::kBits &&
                 !wait_value(x, j[u], v[u], err, rec, row))
                 return false;
 #pragma unroll
@@ -699,9 +708,21 @@ __device__ __forceinline__ bool csr_dot_wait(const double* x, const int* __restr
 // s = q + beta s, x += alpha p, r -= alpha s (first: p = z, s = q).  Writes the forward
 // result and resets the row of z to the pending marker for the backward sweep.  Returns
 // the thread's r.r terms.
-template <int MODE>
-__device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, double* r, const double* q, double* x,
-                          double* p, double* sv, double* z, int* err) {
+template <class V> struct CsrVecs;
+template <> struct CsrVecs<double> {
+    __device__ static double* tmp(const Tri& T) { return T.tmp; }
+    __device__ static const double* fsym(const Tri& T) { return T.fsym; }
+};
+template <> struct CsrVecs<float> {
+    __device__ static float* tmp(const Tri& T) { return T.tmp32; }
+    __device__ static const float* fsym(const Tri& T) { return T.fsym32; }
+};
+
+template <int MODE, class V = double>
+__device__ double csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, const V* q, V* x, V* p, V* sv, V* z,
+                          int* err) {
+    V* tmp = CsrVecs<V>::tmp(T);
+    const V* fsym = CsrVecs<V>::fsym(T);
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
     const bool unit = T.kind != PF2_PRECOND_IC;  // ILU: L has a unit diagonal
@@ -723,27 +744,27 @@ __device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, d
             k0n = __ldg(&T.B.rowptr[row + stride]);
             dn = __ldg(&T.B.diag[row + stride]);
         }
-        double ra = __ldcg(&r[row]);
+        V ra = __ldcg(&r[row]);
         if (MODE == 1) {
             ra -= alpha * __ldcg(&q[row]);
             __stcg(&r[row], ra);
             __stcg(&x[row], __ldcg(&x[row]) + alpha * __ldcg(&p[row]));
         } else if (MODE == 2) {
-            const double zr = __ldcg(&z[row]), wr = __ldcg(&q[row]);
-            const double pr = first ? zr : zr + beta * __ldcg(&p[row]);
-            const double sr = first ? wr : wr + beta * __ldcg(&sv[row]);
+            const V zr = __ldcg(&z[row]), wr = __ldcg(&q[row]);
+            const V pr = first ? zr : zr + beta * __ldcg(&p[row]);
+            const V sr = first ? wr : wr + beta * __ldcg(&sv[row]);
             __stcg(&p[row], pr);
             __stcg(&sv[row], sr);
             __stcg(&x[row], __ldcg(&x[row]) + alpha * pr);
             ra -= alpha * sr;
             __stcg(&r[row], ra);
         }
-        rr += ra * ra;
-        double sum;
-        if (!csr_dot_wait(T.tmp, T.B.col, T.fsym, k0, d, row, err, T.rec, sum)) break;
-        const double v = unit ? ra - sum : (ra - sum) * __ldg(&T.fsym[d]);
-        __stcg(&T.tmp[row], v);
-        __stcg(&z[row], Pending<double>::marker());
+        rr += (double)ra * (double)ra;
+        V sum;
+        if (!csr_dot_wait(tmp, T.B.col, fsym, k0, d, row, err, T.rec, sum)) break;
+        const V v = unit ? ra - sum : (ra - sum) * __ldg(&fsym[d]);
+        __stcg(&tmp[row], v);
+        __stcg(&z[row], Pending<V>::marker());
     }
     }
     return rr;
@@ -751,7 +772,10 @@ __device__ double csr_fwd(const Tri& T, double alpha, double beta, bool first, d
 
 // Backward sweep (groups and rows in reverse order): z = U^{-1} t, the forward result reset to the
 // marker; with p_init the first direction p = z is stored too.  Returns the r.z terms.
-__device__ double csr_bwd(const Tri& T, const double* r, double* z, double* p_init, int* err) {
+template <class V = double>
+__device__ double csr_bwd(const Tri& T, const V* r, V* z, V* p_init, int* err) {
+    V* tmp = CsrVecs<V>::tmp(T);
+    const V* fsym = CsrVecs<V>::fsym(T);
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
     double rz = 0.0;
@@ -772,14 +796,14 @@ __device__ double csr_bwd(const Tri& T, const double* r, double* z, double* p_in
             dn = __ldg(&T.B.diag[row - stride]);
             k1n = __ldg(&T.B.rowptr[row - stride + 1]);
         }
-        const double in = __ldcg(&T.tmp[row]);
-        double sum;
-        if (!csr_dot_wait(z, T.B.col, T.fsym, d + 1, k1, row, err, T.rec, sum)) break;
-        const double v = (in - sum) * __ldg(&T.fsym[d]);
+        const V in = __ldcg(&tmp[row]);
+        V sum;
+        if (!csr_dot_wait(z, T.B.col, fsym, d + 1, k1, row, err, T.rec, sum)) break;
+        const V v = (in - sum) * __ldg(&fsym[d]);
         __stcg(&z[row], v);
         if (p_init) __stcg(&p_init[row], v);
-        __stcg(&T.tmp[row], Pending<double>::marker());
-        rz += __ldcg(&r[row]) * v;
+        __stcg(&tmp[row], Pending<V>::marker());
+        rz += (double)__ldcg(&r[row]) * (double)v;
     }
     }
     return rz;
@@ -808,10 +832,10 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         red[1] += bi * bi;
     }
     if (!grid_sync(a.bar, gridDim.x)) return;
-    red[2] = csr_fwd<0>(T, 0.0, 0.0, true, a.r, nullptr, nullptr, nullptr, nullptr, a.z, a.bar.err);
+    red[2] = csr_fwd<0, double>(T, 0.0, 0.0, true, a.r, nullptr, nullptr, nullptr, nullptr, a.z, a.bar.err);
     if (!grid_sync(a.bar, gridDim.x)) return;
     const bool one = a.variant == PF2_CG_ONE_REDUCTION;
-    red[0] = csr_bwd(T, a.r, a.z, one ? nullptr : a.p, a.bar.err);
+    red[0] = csr_bwd<double>(T, a.r, a.z, one ? nullptr : a.p, a.bar.err);
     double red4[4] = { red[0], red[1], red[2], 0.0 };
     if (one) {  // w = B z and z.w join the first reduction
         if (!grid_sync(a.bar, gridDim.x)) return;
@@ -838,9 +862,9 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         while (!conv && it < a.maxit) {
             ++it;
             double g3[3] = { 0.0, 0.0, 0.0 };  // r.z, z.w, r.r
-            g3[2] = csr_fwd<2>(T, alpha, beta, first, a.r, a.q, xB, a.p, a.s, a.z, a.bar.err);
+            g3[2] = csr_fwd<2, double>(T, alpha, beta, first, a.r, a.q, xB, a.p, a.s, a.z, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return;
-            g3[0] = csr_bwd(T, a.r, a.z, nullptr, a.bar.err);
+            g3[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return;
             g3[1] = spmv_rows(B, a.z, a.q, r0, r1);
             if (!grid_reduce<3>(a.bar, g3, sh)) return;
@@ -858,9 +882,9 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
-        g2[1] = csr_fwd<1>(T, alpha, 0.0, false, a.r, a.q, xB, a.p, nullptr, a.z, a.bar.err);
+        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, a.p, nullptr, a.z, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return;
-        g2[0] = csr_bwd(T, a.r, a.z, nullptr, a.bar.err);
+        g2[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
         if (!grid_reduce<2>(a.bar, g2, sh)) return;
         const double gnew = g2[0];
         rr = g2[1];
@@ -1428,10 +1452,110 @@ __device__ bool precond_apply32(const KArgs& a, const float* src, float* dst, in
 // the iteration continues from the true residual with its search direction kept, so the
 // Krylov space is not restarted.  On GB300 the FP32 iteration also stays off the small
 // FP64 pipe.  a.inner_eta is the refinement trigger (the drop of the iterated residual).
+// Mixed-precision PCG in B's numbering (the CSR path of pcg_csr with the inner iteration
+// in FP32): the SpMV on an FP32 copy of B's values, the sweeps on an FP32 copy of the
+// factors, FP32 vectors; the update d is folded into x (FP64, B's numbering) and the
+// residual recomputed in FP64 from B's FP64 values whenever the iterated residual fell by
+// the inner factor since the last refinement, as in k_pcg_mixed.
+__device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
+    const Tri& T = a.T;
+    const int n = a.A.n;
+    int r0, r1;
+    row_range(n, r0, r1);
+    const Csr B{ n, T.B.rowptr, T.B.col, T.bval, T.B.diag };
+    double* xB = T.xB;
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        __stcg(&xB[i], a.x[__ldg(&T.perm[i])]);
+        __stcg(&a.d32[i], 0.0f);
+    }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    double red[2] = { 0.0, 0.0 };  // b.b, r.r
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double bi = a.b[__ldg(&T.perm[i])];
+        const double ri = bi - row_dot(B, i, xB);
+        __stcg(&a.r32[i], (float)ri);
+        red[0] += bi * bi;
+        red[1] += ri * ri;
+    }
+    if (!grid_reduce<2>(a.bar, red, sh)) return;
+    const double bnorm = sqrt(red[0]);
+    const double target = a.tol * bnorm;
+    double rnorm = sqrt(red[1]);
+    double rlast = rnorm;
+    int it = 0, refinements = 1;
+    bool conv = rnorm <= target;
+    if (!conv) {
+        // z = M^{-1} r, p = z, gamma = r.z
+        csr_fwd<0, float>(T, 0.0f, 0.0f, true, a.r32, nullptr, nullptr, nullptr, nullptr, a.z32, a.bar.err);
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        double g[1] = { csr_bwd<float>(T, a.r32, a.z32, a.p32, a.bar.err) };
+        if (!grid_reduce<1>(a.bar, g, sh)) return;
+        double gamma = g[0];
+        while (it < a.maxit) {
+            ++it;
+            double pq[1] = { (double)spmv_rows<float>(B, T.bval32, a.p32, a.q32, r0, r1) };
+            if (!grid_reduce<1>(a.bar, pq, sh)) return;
+            const float alpha = (float)(gamma / pq[0]);
+            // d += alpha p, r -= alpha q and the forward sweep; the backward sweep with r.z
+            double g2[2] = { 0.0, 0.0 };
+            g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, a.p32, nullptr, a.z32, a.bar.err);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            g2[0] = csr_bwd<float>(T, a.r32, a.z32, nullptr, a.bar.err);
+            if (!grid_reduce<2>(a.bar, g2, sh)) return;
+            double gnew = g2[0];
+            const double rit = sqrt(g2[1]);
+            if (rit <= a.inner_eta * rlast || rit <= target) {
+                // refinement: x += d, r = b - B x and the convergence test in FP64
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    __stcg(&xB[i], __ldcg(&xB[i]) + (double)__ldcg(&a.d32[i]));
+                    __stcg(&a.d32[i], 0.0f);
+                }
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                double rr[1] = { 0.0 };
+                for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                    const double ri = a.b[__ldg(&T.perm[i])] - row_dot(B, i, xB);
+                    __stcg(&a.r32[i], (float)ri);
+                    rr[0] += ri * ri;
+                }
+                if (!grid_reduce<1>(a.bar, rr, sh)) return;
+                ++refinements;
+                rnorm = sqrt(rr[0]);
+                if (rnorm <= target) { conv = true; break; }
+                rlast = rnorm;
+                // continue from the true residual, keeping the search direction
+                csr_fwd<0, float>(T, 0.0f, 0.0f, true, a.r32, nullptr, nullptr, nullptr, nullptr, a.z32, a.bar.err);
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                double g3[1] = { csr_bwd<float>(T, a.r32, a.z32, nullptr, a.bar.err) };
+                if (!grid_reduce<1>(a.bar, g3, sh)) return;
+                gnew = g3[0];
+            }
+            const float beta = (float)(gnew / gamma);
+            gamma = gnew;
+            p_update<float>(a.p32, a.z32, beta, r0, r1);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+        }
+        if (!conv)  // iteration limit: keep the accumulated update
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
+                __stcg(&xB[i], __ldcg(&xB[i]) + (double)__ldcg(&a.d32[i]));
+    }
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[__ldg(&T.perm[i])] = __ldcg(&xB[i]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+        a.out->pad = refinements;
+    }
+}
+
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixed(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
     __shared__ double sh[kShDoubles];
+    if (a.T.csr) {
+        pcg_csr_mixed(a, sh);
+        return;
+    }
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const bool global_pc = (a.precond == PF2_PRECOND_ILU || a.precond == PF2_PRECOND_IC);
@@ -1612,6 +1736,7 @@ struct pf2_solver {
     // own; IC upper (i, j): l_ji; diagonal: -1 - position, stored as its inverse)
     bool csr = false;
     DevBuf<double> bval, fsym, xB;
+    DevBuf<float> bval32, fsym32;  // mixed precision on the CSR path
     DevBuf<int> tpos;
     int ngroups = 0;
     DevBuf<int> cstart;
@@ -1878,9 +2003,8 @@ static pf2_status build_tri_plan(pf2_solver* S) {
     // slot records (rows with at most kBandMaxDeps dependencies): in (range, step) order for
     // the banded solve, in level order for the sync-free one
     const bool banded = K <= kBandMaxDeps && std::max(S->levels_fwd, S->levels_bwd) >= band_min;
-    // FP64 CG with few levels: the whole iteration on B's CSR arrays (pcg_csr)
-    S->csr = std::max(S->levels_fwd, S->levels_bwd) < band_min && S->opt.kind == PF2_SOLVER_CG &&
-             S->opt.precision == PF2_PRECISION_FP64;
+    // CG with few levels: the whole iteration on B's CSR arrays (pcg_csr, pcg_csr_mixed)
+    S->csr = std::max(S->levels_fwd, S->levels_bwd) < band_min && S->opt.kind == PF2_SOLVER_CG;
     if (const char* e = getenv("PF2_CG_SLOTS")) S->csr = S->csr && atoi(e) == 0;  // tuning: keep the slot sweeps
     if (S->csr) {
         std::vector<int> tpos(std::max(nnz, 1));
@@ -1905,6 +2029,10 @@ static pf2_status build_tri_plan(pf2_solver* S) {
         PF2_TRY(S->bval.alloc(nnz));
         PF2_TRY(S->fsym.alloc(nnz));
         PF2_TRY(S->xB.alloc(n));
+        if (S->opt.precision == PF2_PRECISION_MIXED) {
+            PF2_TRY(S->bval32.alloc(nnz));
+            PF2_TRY(S->fsym32.alloc(nnz));
+        }
     }
     if (K <= kBandMaxDeps) {
         const int R = banded ? std::min(n, band_rows) : n;
@@ -1998,7 +2126,8 @@ static Tri tri_of(pf2_solver* S) {
     return Tri{ S->opt.precond, band, Csr{ S->n, S->brp.p, S->bcol.p, nullptr, S->bdiag.p }, S->perm.p, S->iperm.p,
                 S->fwd_order.p, S->bwd_order.p, S->lt_off.p, S->lt_row.p, S->lt_pos.p, S->fact.p, S->tmp.p,
                 S->outB.p, S->fact32.p, S->tmp32.p, S->outB32.p, S->done_f.p, S->done_b.p, S->tickets.p,
-                S->rec.p, S->csr ? 1 : 0, S->bval.p, S->fsym.p, S->xB.p, S->ngroups, S->cstart.p };
+                S->rec.p, S->csr ? 1 : 0, S->bval.p, S->fsym.p, S->xB.p, S->bval32.p, S->fsym32.p, S->ngroups,
+                S->cstart.p };
 }
 
 static bool uses_tri(const pf2_solver* S) {
@@ -2083,6 +2212,11 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
         k_fsym<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->tpos.p, S->fact.p,
                                                                                     S->fsym.p);
         PF2_LAUNCH_CHECK();
+        if (mixed) {
+            k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fsym.p,
+                                                                                            S->fsym32.p);
+            PF2_LAUNCH_CHECK();
+        }
     }
     if (mixed) {
         k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fact.p,
@@ -2132,7 +2266,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.t = S->tv.p;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
-    a.bar = GridBarrier{ S->bar.p, S->bar.p + 1, S->err.p, S->partial.p, S->rec.p };
+    a.bar = GridBarrier{ S->bar.p, S->err.p, S->partial.p, S->rec.p };
     a.T = tri_of(S);
     a.tol = S->opt.tolerance;
     a.maxit = S->opt.max_iterations;
@@ -2162,6 +2296,11 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
             S->nnz, a.A.val, S->bmap.p, S->bval.p);
         PF2_LAUNCH_CHECK();
+        if (mixed) {
+            k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->bval.p,
+                                                                                            S->bval32.p);
+            PF2_LAUNCH_CHECK();
+        }
     }
     if (uses_tri(S)) {
         PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned) * S->tickets.n, st));
@@ -2353,7 +2492,7 @@ pf2_status pf2_solver_solve(pf2_solver* S, const pf2_csr* A, double* x, const do
     info->outer_iterations = S->opt.precision == PF2_PRECISION_MIXED ? S->h_out.p->pad : 1;
     info->status = err ? err : S->h_out.p->status;
     PF2_REQUIRE(err == 0, (pf2_status)err,
-                rec[0] == 1   ? "grid barrier timed out in the solver (block %d, generation %d, arrived %d)"
+                rec[0] == 1   ? "grid barrier timed out in the solver (block %d, barrier %d, arrivals %d)"
                 : rec[0] == 2 ? "row wait timed out in the solver (row %d waited for row %d, epoch %d, flag %d)"
                               : "device-side wait timed out in the solver",
                 rec[1], rec[2], rec[3], rec[4]);
@@ -2398,7 +2537,7 @@ constexpr int kStaticMaxBlocks = 512;
 // the solve record (4 doubles)
 constexpr size_t kStaticDoubles = 5ull * kStaticMaxRows + 8ull * kStaticMaxBlocks + 4;
 static __device__ __align__(256) double g_static_work[kStaticDoubles];
-// barrier count, barrier generation, error word, timeout record (5): all zeroed per call
+// barrier count, (unused), error word, timeout record (5): all zeroed per call
 static __device__ __align__(256) unsigned g_static_words[8];
 
 struct StaticWork {
@@ -2465,7 +2604,7 @@ extern "C" pf2_status pf2_pcg_jacobi_static(const pf2_csr* A, double* x, const d
     a.invd = base + 4 * (size_t)kStaticMaxRows;
     a.partial = base + 5 * (size_t)kStaticMaxRows;
     int* err = reinterpret_cast<int*>(w.words + 2);
-    a.bar = GridBarrier{ w.words, w.words + 1, err, a.partial, reinterpret_cast<int*>(w.words + 3) };
+    a.bar = GridBarrier{ w.words, err, a.partial, reinterpret_cast<int*>(w.words + 3) };
     a.tol = tolerance;
     a.maxit = max_iterations;
     a.criterion = criterion;

@@ -77,11 +77,12 @@ def test_spmv(cuda):
     assert rel_err(y.cpu().numpy(), O.spmv(rp, col, val, x)) < 1e-14
 
 
-@pytest.mark.parametrize("pc,ordering", [("jacobi", 0), ("ic", 0), ("ilu", 0), ("ic", 1)])
+@pytest.mark.parametrize("pc,ordering", [("jacobi", 0), ("ic", 0), ("ilu", 0), ("ic", 1), ("ilu", 1)])
 def test_mixed_precision_refinement_reaches_fp64_residual(cuda, pc, ordering):
     """FP32 inner CG (FP32 Jacobi or FP32 ILU(0)/IC(0) factors) inside FP64 iterative
     refinement reaches ||b - A x|| <= 1e-8 ||b||, with the residual checked by the
-    oracle's FP64 SpMV."""
+    oracle's FP64 SpMV.  The multicolour order (ordering 1) runs the whole iteration on
+    the permuted system's CSR arrays, the natural order the level-scheduled sweeps."""
     m, A, rp, col, val, rhs = _system(128, 32)
     b = torch.tensor(rhs, device="cuda")
     x = torch.zeros_like(b)
@@ -96,6 +97,39 @@ def test_mixed_precision_refinement_reaches_fp64_residual(cuda, pc, ordering):
     info64 = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL).solve(A, x64, b)
     assert info64.converged == 1
     assert rel_err(xs, x64.cpu().numpy()) < 1e-6
+
+
+def test_mixed_precision_on_the_permuted_csr_arrays_matches_the_slot_sweeps(cuda, monkeypatch):
+    """Mixed-precision IC(0) CG on the multicolour order: the CSR path (whole iteration
+    on B's arrays) and the slot sweeps (PF2_CG_SLOTS=1) reach the same solution, and at
+    the iteration limit both keep the accumulated update."""
+    m, A, rp, col, val, rhs = _system(128, 32)
+    b = torch.tensor(rhs, device="cuda")
+    out = {}
+    for slots in ("0", "1"):
+        monkeypatch.setenv("PF2_CG_SLOTS", slots)
+        x = torch.zeros_like(b)
+        s = g.LinearSolver(A, "cg", "ic", tol=1e-8, maxit=5000, criterion=g.CRITERION_REL,
+                           precision=g.PRECISION_MIXED, ordering=1)
+        info = s.solve(A, x, b)
+        assert info.converged == 1
+        y = torch.zeros_like(b)
+        s5 = g.LinearSolver(A, "cg", "ic", tol=1e-30, maxit=5, criterion=g.CRITERION_REL,
+                            precision=g.PRECISION_MIXED, ordering=1)
+        lim = s5.solve(A, y, b, check=False)
+        assert lim.converged == 0 and lim.iterations == 5
+        ys, xs = y.cpu().numpy(), x.cpu().numpy()
+        # CG lowers the A-norm of the error (not necessarily the residual's 2-norm)
+        e5 = ys - xs
+        assert np.isfinite(ys).all() and e5 @ O.spmv(rp, col, val, e5) < 0.5 * (xs @ O.spmv(rp, col, val, xs))
+        # five FP32 iterations follow five FP64 ones up to FP32 rounding
+        y64 = torch.zeros_like(b)
+        g.LinearSolver(A, "cg", "ic", tol=1e-30, maxit=5, ordering=1).solve(A, y64, b, check=False)
+        assert rel_err(ys, y64.cpu().numpy()) < 1e-4
+        out[slots] = (xs, info.iterations, ys)
+    assert abs(out["0"][1] - out["1"][1]) <= 3
+    assert rel_err(out["0"][0], out["1"][0]) < 1e-6
+    assert rel_err(out["0"][2], out["1"][2]) < 1e-4  # five FP32 iterations, two sweep orders
 
 
 def _greedy_colour_perm(rp, col):
