@@ -570,6 +570,8 @@ struct KArgs {
     // mixed precision
     const float* val32;   // FP32 copy of the matrix values
     float *d32, *r32, *p32, *q32, *z32, *invd32;
+    float* p32b;  // second direction array of the mixed CSR path
+    int fuse_p;   // CSR paths: direction update inside the SpMV (1) or separate (0)
     double inner_eta;     // inner solves stop at ||r_inner|| <= eta ||r_outer||
     int max_outer;
 };
@@ -651,6 +653,52 @@ __device__ __forceinline__ V spmv_rows(const Csr& A, const V* __restrict__ val, 
 
 __device__ __forceinline__ double spmv_rows(const Csr& A, const double* p, double* q, int r0, int r1) {
     return spmv_rows<double>(A, A.val, p, q, r0, r1);
+}
+
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// The direction update fused into the SpMV: q = A pn with pn = z + beta po formed on the
+// fly at every column (po and z are read-only in this phase), and the block's own rows of
+// pn stored; each pn entry is one fma, so the stored pn and the values the SpMV used
+// carry the same bits.  Saves the grid barrier between a separate direction update and
+// the SpMV.  Returns the thread's pn.q terms.
+template <class V>
+__device__ __forceinline__ V spmv_rows_pz(const Csr& A, const V* __restrict__ val, const V* z, const V* po, V beta,
+                                          V* pn, V* q, int r0, int r1) {
+    V pq = V(0);
+    for (int i0 = r0 + threadIdx.x; i0 < r1; i0 += 4 * blockDim.x) {
+        int s[4], e[4];
+        V acc[4] = { V(0), V(0), V(0), V(0) };
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            s[u] = i < r1 ? __ldg(&A.rowptr[i]) : 0;
+            e[u] = i < r1 ? __ldg(&A.rowptr[i + 1]) : 0;
+        }
+        int len = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) len = max(len, e[u] - s[u]);
+        for (int k = 0; k < len; ++k) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (s[u] + k < e[u]) {
+                    const int j = __ldg(&A.col[s[u] + k]);
+                    acc[u] += __ldg(&val[s[u] + k]) * fma_rn(beta, __ldcg(&po[j]), __ldcg(&z[j]));
+                }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i < r1) {
+                const V pi = fma_rn(beta, __ldcg(&po[i]), __ldcg(&z[i]));
+                __stcg(&pn[i], pi);
+                __stcg(&q[i], acc[u]);
+                pq += pi * acc[u];
+            }
+        }
+    }
+    return pq;
 }
 
 // p = z + beta p over the block's rows, four rows per pass with the loads first (z is
@@ -876,23 +924,39 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
             first = false;
         }
     }
+    // with fuse_p three barriers per iteration: the direction update p = z + beta p runs
+    // inside the next SpMV (spmv_rows_pz), alternating p between two arrays; else a
+    // separate update and barrier
+    double* pc = a.p;
+    double* pa = a.s;
+    double beta = 0.0;
     while (!conv && it < a.maxit) {
+        double pq[1];
+        if (it == 0 || !a.fuse_p) {
+            pq[0] = spmv_rows(B, pc, a.q, r0, r1);
+        } else {
+            pq[0] = spmv_rows_pz<double>(B, T.bval, a.z, pc, beta, pa, a.q, r0, r1);
+            double* t = pc;
+            pc = pa;
+            pa = t;
+        }
         ++it;
-        double pq[1] = { spmv_rows(B, a.p, a.q, r0, r1) };
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
-        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, a.p, nullptr, a.z, a.bar.err);
+        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err);
         if (!grid_sync(a.bar, gridDim.x)) return;
         g2[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
         if (!grid_reduce<2>(a.bar, g2, sh)) return;
         const double gnew = g2[0];
         rr = g2[1];
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
-        const double beta = gnew / gamma;
+        beta = gnew / gamma;
         gamma = gnew;
-        p_update(a.p, a.z, beta, r0, r1);
-        if (!grid_sync(a.bar, gridDim.x)) return;
+        if (!a.fuse_p) {
+            p_update(pc, a.z, beta, r0, r1);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+        }
     }
     // every x update happened before the last reduction's barrier
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[__ldg(&T.perm[i])] = __ldcg(&xB[i]);
@@ -1491,14 +1555,27 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
         double g[1] = { csr_bwd<float>(T, a.r32, a.z32, a.p32, a.bar.err) };
         if (!grid_reduce<1>(a.bar, g, sh)) return;
         double gamma = g[0];
+        // the direction update runs inside the next SpMV (spmv_rows_pz), p alternating
+        // between two arrays
+        float* pc = a.p32;
+        float* pa = a.p32b;
+        float beta = 0.0f;
         while (it < a.maxit) {
+            double pq[1];
+            if (it == 0 || !a.fuse_p) {
+                pq[0] = (double)spmv_rows<float>(B, T.bval32, pc, a.q32, r0, r1);
+            } else {
+                pq[0] = (double)spmv_rows_pz<float>(B, T.bval32, a.z32, pc, beta, pa, a.q32, r0, r1);
+                float* t = pc;
+                pc = pa;
+                pa = t;
+            }
             ++it;
-            double pq[1] = { (double)spmv_rows<float>(B, T.bval32, a.p32, a.q32, r0, r1) };
             if (!grid_reduce<1>(a.bar, pq, sh)) return;
             const float alpha = (float)(gamma / pq[0]);
             // d += alpha p, r -= alpha q and the forward sweep; the backward sweep with r.z
             double g2[2] = { 0.0, 0.0 };
-            g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, a.p32, nullptr, a.z32, a.bar.err);
+            g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, pc, nullptr, a.z32, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return;
             g2[0] = csr_bwd<float>(T, a.r32, a.z32, nullptr, a.bar.err);
             if (!grid_reduce<2>(a.bar, g2, sh)) return;
@@ -1529,10 +1606,12 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
                 if (!grid_reduce<1>(a.bar, g3, sh)) return;
                 gnew = g3[0];
             }
-            const float beta = (float)(gnew / gamma);
+            beta = (float)(gnew / gamma);
             gamma = gnew;
-            p_update<float>(a.p32, a.z32, beta, r0, r1);
-            if (!grid_sync(a.bar, gridDim.x)) return;
+            if (!a.fuse_p) {
+                p_update<float>(pc, a.z32, beta, r0, r1);
+                if (!grid_sync(a.bar, gridDim.x)) return;
+            }
         }
         if (!conv)  // iteration limit: keep the accumulated update
             for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x)
@@ -1720,7 +1799,7 @@ struct pf2_solver {
     // ILU / IC
     DevBuf<double> fact, tmp;
     // mixed precision
-    DevBuf<float> val32, d32, r32, p32, q32, z32, invd32;
+    DevBuf<float> val32, d32, r32, p32, q32, z32, invd32, p32b;
     DevBuf<int> fwd_order, bwd_order, lt_off, lt_row, lt_pos, done_f, done_b;
     DevBuf<unsigned> tickets;
     DevBuf<int> epoch;  // device counter of the row flags' epochs (graph replays stay valid)
@@ -2279,6 +2358,10 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.vpart = S->vpart.p;
     a.vtot = S->vpart.p ? S->vpart.p + (size_t)(S->m + 1) * S->blocks : nullptr;
     const bool mixed = S->opt.precision == PF2_PRECISION_MIXED && !precond_only;
+    // CSR paths: the direction update inside the SpMV (saves a barrier, gathers z and p);
+    // PF2_CG_FUSED_P=0/1 overrides the default (tuning)
+    a.fuse_p = mixed ? 1 : 0;
+    if (const char* e = getenv("PF2_CG_FUSED_P")) a.fuse_p = atoi(e) != 0;
     if (mixed) {
         a.val32 = S->val32.p;
         a.d32 = S->d32.p;
@@ -2287,6 +2370,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         a.q32 = S->q32.p;
         a.z32 = S->z32.p;
         a.invd32 = S->invd32.p;
+        a.p32b = S->p32b.p;
         a.inner_eta = kMixedInnerEta;
         if (const char* e = getenv("PF2_MIXED_INNER_ETA")) a.inner_eta = std::max(1e-12, atof(e));  // tuning
         a.max_outer = kMaxOuter;
@@ -2407,7 +2491,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // at least ~512 rows per block keeps the barrier count per unit of work low
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
-        (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_ONE_REDUCTION && (s = S->s.alloc(S->n))) ||
+        (opt->kind == PF2_SOLVER_CG && (s = S->s.alloc(S->n))) ||
         (opt->kind == PF2_SOLVER_BICGSTAB && ((s = S->s.alloc(S->n)) || (s = S->rhat.alloc(S->n)) ||
                                                (s = S->yv.alloc(S->n)) || (s = S->tv.alloc(S->n)))) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
@@ -2415,7 +2499,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
         return fail(s);
     if (mixed && ((s = S->val32.alloc(S->nnz)) || (s = S->d32.alloc(S->n)) || (s = S->r32.alloc(S->n)) ||
                   (s = S->p32.alloc(S->n)) || (s = S->q32.alloc(S->n)) || (s = S->z32.alloc(S->n)) ||
-                  (s = S->invd32.alloc(S->n))))
+                  (s = S->invd32.alloc(S->n)) || (s = S->p32b.alloc(S->n))))
         return fail(s);
     if (opt->kind == PF2_SOLVER_GMRES) {
         int m = opt->restart > 0 ? opt->restart : S->opt.max_iterations;
