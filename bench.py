@@ -282,7 +282,10 @@ def study_learned(args):
     prm = dict(prm, max_iterations=20000)
     # "untrained": the same start with a network that never trains, which isolates what
     # the trained network adds to the projection onto the last increment
+    # "fp64_jacobi": the reference cylinder driver's own pressure solver (Jacobi PCG,
+    # Cylinder2D/main.cu:769-771) on the same steps
     variants = [("fp64_plain", dict(pressure_precision=0, pressure_x0=0)),
+                ("fp64_jacobi", dict(pressure_precision=0, pressure_x0=0, pressure_precond=0)),
                 ("fp64_learned", dict(pressure_precision=0, pressure_x0=1)),
                 ("fp64_untrained", dict(pressure_precision=0, pressure_x0=1, learn_steps=0)),
                 ("mixed", dict(pressure_precision=1, pressure_x0=0)),
@@ -320,9 +323,11 @@ def study_learned(args):
         del eng
         torch.cuda.synchronize()
     base = res["fp64_plain"]["pressure_ms_per_step"]
+    basej = res["fp64_jacobi"]["pressure_ms_per_step"]
     p0, u0 = finals["fp64_plain"]
     for label, v in res.items():
         v["time_vs_fp64_plain"] = v["pressure_ms_per_step"] / base
+        v["time_vs_fp64_jacobi"] = v["pressure_ms_per_step"] / basej
         # fields after the same steps against the plain FP64 run
         v["p_rel_diff_vs_fp64_plain"] = float(np.linalg.norm(finals[label][0] - p0) / np.linalg.norm(p0))
         v["ux_rel_diff_vs_fp64_plain"] = float(np.linalg.norm(finals[label][1] - u0) / np.linalg.norm(u0))

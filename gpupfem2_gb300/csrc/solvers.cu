@@ -755,7 +755,8 @@ __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__
 // x += alpha p, r -= alpha q (q = A p); MODE 2 (one-reduction CG, q = A z) p = z + beta p,
 // s = q + beta s, x += alpha p, r -= alpha s (first: p = z, s = q).  Writes the forward
 // result and resets the row of z to the pending marker for the backward sweep.  Returns
-// the thread's r.r terms.
+// the thread's r.r terms (x) and t.t terms of the forward result t (y): with IC(0),
+// t = L^{-1} r and z = L^{-T} t, so r.z = t.t.
 template <class V> struct CsrVecs;
 template <> struct CsrVecs<double> {
     __device__ static double* tmp(const Tri& T) { return T.tmp; }
@@ -767,14 +768,14 @@ template <> struct CsrVecs<float> {
 };
 
 template <int MODE, class V = double>
-__device__ double csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, const V* q, V* x, V* p, V* sv, V* z,
-                          int* err) {
+__device__ double2 csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, const V* q, V* x, V* p, V* sv, V* z,
+                           int* err) {
     V* tmp = CsrVecs<V>::tmp(T);
     const V* fsym = CsrVecs<V>::fsym(T);
     const int n = T.B.n;
     const int stride = gridDim.x * blockDim.x;
     const bool unit = T.kind != PF2_PRECOND_IC;  // ILU: L has a unit diagonal
-    double rr = 0.0;
+    double rr = 0.0, tt = 0.0;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
     (void)n;
     for (int gi = 0; gi < T.ngroups; ++gi) {
@@ -813,15 +814,17 @@ __device__ double csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, const
         const V v = unit ? ra - sum : (ra - sum) * __ldg(&fsym[d]);
         __stcg(&tmp[row], v);
         __stcg(&z[row], Pending<V>::marker());
+        tt += (double)v * (double)v;
     }
     }
-    return rr;
+    return make_double2(rr, tt);
 }
 
 // Backward sweep (groups and rows in reverse order): z = U^{-1} t, the forward result reset to the
-// marker; with p_init the first direction p = z is stored too.  Returns the r.z terms.
-template <class V = double>
-__device__ double csr_bwd(const Tri& T, const V* r, V* z, V* p_init, int* err) {
+// marker; with p_init the first direction p = z is stored too (PUPD: the direction update
+// p = z + beta p instead, one fma per row).  Returns the r.z terms (none with PUPD).
+template <class V = double, bool PUPD = false>
+__device__ double csr_bwd(const Tri& T, const V* r, V* z, V* p_init, int* err, V beta = V(0)) {
     V* tmp = CsrVecs<V>::tmp(T);
     const V* fsym = CsrVecs<V>::fsym(T);
     const int n = T.B.n;
@@ -849,9 +852,12 @@ __device__ double csr_bwd(const Tri& T, const V* r, V* z, V* p_init, int* err) {
         if (!csr_dot_wait(z, T.B.col, fsym, d + 1, k1, row, err, T.rec, sum)) break;
         const V v = (in - sum) * __ldg(&fsym[d]);
         __stcg(&z[row], v);
-        if (p_init) __stcg(&p_init[row], v);
+        if (PUPD)
+            __stcg(&p_init[row], fma_rn(beta, __ldcg(&p_init[row]), v));
+        else if (p_init)
+            __stcg(&p_init[row], v);
         __stcg(&tmp[row], Pending<V>::marker());
-        rz += (double)__ldcg(&r[row]) * (double)v;
+        if (!PUPD) rz += (double)__ldcg(&r[row]) * (double)v;
     }
     }
     return rz;
@@ -860,9 +866,10 @@ __device__ double csr_bwd(const Tri& T, const V* r, V* z, V* p_init, int* err) {
 // PCG in B's numbering (the ordering's permuted system B = P A P^T, with b and x
 // permuted on the way in and out): the SpMV, the two sweeps and every vector run on
 // B's CSR arrays, so the whole iteration reads one compact set of arrays (A's values on
-// B's pattern, the factors, six vectors) that stays in L2 at a million rows.  Same
-// iteration as below: four barriers (p.q reduction, forward -> backward, r.z reduction,
-// p update).
+// B's pattern, the factors, six vectors) that stays in L2 at a million rows.  ILU(0): the
+// iteration of k_pcg, four barriers (p.q reduction, forward -> backward, r.z reduction,
+// p update).  IC(0): three (p.q reduction, r.z = t.t and r.r reduction after the forward
+// sweep, the backward sweep with the direction update).
 __device__ void pcg_csr(const KArgs& a, double* sh) {
     const Tri& T = a.T;
     const int n = a.A.n;
@@ -880,7 +887,7 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         red[1] += bi * bi;
     }
     if (!grid_sync(a.bar, gridDim.x)) return;
-    red[2] = csr_fwd<0, double>(T, 0.0, 0.0, true, a.r, nullptr, nullptr, nullptr, nullptr, a.z, a.bar.err);
+    red[2] = csr_fwd<0, double>(T, 0.0, 0.0, true, a.r, nullptr, nullptr, nullptr, nullptr, a.z, a.bar.err).x;
     if (!grid_sync(a.bar, gridDim.x)) return;
     const bool one = a.variant == PF2_CG_ONE_REDUCTION;
     red[0] = csr_bwd<double>(T, a.r, a.z, one ? nullptr : a.p, a.bar.err);
@@ -910,7 +917,7 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         while (!conv && it < a.maxit) {
             ++it;
             double g3[3] = { 0.0, 0.0, 0.0 };  // r.z, z.w, r.r
-            g3[2] = csr_fwd<2, double>(T, alpha, beta, first, a.r, a.q, xB, a.p, a.s, a.z, a.bar.err);
+            g3[2] = csr_fwd<2, double>(T, alpha, beta, first, a.r, a.q, xB, a.p, a.s, a.z, a.bar.err).x;
             if (!grid_sync(a.bar, gridDim.x)) return;
             g3[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
             if (!grid_sync(a.bar, gridDim.x)) return;
@@ -930,6 +937,7 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
     double* pc = a.p;
     double* pa = a.s;
     double beta = 0.0;
+    const bool ic = T.kind == PF2_PRECOND_IC;
     while (!conv && it < a.maxit) {
         double pq[1];
         if (it == 0 || !a.fuse_p) {
@@ -944,7 +952,22 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         if (!grid_reduce<1>(a.bar, pq, sh)) return;
         const double alpha = gamma / pq[0];
         double g2[2] = { 0.0, 0.0 };
-        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err);
+        if (ic && !a.fuse_p) {
+            // IC(0): r.z = |L^{-1} r|^2 is known after the forward sweep, so one reduction
+            // of r.z and r.r follows it and the backward sweep carries the direction update
+            // (three barriers per iteration)
+            const double2 f = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err);
+            double gt[2] = { f.y, f.x };
+            if (!grid_reduce<2>(a.bar, gt, sh)) return;
+            rr = gt[1];
+            if (done_test(gt[0], rr)) { gamma = gt[0]; conv = true; break; }
+            beta = gt[0] / gamma;
+            gamma = gt[0];
+            csr_bwd<double, true>(T, nullptr, a.z, pc, a.bar.err, beta);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            continue;
+        }
+        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err).x;
         if (!grid_sync(a.bar, gridDim.x)) return;
         g2[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
         if (!grid_reduce<2>(a.bar, g2, sh)) return;
@@ -1575,7 +1598,7 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
             const float alpha = (float)(gamma / pq[0]);
             // d += alpha p, r -= alpha q and the forward sweep; the backward sweep with r.z
             double g2[2] = { 0.0, 0.0 };
-            g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, pc, nullptr, a.z32, a.bar.err);
+            g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, pc, nullptr, a.z32, a.bar.err).x;
             if (!grid_sync(a.bar, gridDim.x)) return;
             g2[0] = csr_bwd<float>(T, a.r32, a.z32, nullptr, a.bar.err);
             if (!grid_reduce<2>(a.bar, g2, sh)) return;
