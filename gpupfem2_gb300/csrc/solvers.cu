@@ -1578,11 +1578,13 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
         double g[1] = { csr_bwd<float>(T, a.r32, a.z32, a.p32, a.bar.err) };
         if (!grid_reduce<1>(a.bar, g, sh)) return;
         double gamma = g[0];
-        // the direction update runs inside the next SpMV (spmv_rows_pz), p alternating
-        // between two arrays
+        // IC(0): three barriers per iteration with r.z = t.t (below); ILU(0) (fuse_p): the
+        // direction update inside the next SpMV (spmv_rows_pz), p alternating between two
+        // arrays
         float* pc = a.p32;
         float* pa = a.p32b;
         float beta = 0.0f;
+        const bool ic = T.kind == PF2_PRECOND_IC;
         while (it < a.maxit) {
             double pq[1];
             if (it == 0 || !a.fuse_p) {
@@ -1596,6 +1598,46 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
             ++it;
             if (!grid_reduce<1>(a.bar, pq, sh)) return;
             const float alpha = (float)(gamma / pq[0]);
+            if (ic && !a.fuse_p) {
+                // IC(0) in three barriers (as pcg_csr): r.z = t.t after the forward sweep,
+                // the backward sweep with the direction update
+                const double2 f =
+                    csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, pc, nullptr, a.z32, a.bar.err);
+                double gt[2] = { f.y, f.x };
+                if (!grid_reduce<2>(a.bar, gt, sh)) return;
+                double gnew = gt[0];
+                const double rit = sqrt(gt[1]);
+                if (rit <= a.inner_eta * rlast || rit <= target) {
+                    // refinement; the forward results are reset to the marker for the
+                    // forward sweep on the new residual
+                    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                        __stcg(&xB[i], __ldcg(&xB[i]) + (double)__ldcg(&a.d32[i]));
+                        __stcg(&a.d32[i], 0.0f);
+                        __stcg(&T.tmp32[i], Pending<float>::marker());
+                    }
+                    if (!grid_sync(a.bar, gridDim.x)) return;
+                    double rr[1] = { 0.0 };
+                    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                        const double ri = a.b[__ldg(&T.perm[i])] - row_dot(B, i, xB);
+                        __stcg(&a.r32[i], (float)ri);
+                        rr[0] += ri * ri;
+                    }
+                    if (!grid_reduce<1>(a.bar, rr, sh)) return;
+                    ++refinements;
+                    rnorm = sqrt(rr[0]);
+                    if (rnorm <= target) { conv = true; break; }
+                    rlast = rnorm;
+                    double g3[1] = { csr_fwd<0, float>(T, 0.0f, 0.0f, true, a.r32, nullptr, nullptr, nullptr, nullptr,
+                                                       a.z32, a.bar.err).y };
+                    if (!grid_reduce<1>(a.bar, g3, sh)) return;
+                    gnew = g3[0];
+                }
+                beta = (float)(gnew / gamma);
+                gamma = gnew;
+                csr_bwd<float, true>(T, nullptr, a.z32, pc, a.bar.err, beta);
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                continue;
+            }
             // d += alpha p, r -= alpha q and the forward sweep; the backward sweep with r.z
             double g2[2] = { 0.0, 0.0 };
             g2[1] = csr_fwd<1, float>(T, alpha, 0.0f, false, a.r32, a.q32, a.d32, pc, nullptr, a.z32, a.bar.err).x;
@@ -2383,7 +2425,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     const bool mixed = S->opt.precision == PF2_PRECISION_MIXED && !precond_only;
     // CSR paths: the direction update inside the SpMV (saves a barrier, gathers z and p);
     // PF2_CG_FUSED_P=0/1 overrides the default (tuning)
-    a.fuse_p = mixed ? 1 : 0;
+    a.fuse_p = mixed && S->opt.precond != PF2_PRECOND_IC ? 1 : 0;
     if (const char* e = getenv("PF2_CG_FUSED_P")) a.fuse_p = atoi(e) != 0;
     if (mixed) {
         a.val32 = S->val32.p;
