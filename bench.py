@@ -238,9 +238,10 @@ def study_solver(args):
                  ("fp64_jacobi_one_reduction", dict(precond="jacobi", cg_variant=g.CG_ONE_REDUCTION)),
                  ("fp64_ic0_multicolour_one_reduction", dict(precond="ic", ordering=1, cg_variant=g.CG_ONE_REDUCTION)),
                  ("mixed_jacobi", dict(precond="jacobi", precision=g.PRECISION_MIXED)),
-                 ("mixed_ic0_multicolour", dict(precond="ic", ordering=1, precision=g.PRECISION_MIXED))]
-        if args.quick:  # FP64 and mixed, standard CG
-            cases = [cases[i] for i in (0, 1, 4, 5)]
+                 ("mixed_ic0_multicolour", dict(precond="ic", ordering=1, precision=g.PRECISION_MIXED)),
+                 ("fp64_ic0_multicolour_pipelined", dict(precond="ic", ordering=1, cg_variant=g.CG_PIPELINED))]
+        if args.quick:  # FP64 and mixed, standard and pipelined CG
+            cases = [cases[i] for i in (0, 1, 4, 5, 6)]
         for label, kw in cases:
             s = g.LinearSolver(A, "cg", tol=1e-8, maxit=20000, criterion=g.CRITERION_REL, **kw)
             times, info, x0 = [], None, None
@@ -346,7 +347,8 @@ def main():
     ap.add_argument("--precond", type=int, default=None, help="pressure preconditioner override (0 J, 1 ILU, 2 IC)")
     ap.add_argument("--ordering", type=int, default=None, help="ILU/IC ordering override (0 natural, 1 multicolour)")
     ap.add_argument("--gs", type=int, default=None, help="GMRES Gram-Schmidt override (0 modified, 1 classical twice)")
-    ap.add_argument("--cg", type=int, default=None, help="CG variant override (0 standard, 1 one reduction)")
+    ap.add_argument("--cg", type=int, default=None,
+                    help="CG variant override (0 standard, 1 one reduction, 2 pipelined)")
     ap.add_argument("--pred", type=int, default=None, help="prediction solver override (1 GMRES, 2 BiCGStab)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -493,7 +495,7 @@ def main():
                    "particles": int(np_), "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
                    "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
                    "gmres_gram_schmidt": ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)],
-                   "cg_variant": ["standard", "one_reduction"][prm.get("cg_variant", 0)],
+                   "cg_variant": ["standard", "one_reduction", "pipelined"][prm.get("cg_variant", 0)],
                    "prediction_solver": {1: "gmres", 2: "bicgstab"}[prm.get("prediction_solver", 1)],
                    "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
                    "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),

@@ -28,7 +28,7 @@ CRITERION_ABS, CRITERION_REL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 RHS_GAUSSIAN, RHS_SINSIN = 0, 1
 RHS3D_GAUSSIAN, RHS3D_SINSINSIN = 0, 1
-CG_STANDARD, CG_ONE_REDUCTION = 0, 1
+CG_STANDARD, CG_ONE_REDUCTION, CG_PIPELINED = 0, 1, 2
 FIELDS = {"ux": 0, "uy": 1, "ux_old": 2, "uy_old": 3, "pred_x": 4, "pred_y": 5, "p": 6, "p_old": 7}
 MESH_FIELDS = {"xy": 0, "tri": 1, "area": 2, "inv_jacobi": 3, "neighbor_offsets": 4, "neighbor_indices": 5,
                "edge_ids": 6}

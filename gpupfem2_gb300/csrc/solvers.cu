@@ -572,6 +572,7 @@ struct KArgs {
     float *d32, *r32, *p32, *q32, *z32, *invd32;
     float* p32b;  // second direction array of the mixed CSR path
     int fuse_p;   // CSR paths: direction update inside the SpMV (1) or separate (0)
+    double* pipe;  // pipelined CG: u, w, z and three m arrays (6 n)
     double inner_eta;     // inner solves stop at ||r_inner|| <= eta ||r_outer||
     int max_outer;
 };
@@ -1159,6 +1160,194 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(mm);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+// Pipelined PCG (Ghysels and Vanroose, "Hiding global synchronization latency in the
+// preconditioned Conjugate Gradient algorithm", Parallel Computing 40 (2014), Algorithm 4)
+// on B's CSR arrays, with ILU(0)/IC(0) on a few-level order: one grid-wide step per
+// iteration.  The recurrences carry u = M^{-1} r, w = A u, m = M^{-1} w, n = A m and
+// z, q, s, p beside x and r; in exact arithmetic the iterates equal PCG's.  Iteration i:
+//  (1) rows in sweep order (group by group, thread t taking rows t, t + T, ...): with the
+//      previous iteration's alpha, beta, n = (B m_{i-1})_row and the row's updates
+//      z = n + beta z, q = m + beta q, s = w + beta s, p = u + beta p, x += alpha p,
+//      r -= alpha s, u -= alpha q, w -= alpha z; the row's terms of r.u, w.u and r.r; then
+//      the forward sweep on w over the same rows (the same thread handles a row in both
+//      passes, so no barrier);
+//  (2) the backward sweep into m_i, each row waiting for its own forward result (the value
+//      is its flag) and its upper neighbours' m;
+//  (3) one barrier fused with the reduction of r.u, w.u, r.r, which gives alpha, beta.
+// m cycles through three arrays: m_i is written in (2), read by (1) of iteration i + 1,
+// and the array for m_{i+1} is reset to the marker in (1) of iteration i, a barrier
+// before its first write.  The forward results are reset by the backward sweep.
+template <int kPipeW>  // rows of the update pass whose SpMV loads are in flight together
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_pipe(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    const Tri& T = a.T;
+    const int n = a.A.n;
+    int r0, r1;
+    row_range(n, r0, r1);
+    const Csr B{ n, T.B.rowptr, T.B.col, T.bval, T.B.diag };
+    double* xB = T.xB;
+    double* tmp = T.tmp;
+    const double* fsym = T.fsym;
+    double *r = a.r, *p = a.p, *q = a.q, *s = a.s;
+    double* u = a.pipe;
+    double* w = u + n;
+    double* zv = w + n;
+    double* m3 = zv + n;  // three arrays of n
+    const bool unit = T.kind != PF2_PRECOND_IC;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    int* err = a.bar.err;
+    const double mk = Pending<double>::marker();
+    // x and b in B's numbering, r = b - B x; z, q, s, p = 0; m_0 pending
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        __stcg(&xB[i], a.x[__ldg(&T.perm[i])]);
+        __stcg(&zv[i], 0.0);
+        __stcg(&q[i], 0.0);
+        __stcg(&s[i], 0.0);
+        __stcg(&p[i], 0.0);
+        __stcg(&m3[i], mk);
+    }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    double bb[1] = { 0.0 };
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+        const double bi = a.b[__ldg(&T.perm[i])];
+        __stcg(&r[i], bi - row_dot(B, i, xB));
+        bb[0] += bi * bi;
+    }
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    // u = M^{-1} r, w = B u
+    csr_fwd<0, double>(T, 0.0, 0.0, true, r, nullptr, nullptr, nullptr, nullptr, u, err);
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    csr_bwd<double>(T, r, u, nullptr, err);
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    spmv_rows(B, u, w, r0, r1);
+    if (!grid_reduce<1>(a.bar, bb, sh)) return;
+    const double bnorm = sqrt(bb[0]);
+    const double tol2 = a.tol * a.tol;
+    const int stride = gridDim.x * blockDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double alpha = 0.0, beta = 0.0, gamma = 0.0, gamma_old = 0.0, alpha_old = 0.0, rr = 0.0;
+    int it = 0;
+    bool conv = false;
+    for (int i = 0;; ++i) {
+        const double* mprev = m3 + (size_t)((i + 2) % 3) * n;  // m_{i-1}
+        double* mcur = m3 + (size_t)(i % 3) * n;                // m_i
+        double* mnext = m3 + (size_t)((i + 1) % 3) * n;         // reset for m_{i+1}
+        double g[3] = { 0.0, 0.0, 0.0 };                        // r.u, w.u, r.r
+        // (1) updates, rows in sweep order (no waits), then the forward sweep on w over the
+        // same rows of the same thread, so the sweep's dependency chain carries no SpMV.
+        // The update pass takes the thread's rows of kPipeW groups together (row j of
+        // each), so the loads of kPipeW SpMV rows are in flight at once.
+        for (int gb = 0; gb < T.ngroups; gb += kPipeW) {
+            int lo[kPipeW], hi[kPipeW];
+#pragma unroll
+            for (int v = 0; v < kPipeW; ++v) {
+                lo[v] = gb + v < T.ngroups ? __ldg(&T.cstart[gb + v]) : 0;
+                hi[v] = gb + v < T.ngroups ? __ldg(&T.cstart[gb + v + 1]) : 0;
+            }
+            for (int j = tid;; j += stride) {
+                int rw[kPipeW], ks[kPipeW], ke[kPipeW];
+                bool any = false;
+#pragma unroll
+                for (int v = 0; v < kPipeW; ++v) {
+                    rw[v] = lo[v] + j < hi[v] ? lo[v] + j : -1;
+                    any = any || rw[v] >= 0;
+                }
+                if (!any) break;
+                double nsum[kPipeW] = {};
+                if (i > 0) {
+                    int len = 0;
+#pragma unroll
+                    for (int v = 0; v < kPipeW; ++v) {
+                        ks[v] = rw[v] >= 0 ? __ldg(&B.rowptr[rw[v]]) : 0;
+                        ke[v] = rw[v] >= 0 ? __ldg(&B.rowptr[rw[v] + 1]) : 0;
+                        len = max(len, ke[v] - ks[v]);
+                    }
+                    for (int k = 0; k < len; ++k) {
+#pragma unroll
+                        for (int v = 0; v < kPipeW; ++v)
+                            if (ks[v] + k < ke[v])
+                                nsum[v] += __ldg(&B.val[ks[v] + k]) * __ldcg(&mprev[__ldg(&B.col[ks[v] + k])]);
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < kPipeW; ++v) {
+                    const int row = rw[v];
+                    if (row < 0) continue;
+                    double ri = __ldcg(&r[row]), ui = __ldcg(&u[row]), wi = __ldcg(&w[row]);
+                    if (i > 0) {
+                        const double zi = nsum[v] + beta * __ldcg(&zv[row]);
+                        const double qi = __ldcg(&mprev[row]) + beta * __ldcg(&q[row]);
+                        const double si = wi + beta * __ldcg(&s[row]);
+                        const double pi = ui + beta * __ldcg(&p[row]);
+                        __stcg(&zv[row], zi);
+                        __stcg(&q[row], qi);
+                        __stcg(&s[row], si);
+                        __stcg(&p[row], pi);
+                        __stcg(&xB[row], __ldcg(&xB[row]) + alpha * pi);
+                        ri -= alpha * si;
+                        ui -= alpha * qi;
+                        wi -= alpha * zi;
+                        __stcg(&r[row], ri);
+                        __stcg(&u[row], ui);
+                        __stcg(&w[row], wi);
+                    }
+                    g[0] += ri * ui;
+                    g[1] += wi * ui;
+                    g[2] += ri * ri;
+                    __stcg(&mnext[row], mk);
+                }
+            }
+        }
+        for (int gi = 0; gi < T.ngroups; ++gi) {
+            const int g0 = __ldg(&T.cstart[gi]), g1 = __ldg(&T.cstart[gi + 1]);
+            for (int row = g0 + tid; row < g1; row += stride) {
+                const int k0 = __ldg(&B.rowptr[row]), d = __ldg(&B.diag[row]);
+                const double wi = __ldcg(&w[row]);
+                double sum;
+                if (!csr_dot_wait(tmp, B.col, fsym, k0, d, row, err, T.rec, sum)) break;
+                __stcg(&tmp[row], unit ? wi - sum : (wi - sum) * __ldg(&fsym[d]));
+            }
+        }
+        // (2) backward sweep into m_i
+        for (int gi = T.ngroups - 1; gi >= 0; --gi) {
+            const int g0 = __ldg(&T.cstart[gi]), g1 = __ldg(&T.cstart[gi + 1]);
+            for (int row = g1 - 1 - tid; row >= g0; row -= stride) {
+                const int d = __ldg(&B.diag[row]), k1 = __ldg(&B.rowptr[row + 1]);
+                double in;
+                if (!wait_value(tmp, row, in, err, T.rec, row)) break;
+                double sum;
+                if (!csr_dot_wait(mcur, B.col, fsym, d + 1, k1, row, err, T.rec, sum)) break;
+                __stcg(&mcur[row], (in - sum) * __ldg(&fsym[d]));
+                __stcg(&tmp[row], mk);
+            }
+        }
+        // (3) the one grid-wide step
+        if (!grid_reduce<3>(a.bar, g, sh)) return;
+        gamma = g[0];
+        rr = g[2];
+        it = i;
+        if (rel ? (sqrt(rr) <= a.tol * bnorm) : (gamma < tol2)) { conv = true; break; }
+        if (i >= a.maxit) break;
+        if (i == 0) {
+            beta = 0.0;
+            alpha = gamma / g[1];
+        } else {
+            beta = gamma / gamma_old;
+            alpha = gamma / (g[1] - beta * gamma / alpha_old);
+        }
+        gamma_old = gamma;
+        alpha_old = alpha;
+    }
+    // every x update happened before the last barrier
+    for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[__ldg(&T.perm[i])] = __ldcg(&xB[i]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1881,6 +2070,7 @@ struct pf2_solver {
     bool csr = false;
     DevBuf<double> bval, fsym, xB;
     DevBuf<float> bval32, fsym32;  // mixed precision on the CSR path
+    DevBuf<double> pipe;           // pipelined CG: u, w, z, three m arrays
     DevBuf<int> tpos;
     int ngroups = 0;
     DevBuf<int> cstart;
@@ -2392,6 +2582,14 @@ static void* solve_kernel(const pf2_solver_options& o) {
     return (void*)k_pcg;
 }
 
+// The pipelined CG kernel: PF2_PIPE_W=1/2/4 picks the rows its update pass walks together
+// (tuning; 2 measured fastest at 1M rows)
+static void* pipe_kernel() {
+    int w = 2;
+    if (const char* e = getenv("PF2_PIPE_W")) w = atoi(e);
+    return w >= 4 ? (void*)k_pcg_pipe<4> : w == 2 ? (void*)k_pcg_pipe<2> : (void*)k_pcg_pipe<1>;
+}
+
 static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, const double* b, cudaStream_t st,
                                 bool precond_only = false) {
     KArgs a{};
@@ -2404,6 +2602,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.p = S->p.p;
     a.q = S->q.p;
     a.s = S->s.p;
+    a.pipe = S->pipe.p;
     a.variant = S->opt.cg_variant;
     a.rhat = S->rhat.p;
     a.y = S->yv.p;
@@ -2475,6 +2674,10 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         return PF2_OK;
     }
     void* fn = mixed ? (void*)k_pcg_mixed : solve_kernel(S->opt);
+    // pipelined CG on B's CSR arrays (ILU(0)/IC(0) on a few-level order); the standard
+    // iteration elsewhere
+    if (!mixed && S->opt.kind == PF2_SOLVER_CG && S->opt.cg_variant == PF2_CG_PIPELINED && S->csr)
+        fn = pipe_kernel();
     PF2_COOP_LAUNCH(fn, dim3(S->blocks), dim3(kSolverThreads), args, S->smem, st);
     if (uses_tri(S)) {
         k_epoch_advance<<<1, 1, 0, st>>>(S->epoch.p, 2 * applies + 2);
@@ -2515,7 +2718,9 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
                 "unknown ordering %d", opt->ordering);
     PF2_REQUIRE(opt->orthogonalization == PF2_GS_MODIFIED || opt->orthogonalization == PF2_GS_CLASSICAL_TWICE,
                 PF2_BAD_INPUT, "unknown orthogonalization %d", opt->orthogonalization);
-    PF2_REQUIRE(opt->cg_variant == PF2_CG_STANDARD || opt->cg_variant == PF2_CG_ONE_REDUCTION, PF2_BAD_INPUT,
+    PF2_REQUIRE(opt->cg_variant == PF2_CG_STANDARD || opt->cg_variant == PF2_CG_ONE_REDUCTION ||
+                    opt->cg_variant == PF2_CG_PIPELINED,
+                PF2_BAD_INPUT,
                 "unknown CG variant %d", opt->cg_variant);
     PF2_REQUIRE(opt->precision == PF2_PRECISION_FP64 || (opt->precision == PF2_PRECISION_MIXED && opt->kind == PF2_SOLVER_CG),
                 PF2_BAD_INPUT, "unknown precision %d for this solver", opt->precision);
@@ -2552,11 +2757,20 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // PF2_SOLVER_BLOCKS_PER_SM overrides the default of kSolverBlocksPerSm (tuning)
     int bps = kSolverBlocksPerSm;
     if (const char* e = getenv("PF2_SOLVER_BLOCKS_PER_SM")) bps = std::max(1, atoi(e));
+    if (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_PIPELINED) {
+        int occ_pp = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_pp, pipe_kernel(), kSolverThreads, S->smem) !=
+                cudaSuccess ||
+            occ_pp < 1)
+            return fail(cuda_fail(cudaGetLastError(), "occupancy query", __FILE__, __LINE__));
+        occ = std::min(occ, occ_pp);
+    }
     const int maxb = std::min(std::min(occ, occ_pc), bps) * num_sms();
     // at least ~512 rows per block keeps the barrier count per unit of work low
     S->blocks = std::max(1, std::min(maxb, (int)((S->n + 511) / 512)));
     if ((s = S->r.alloc(S->n)) || (s = S->z.alloc(S->n)) || (s = S->p.alloc(S->n)) || (s = S->q.alloc(S->n)) ||
         (opt->kind == PF2_SOLVER_CG && (s = S->s.alloc(S->n))) ||
+        (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_PIPELINED && (s = S->pipe.alloc(6 * S->n))) ||
         (opt->kind == PF2_SOLVER_BICGSTAB && ((s = S->s.alloc(S->n)) || (s = S->rhat.alloc(S->n)) ||
                                                (s = S->yv.alloc(S->n)) || (s = S->tv.alloc(S->n)))) ||
         (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||

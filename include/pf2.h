@@ -284,9 +284,13 @@ enum { PF2_GS_MODIFIED = 0,           /* GMRES Gram-Schmidt as the reference (li
        PF2_GS_CLASSICAL_TWICE = 1 };  /* classical Gram-Schmidt with one reorthogonalisation */
 enum { PF2_CG_STANDARD = 0,           /* PCG as the reference (linear_solver.cu:301-376): two
                                          grid-wide reductions per iteration */
-       PF2_CG_ONE_REDUCTION = 1 };    /* Chronopoulos-Gear PCG: the same iterates in exact
+       PF2_CG_ONE_REDUCTION = 1,      /* Chronopoulos-Gear PCG: the same iterates in exact
                                          arithmetic with r.z, (A z).z and r.r in one reduction;
                                          FP64 with Jacobi/none, or ILU(0)/IC(0) on few-level
+                                         orderings (else the standard iteration runs) */
+       PF2_CG_PIPELINED = 2 };        /* pipelined PCG (Ghysels-Vanroose 2014): the same
+                                         iterates in exact arithmetic with one grid-wide step
+                                         per iteration; FP64 ILU(0)/IC(0) on few-level
                                          orderings (else the standard iteration runs) */
 
 typedef struct pf2_solver_options {

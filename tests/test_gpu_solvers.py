@@ -258,6 +258,50 @@ def test_one_reduction_cg_matches_standard(cuda, pc, ordering, criterion):
     assert rel_err(res[1][0], ox) < 1e-6
 
 
+@pytest.mark.parametrize("pc", ["ic", "ilu"])
+@pytest.mark.parametrize("criterion", [g.CRITERION_ABS, g.CRITERION_REL])
+def test_pipelined_cg_matches_standard(cuda, pc, criterion):
+    """Pipelined PCG (one grid-wide step per iteration, ILU(0)/IC(0) on the multicolour
+    order, B's CSR arrays): the standard iteration's solution within the solve tolerance
+    in the same number of iterations up to rounding at the stopping test."""
+    m, A, rp, col, val, rhs = _system(128, 32)
+    b = torch.tensor(rhs, device="cuda")
+    res = {}
+    for variant in (g.CG_STANDARD, g.CG_PIPELINED):
+        x = torch.zeros_like(b)
+        s = g.LinearSolver(A, "cg", pc, tol=1e-8, maxit=3000, criterion=criterion, ordering=1, cg_variant=variant)
+        info = s.solve(A, x, b)
+        assert info.converged == 1 and info.status == 0
+        res[variant] = (x.cpu().numpy(), info.iterations)
+    assert abs(res[0][1] - res[2][1]) <= 3
+    assert rel_err(res[2][0], res[0][0]) < 1e-6
+    if criterion == g.CRITERION_REL:
+        r = rhs - O.spmv(rp, col, val, res[2][0])
+        assert np.linalg.norm(r) <= 1e-8 * np.linalg.norm(rhs) * 1.01
+
+
+def test_pipelined_cg_at_the_limit_and_off_the_csr_path(cuda, monkeypatch):
+    m, A, rp, col, val, rhs = _system()
+    b = torch.tensor(rhs, device="cuda")
+    # seven iterations of each: the same Krylov iterate up to rounding
+    xs = {}
+    for variant in (g.CG_STANDARD, g.CG_PIPELINED):
+        x = torch.zeros_like(b)
+        info = g.LinearSolver(A, "cg", "ic", tol=1e-30, maxit=7, ordering=1, cg_variant=variant).solve(
+            A, x, b, check=False)
+        assert info.converged == 0 and info.iterations == 7
+        xs[variant] = x.cpu().numpy()
+    assert rel_err(xs[2], xs[0]) < 1e-9
+    # slot sweeps (PF2_CG_SLOTS=1, not B's CSR arrays): the standard iteration runs, bit for bit
+    monkeypatch.setenv("PF2_CG_SLOTS", "1")
+    out = []
+    for variant in (g.CG_STANDARD, g.CG_PIPELINED):
+        x = torch.zeros_like(b)
+        g.LinearSolver(A, "cg", "ic", tol=1e-8, maxit=2000, ordering=1, cg_variant=variant).solve(A, x, b)
+        out.append(x.cpu().numpy())
+    assert np.array_equal(out[0], out[1])
+
+
 def test_one_reduction_cg_stops_at_the_limit(cuda):
     m, A, rp, col, val, rhs = _system()
     b = torch.tensor(rhs, device="cuda")
