@@ -204,8 +204,8 @@ def _timed(fn):
 def study_solver(args):
     """Pressure solve to a 1e-8 relative residual on the flow's own pressure matrix after
     --record steps of the cylinder case, on the 994,240-triangle mesh and its 1:4
-    refinement (3,976,960 triangles): FP64 PCG (standard and one-reduction) and the
-    mixed-precision refinement, with Jacobi and IC(0) on the multicolour order.  b = A x* with x* uniform in
+    refinement (3,976,960 triangles): FP64 PCG (standard, one-reduction and pipelined)
+    and the mixed-precision refinement, with Jacobi and IC(0) on the multicolour order.  b = A x* with x* uniform in
     [-1, 1] (splitmix64 seed 0), x0 = 0; median of 3 solves after one warm-up."""
     import torch
     import gpupfem2_gb300 as g
