@@ -178,13 +178,18 @@ def cpu_baseline(name, precond, max_seconds=25.0):
 
 def run_reference(args):
     name, precond = args.workload, args.precond
+    wp = WORKLOADS[name]["params"]
     base = cpu_baseline(name, precond, max_seconds=20.0)
     line = {"metric": "ms per PFEM-2 step", "value": base["value"], "unit": "ms/step", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"], "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name, "pressure_precond": PRECOND_NAMES[WORKLOADS[name]["params"]
-                                                                            ["pressure_precond"]
-                                                                            if precond is None else precond]},
+            "config": {"workload": name,
+                       "pressure_precond": PRECOND_NAMES[wp["pressure_precond"] if precond is None else precond],
+                       # the oracle follows the reference's algorithms: natural-order ILU/IC
+                       # sweeps and GMRES with modified Gram-Schmidt for the prediction
+                       "pressure_ordering": "natural", "prediction_solver": "gmres",
+                       "gmres_gram_schmidt": "modified", "scheme": "AB"[wp["scheme"]], "level": wp["level"],
+                       "n_outer": wp["n_outer"]},
             "impl": "reference", "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
