@@ -16,9 +16,10 @@ namespace {
 constexpr char kMagic[8] = { 'P', 'F', '2', 'C', 'K', 'P', 'T', '\0' };
 constexpr uint32_t kVersion = 1;
 
+// a section tag: up to 8 characters, NUL-padded (not NUL-terminated at 8)
 void tag8(const char* tag, char out[8]) {
     memset(out, 0, 8);
-    strncpy(out, tag, 8);
+    for (int i = 0; i < 8 && tag[i]; ++i) out[i] = tag[i];
 }
 }  // namespace
 

@@ -1097,7 +1097,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
     double rho_old = 1.0, alpha = 1.0, omega = 1.0;
     double rho = red[0], rr = red[1], mm = red[2];
     int it = 0;
-    bool conv = done_test(rr, mm), broke = false;
+    bool conv = done_test(rr, mm);
     while (!conv && it < a.maxit) {
         ++it;
         const double beta = (rho / rho_old) * (alpha / omega);
@@ -1116,7 +1116,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             rv[0] += a.rhat[i] * vi;
         }
         if (!grid_reduce<1>(a.bar, rv, sh)) return;
-        if (rv[0] == 0.0) { broke = true; break; }
+        if (rv[0] == 0.0) break;  // breakdown: ends unconverged
         alpha = rho / rv[0];
         // s = r - alpha v; z = M^{-1} s
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -1134,7 +1134,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             ts[1] += ti * ti;
         }
         if (!grid_reduce<2>(a.bar, ts, sh)) return;
-        if (ts[1] == 0.0) { broke = true; break; }
+        if (ts[1] == 0.0) break;
         omega = ts[0] / ts[1];
         // x += alpha y + omega z; r = s - omega t; rhat.r, r.r, |M^{-1} r|^2
         double g3[3] = { 0.0, 0.0, 0.0 };
@@ -1153,9 +1153,8 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
         rr = g3[1];
         mm = g3[2];
         conv = done_test(rr, mm);
-        if (!conv && (rho == 0.0 || omega == 0.0)) { broke = true; break; }
+        if (!conv && (rho == 0.0 || omega == 0.0)) break;
     }
-    (void)broke;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
