@@ -25,6 +25,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -356,6 +357,7 @@ def main():
                     help="CG variant override (0 standard, 1 one reduction, 2 pipelined)")
     ap.add_argument("--pred", type=int, default=None, help="prediction solver override (1 GMRES, 2 BiCGStab)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--clock-log", default=None, help="where the nvidia-smi clock samples go (default: a temp file)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--study", default=None, choices=["solver", "learned"])
     ap.add_argument("--quick", action="store_true")
@@ -400,8 +402,7 @@ def main():
     # ---- timed region: K steps, device time with CUDA events on the launching stream
     g._check(L.pf2_flow_enable_timing(eng.h, args.steps), "enable timing")
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks = ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
-                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pf2_clocks.csv")
+    clocks = ClockSampler(args.clock_log or os.path.join(tempfile.gettempdir(), "pf2_clocks_%d.csv" % os.getpid()))
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()

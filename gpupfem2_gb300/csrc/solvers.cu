@@ -1066,8 +1066,8 @@ __device__ void pcg_one_reduction(const KArgs& a, double* sh) {
 // preconditioner, on the block's rows: per iteration two SpMVs, two barriers and three
 // fused reductions.  Stops on ||M^{-1} r|| < tol (absolute: the preconditioned residual
 // that the reference's GMRES tests, linear_solver.cu:500-505) or ||r|| <= tol ||b||
-// (relative); a zero (rhat, v) or t.t ends the solve unconverged.  x changes every
-// iteration (x += alpha y + omega z).
+// (relative); a zero (rhat, v) ends the solve unconverged, and so does t.t = 0 unless
+// the half step x += alpha y converged.  x changes every iteration (x += alpha y + omega z).
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab(KArgs a) {
     __shared__ double sh[kShDoubles];
     int r0, r1;
@@ -1134,8 +1134,10 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             ts[1] += ti * ti;
         }
         if (!grid_reduce<2>(a.bar, ts, sh)) return;
-        if (ts[1] == 0.0) break;
-        omega = ts[0] / ts[1];
+        // t = A M^{-1} s is zero only where s is: the half step alpha y already solves
+        // the system, so take it (omega = 0: x += alpha y, r = s) and let the test below
+        // decide; a nonzero s that A M^{-1} maps to zero ends the solve unconverged
+        omega = ts[1] == 0.0 ? 0.0 : ts[0] / ts[1];
         // x += alpha y + omega z; r = s - omega t; rhat.r, r.r, |M^{-1} r|^2
         double g3[3] = { 0.0, 0.0, 0.0 };
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -2972,20 +2974,27 @@ extern "C" pf2_status pf2_pcg_jacobi_static(const pf2_csr* A, double* x, const d
     a.criterion = criterion;
     a.out = reinterpret_cast<SolveOut*>(base + 5 * (size_t)kStaticMaxRows + 8 * (size_t)kStaticMaxBlocks);
     PF2_CUDA(cudaMemsetAsync(w.words, 0, 8 * sizeof(unsigned), st));
+    // the solve record of the previous call must not stand in for this one's: a kernel
+    // that gives up on a wait returns before writing it
+    PF2_CUDA(cudaMemsetAsync(a.out, 0, sizeof(SolveOut), st));
     void* args[] = { &a };
     PF2_COOP_LAUNCH((void*)k_pcg, dim3(blocks), dim3(kSolverThreads), args, 0, st);
     if (!info) return PF2_OK;
     SolveOut o{};
-    int e = 0;
+    int e = 0, rec[5] = { 0, 0, 0, 0, 0 };
     PF2_CUDA(cudaMemcpyAsync(&o, a.out, sizeof(SolveOut), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PF2_CUDA(cudaMemcpyAsync(rec, w.words + 3, sizeof(rec), cudaMemcpyDeviceToHost, st));
     PF2_CUDA(cudaStreamSynchronize(st));
     info->iterations = o.iterations;
     info->converged = o.converged;
     info->residual = o.residual;
     info->outer_iterations = 1;
     info->status = e ? e : o.status;
-    PF2_REQUIRE(e == 0, (pf2_status)e, "device-side wait timed out in the solver");
+    PF2_REQUIRE(e == 0, (pf2_status)e,
+                rec[0] == 1 ? "grid barrier timed out in the solver (block %d, barrier %d, arrivals %d)"
+                            : "device-side wait timed out in the solver",
+                rec[1], rec[2], rec[3]);
     if (!info->converged) {
         set_error("solver did not converge in %d iterations (residual %g)", info->iterations, info->residual);
         return PF2_NOT_CONVERGED;

@@ -2,9 +2,9 @@
 // (andreyypopov/gpuPfem2, src/), implemented over the C ABI of pf2.h.
 //
 // A case driver written against the reference (cases/*/main.cu) compiles against these
-// classes with the changes listed in INTEGRATION.md: velocity fields are passed as two
-// device pointers instead of a device array of pointers, and assembly goes through the
-// pf2_assemble_* entry points instead of the driver's own kernels.  Failures throw
+// classes with two changes: velocity fields are passed as two device pointers instead of
+// a device array of pointers, and assembly goes through the pf2_assemble_* entry points
+// instead of the driver's own kernels.  Failures throw
 // gpupfem2::Error (the reference calls exit()); solver non-convergence returns false as
 // in the reference.
 #pragma once

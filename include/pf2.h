@@ -367,7 +367,11 @@ pf2_status pf2_export_particles_vtu(const pf2_particles* ph, const char* path);
  * - The storage is one per device: two calls whose work overlaps on one device (other
  *   streams, other host threads) race on it and give undefined results; order them.
  * - The first call on a device looks up the array's address (cudaGetSymbolAddress) and
- *   caches it; make that first call before any stream capture.
+ *   caches it; make that first call before any stream capture.  The cached address
+ *   belongs to the device's current primary context: after cudaDeviceReset on that
+ *   device it is stale, so do not call this function again in that process.
+ * - The solve record in the array is cleared before each launch, so a device-side
+ *   timeout reports no iterations rather than the previous call's.
  * info may be NULL (no synchronisation); otherwise the call synchronises `stream` and
  * fills it, returning PF2_NOT_CONVERGED when max_iterations is reached. */
 enum { PF2_STATIC_MAX_ROWS = 131072 };

@@ -12,7 +12,7 @@
 #  3. ref_poisson3d.cubin (Mesh3D and Poisson3D kernels) with ref_kernels3d.names.
 # Needs the reference tree and nvcc (x86-64 or aarch64 host).
 set -euo pipefail
-REF=${REF:-/root/reference/src}
+REF=${REF:-${PF2_REFERENCE_DIR:-/root/reference}/src}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT=$HERE/_ref
 [ -d "$REF" ] || { echo "reference sources not found at $REF" >&2; exit 1; }

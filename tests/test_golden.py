@@ -20,7 +20,7 @@ GENERATED = {
     "channel64x16": lambda: mg.channel(64, 16, 4.0, 1.0),
     "cylinder_nx100": lambda: mg.cylinder_channel(nxh=100, nyh=100, nr=6),
 }
-SHIPPED_DIR = "/root/reference/cases"
+SHIPPED_DIR = os.path.join(os.environ.get("PF2_REFERENCE_DIR", "/root/reference"), "cases")
 SHIPPED = {"TestProblem2.dat": "Poisson2D", "ChannelMesh.dat": "PoiseuilleFlow2D",
            "CylinderMesh.dat": "Cylinder2D", "CylinderMesh3.dat": "Cylinder2D"}
 

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 FIX = json.load(open(os.path.join(HERE, "golden", "reference_host.json")))
 GENERATED = {"box8x4x2": lambda: mg.box_tets(8, 4, 2), "box40x20x10": lambda: mg.box_tets()}
 SHIPPED = {"BoxMesh.dat": "Poisson3D", "BoxMesh2.dat": "Poisson3D"}
-SHIPPED_DIR = "/root/reference/cases"
+SHIPPED_DIR = os.path.join(os.environ.get("PF2_REFERENCE_DIR", "/root/reference"), "cases")
 
 
 def digest(a):

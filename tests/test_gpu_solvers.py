@@ -365,3 +365,26 @@ def test_bicgstab_stops_at_the_limit_and_rejects_triangular_preconditioners(cuda
     with pytest.raises(g.Pf2Error) as e:
         g.LinearSolver(A, "bicgstab", "ilu")
     assert e.value.status == g.BAD_INPUT
+
+
+def test_bicgstab_half_step_solution_is_converged(cuda):
+    """A diagonal system with power-of-two entries and the Jacobi preconditioner: the
+    first half step (alpha = 1) solves it exactly, so s = 0 and t = A M^{-1} s = 0.  That is
+    convergence, not a breakdown: x = b / d exactly, reported converged in one iteration."""
+    xy, tri = mg.channel(8, 4, 4.0, 1.0)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    A = g.SparseMatrixCSR(m)
+    rp, col, _ = A.download()
+    n = rp.size - 1
+    d = 2.0 ** np.arange(-3, 5)[np.arange(n) % 8]
+    val = np.zeros(col.size)
+    for i in range(n):
+        val[rp[i] + np.searchsorted(col[rp[i]:rp[i + 1]], i)] = d[i]
+    A.upload_values(val)
+    rhs = mg.uniform_pm1(7, n)
+    for criterion in (g.CRITERION_ABS, g.CRITERION_REL):
+        b = torch.tensor(rhs, device="cuda")
+        x = torch.zeros_like(b)
+        info = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-10, maxit=50, criterion=criterion).solve(A, x, b)
+        assert info.converged == 1 and info.status == 0 and info.iterations == 1
+        assert np.array_equal(x.cpu().numpy(), rhs / d)
