@@ -51,7 +51,8 @@ class Params(C.Structure):
                 ("pressure_precision", C.c_int), ("pressure_x0", C.c_int), ("gmres_restart", C.c_int),
                 ("pressure_criterion", C.c_int), ("learn_steps", C.c_int), ("learn_rate", C.c_float),
                 ("pressure_ordering", C.c_int), ("gmres_orthogonalization", C.c_int), ("cg_variant", C.c_int),
-                ("prediction_solver", C.c_int)]
+                ("prediction_solver", C.c_int), ("pressure_tolerance", C.c_double),
+                ("pressure_max_iterations", C.c_int)]
 
 
 class MeshView(C.Structure):
@@ -80,7 +81,7 @@ class StepInfo(C.Structure):
     _fields_ = [("particles", C.c_int), ("it_prediction", (C.c_int * 8) * 2), ("it_pressure", C.c_int * 8),
                 ("it_correction", (C.c_int * 8) * 2), ("converged", C.c_int), ("status", C.c_int),
                 ("cx", C.c_double), ("cy", C.c_double), ("guess_used", C.c_int),
-                ("guess_residual", C.c_double * 2)]
+                ("guess_residual", C.c_double * 2), ("pressure_residual", C.c_double * 8)]
 
 
 def lib():

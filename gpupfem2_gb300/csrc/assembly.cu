@@ -507,6 +507,8 @@ pf2_status pf2_params_default(pf2_params* p) {
     p->pressure_x0 = PF2_X0_GIVEN;
     p->gmres_restart = 0;
     p->pressure_criterion = PF2_CRITERION_ABS;
+    p->pressure_tolerance = 0.0;
+    p->pressure_max_iterations = 0;
     p->learn_steps = 500;
     p->learn_rate = 1e-3f;
     p->pressure_ordering = PF2_ORDERING_NATURAL;

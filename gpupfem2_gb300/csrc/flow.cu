@@ -136,8 +136,12 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.precond = p->pressure_precond;
     o.precision = p->pressure_precision;
     o.criterion = p->pressure_criterion;
+    if (p->pressure_tolerance > 0) o.tolerance = p->pressure_tolerance;
+    if (p->pressure_max_iterations > 0) o.max_iterations = p->pressure_max_iterations;
     o.ordering = p->pressure_ordering;
     if ((s = pf2_solver_create(F->A[2], &o, &F->cg_p))) return fail(s);
+    o.tolerance = p->tolerance;
+    o.max_iterations = p->max_iterations;
     o.precision = PF2_PRECISION_FP64;
     o.criterion = PF2_CRITERION_ABS;
     o.ordering = PF2_ORDERING_NATURAL;
@@ -434,6 +438,7 @@ pf2_status pf2_flow_step_info(pf2_flow* F, pf2_step_info* info) {
         info->it_prediction[0][it] = r[0].iterations;
         info->it_prediction[1][it] = r[1].iterations;
         info->it_pressure[it] = r[2].iterations;
+        info->pressure_residual[it] = r[2].relres;
         info->it_correction[0][it] = r[3].iterations;
         info->it_correction[1][it] = r[4].iterations;
         for (int k = 0; k < 5; ++k) {

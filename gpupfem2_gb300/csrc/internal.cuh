@@ -45,6 +45,7 @@ struct SolveRecord {
     double residual;
     int status;
     int err;
+    double relres;  // ||r|| / ||b|| at the end of the solve (CG and BiCGStab)
 };
 // refactor = false reuses the preconditioner of the previous solve (same matrix values)
 pf2_status solver_solve_async(pf2_solver* s, const pf2_csr* A, double* x, const double* b, SolveRecord* rec,

@@ -541,6 +541,7 @@ struct SolveOut {
     double residual;
     int status;
     int pad;
+    double relres;  // ||r|| / ||b|| at the end (the iterated residual; the true one for MIXED)
 };
 
 struct KArgs {
@@ -988,6 +989,7 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1058,6 +1060,7 @@ __device__ void pcg_one_reduction(const KArgs& a, double* sh) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1067,7 +1070,8 @@ __device__ void pcg_one_reduction(const KArgs& a, double* sh) {
 // fused reductions.  Stops on ||M^{-1} r|| < tol (absolute: the preconditioned residual
 // that the reference's GMRES tests, linear_solver.cu:500-505) or ||r|| <= tol ||b||
 // (relative); a zero (rhat, v) ends the solve unconverged, and so does t.t = 0 unless
-// the half step x += alpha y converged.  x changes every iteration (x += alpha y + omega z).
+// the half step x += alpha y converged; a zero rhat.r with r != 0 restarts the shadow
+// residual.  x changes every iteration (x += alpha y + omega z).
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab(KArgs a) {
     __shared__ double sh[kShDoubles];
     int r0, r1;
@@ -1155,12 +1159,28 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
         rr = g3[1];
         mm = g3[2];
         conv = done_test(rr, mm);
-        if (!conv && (rho == 0.0 || omega == 0.0)) break;
+        if (!conv && omega == 0.0) break;
+        if (!conv && rho == 0.0) {
+            // r orthogonal to rhat: with rhat = r0 supported on the Dirichlet rows alone
+            // (the first step of a flow from rest), the first iteration zeroes r there.
+            // Restart the shadow residual: rhat = r, p = v = 0 (each thread its own rows,
+            // which it alone reads next)
+            for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+                a.rhat[i] = a.r[i];
+                a.p[i] = 0.0;
+                a.q[i] = 0.0;
+            }
+            rho = rr;
+            rho_old = 1.0;
+            alpha = 1.0;
+            omega = 1.0;
+        }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(mm);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1349,6 +1369,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_pipe
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1470,6 +1491,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1674,6 +1696,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_gmres(KA
         a.out->iterations = total_it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = res;
+        a.out->relres = 0.0;  // GMRES tracks the preconditioned residual only
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
     }
 }
@@ -1877,6 +1900,7 @@ __device__ void pcg_csr_mixed(const KArgs& a, double* sh) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->relres = rnorm / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
         a.out->pad = refinements;
     }
@@ -2013,6 +2037,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_mixe
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
         a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->relres = rnorm / (bnorm > 0 ? bnorm : 1.0);
         a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
         a.out->pad = refinements;
     }
@@ -2818,6 +2843,7 @@ __global__ void k_record(const SolveOut* out, const int* err, SolveRecord* rec) 
     rec->iterations = out->iterations;
     rec->converged = out->converged;
     rec->residual = out->residual;
+    rec->relres = out->relres;
     rec->status = out->status;
     rec->err = *err;
 }

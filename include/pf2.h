@@ -228,6 +228,9 @@ typedef struct pf2_params {
     int gmres_orthogonalization; /* PF2_GS_* of the prediction GMRES */
     int cg_variant;          /* PF2_CG_* of the pressure and correction CG solves */
     int prediction_solver;   /* PF2_SOLVER_GMRES (the reference's) or PF2_SOLVER_BICGSTAB */
+    double pressure_tolerance;   /* tolerance of the pressure solve; 0 = tolerance (the reference
+                                    has one tolerance for every solve) */
+    int pressure_max_iterations; /* iteration limit of the pressure solve; 0 = max_iterations */
 } pf2_params;
 /* SimulationParameters::setDefaultParameters(), parameters.cuh:30-50 */
 pf2_status pf2_params_default(pf2_params* p);
@@ -481,6 +484,8 @@ typedef struct pf2_step_info {
     double cx, cy;       /* loads, when calculate_loads */
     int guess_used;      /* PF2_X0_LEARNED: 1 if the network's increment got a nonzero coefficient */
     double guess_residual[2]; /* ||b - A p|| of the previous pressure and ||b - A x0|| of the start */
+    double pressure_residual[8]; /* ||r|| / ||b|| at the end of each pressure solve (the CG's
+                                    iterated residual; the true residual for PF2_PRECISION_MIXED) */
 } pf2_step_info;
 /* Statistics of the last completed step. Synchronises. */
 pf2_status pf2_flow_step_info(pf2_flow* f, pf2_step_info* info);

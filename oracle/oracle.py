@@ -30,7 +30,9 @@ class Params(C.Structure):
                 ("thickness", C.c_double), ("mean_velocity", C.c_double),
                 ("lx", C.c_double), ("ly", C.c_double),
                 ("has_cylinder", C.c_int),
-                ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double)]
+                ("cx", C.c_double), ("cy", C.c_double), ("radius", C.c_double),
+                ("pressure_ordering", C.c_int), ("prediction_solver", C.c_int), ("gmres_orth", C.c_int),
+                ("pressure_criterion", C.c_int), ("pressure_tol", C.c_double), ("pressure_maxit", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -40,7 +42,7 @@ class SolveInfo(C.Structure):
 class StepInfo(C.Structure):
     _fields_ = [("particles", C.c_int), ("deleted", C.c_int), ("added", C.c_int),
                 ("it_pred", (C.c_int * 8) * 2), ("it_pres", C.c_int * 8), ("it_corr", (C.c_int * 8) * 2),
-                ("conv_ok", C.c_int), ("cx", C.c_double), ("cy", C.c_double)]
+                ("conv_ok", C.c_int), ("cx", C.c_double), ("cy", C.c_double), ("res_pres", C.c_double * 8)]
 
 
 PRECOND = {"none": -1, "jacobi": 0, "ilu": 1, "ic": 2}
@@ -112,6 +114,18 @@ def _declare(L):
     L.or_flow_csr_nnz.argtypes = [vp]
     L.or_flow_csr_nnz.restype = C.c_int
     L.or_flow_get_matrix.argtypes = [vp, C.c_int, _dp, _dp]
+    L.or_multicolour_order.argtypes = [C.c_int, _ip, _ip, C.c_int, _ip, vp]
+    L.or_multicolour_order.restype = C.c_int
+    L.or_cg.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int,
+                        C.POINTER(SolveInfo), C.POINTER(C.c_double)]
+    L.or_cg.restype = C.c_int
+    L.or_bicgstab.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int, C.c_int,
+                              C.POINTER(SolveInfo)]
+    L.or_bicgstab.restype = C.c_int
+    L.or_gmres_cgs2.argtypes = [C.c_int, _ip, _ip, _dp, _dp, _dp, C.c_double, C.c_int, C.c_int,
+                                C.POINTER(SolveInfo)]
+    L.or_gmres_cgs2.restype = C.c_int
+    L.or_flow_set_solvers.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.or_mesh3d_geometry.argtypes = [C.c_int, _dp, _ip, _dp, _dp]
     L.or_mesh3d_neighbors.argtypes = [C.c_int, _ip, _ip, vp]
     L.or_mesh3d_neighbors.restype = C.c_int
@@ -260,6 +274,45 @@ def gmres(rowptr, col, val, b, x0=None, tol=1e-8, maxit=1000, precond="jacobi"):
     return x, info
 
 
+def multicolour_order(rowptr, col, kempe=True):
+    """(perm, colour starts): the multicolour order of the engine's ILU(0)/IC(0) option."""
+    n = rowptr.size - 1
+    perm = np.empty(n, I)
+    starts = np.empty(n + 2, I)
+    nc = lib().or_multicolour_order(n, _c(rowptr, I), _c(col, I), int(kempe), perm, starts.ctypes.data_as(C.c_void_p))
+    return perm, starts[:nc + 1].copy()
+
+
+def cg(rowptr, col, val, b, x0=None, tol=1e-8, maxit=1000, precond="jacobi", ordering=0, criterion=0):
+    """CG with the engine's options: ordering 1 = multicolour ILU/IC, criterion 1 = relative.
+    Returns (x, info, final ||r|| / ||b||)."""
+    n = rowptr.size - 1
+    x = np.zeros(n, D) if x0 is None else _c(x0, D).copy()
+    info = SolveInfo()
+    rel = C.c_double()
+    lib().or_cg(n, _c(rowptr, I), _c(col, I), _c(val, D), x, _c(b, D), tol, maxit, PRECOND[precond], ordering,
+                criterion, C.byref(info), C.byref(rel))
+    return x, info, rel.value
+
+
+def bicgstab(rowptr, col, val, b, x0=None, tol=1e-8, maxit=1000, precond="jacobi", criterion=0):
+    n = rowptr.size - 1
+    x = np.zeros(n, D) if x0 is None else _c(x0, D).copy()
+    info = SolveInfo()
+    lib().or_bicgstab(n, _c(rowptr, I), _c(col, I), _c(val, D), x, _c(b, D), tol, maxit, PRECOND[precond],
+                      criterion, C.byref(info))
+    return x, info
+
+
+def gmres_cgs2(rowptr, col, val, b, x0=None, tol=1e-8, maxit=1000, precond="jacobi"):
+    n = rowptr.size - 1
+    x = np.zeros(n, D) if x0 is None else _c(x0, D).copy()
+    info = SolveInfo()
+    lib().or_gmres_cgs2(n, _c(rowptr, I), _c(col, I), _c(val, D), x, _c(b, D), tol, maxit, PRECOND[precond],
+                        C.byref(info))
+    return x, info
+
+
 def ilu0(rowptr, col, val):
     f = _c(val, D).copy()
     lib().or_ilu0(rowptr.size - 1, _c(rowptr, I), _c(col, I), f)
@@ -337,7 +390,8 @@ def make_params(**kw):
     p = Params()
     defaults = dict(rho=1.0, mu=1.0, dt=0.01, tol=1e-8, maxit=1000, scheme=0, substeps=3, level=2, n_outer=2,
                     pressure_precond=0, calc_loads=0, body_id=-1, thickness=1.0, mean_velocity=1.0,
-                    lx=1.0, ly=1.0, has_cylinder=0, cx=0.2, cy=0.2, radius=0.05)
+                    lx=1.0, ly=1.0, has_cylinder=0, cx=0.2, cy=0.2, radius=0.05, pressure_ordering=0,
+                    prediction_solver=1, gmres_orth=0, pressure_criterion=0, pressure_tol=0.0, pressure_maxit=0)
     defaults.update(kw)
     for k, v in defaults.items():
         setattr(p, k, v)
@@ -375,6 +429,12 @@ class Flow:
         if rc != 0:
             raise RuntimeError("oracle step failed (particle capacity)")
         return info
+
+    def set_solvers(self, pressure_precond, pressure_ordering=0, prediction_solver=1, gmres_orth=0,
+                    pressure_criterion=0):
+        """The solver choices of the following steps; the state is kept."""
+        lib().or_flow_set_solvers(self.h, pressure_precond, pressure_ordering, prediction_solver, gmres_orth,
+                                  pressure_criterion)
 
     def field(self, name):
         out = np.empty(self.nv, D)

@@ -431,10 +431,24 @@ static void precond_free(or_precond* P)
     free(P->tmp);
 }
 
+/* Dot product summed over fixed 4,096-entry chunks in chunk order: the bits do not
+ * depend on the number of threads. */
 static double dotv(int n, const double* a, const double* b)
 {
+    enum { CH = 4096 };
+    const int nch = (n + CH - 1) / CH;
+    double stack[256];
+    double* part = nch <= 256 ? stack : (double*)malloc(sizeof(double) * nch);
+#pragma omp parallel for schedule(static) if (n > 32768)
+    for (int c = 0; c < nch; ++c) {
+        const int i1 = (c + 1) * CH < n ? (c + 1) * CH : n;
+        double s = 0.0;
+        for (int i = c * CH; i < i1; ++i) s += a[i] * b[i];
+        part[c] = s;
+    }
     double s = 0.0;
-    for (int i = 0; i < n; ++i) s += a[i] * b[i];
+    for (int c = 0; c < nch; ++c) s += part[c];
+    if (part != stack) free(part);
     return s;
 }
 
@@ -524,7 +538,10 @@ int or_gmres(int n, const int* rowptr, const int* col, const double* val, double
             double* h = H + (size_t)maxit * (it - 1);
             for (int i = 0; i < it; ++i) {
                 h[i] = dotv(n, vkp, V[i]);
-                for (int q = 0; q < n; ++q) vkp[q] -= h[i] * V[i][q];
+                const double hi = h[i];
+                const double* vi = V[i];
+#pragma omp parallel for schedule(static) if (n > 32768)
+                for (int q = 0; q < n; ++q) vkp[q] -= hi * vi[q];
             }
             double aux = sqrt(dotv(n, vkp, vkp));
             for (int q = 0; q < n; ++q) vkp[q] = vkp[q] / aux;
@@ -1186,16 +1203,33 @@ int or_flow_step(or_flow* f, or_step_info* info)
             or_prediction_bc(f->nc, f->tri, f->area, f->invJ, P, pr, pold, f->nbc[k], f->bc_node[k], f->bc_val[k],
                              f->node_to_bc[k], k, f->pred_bc_val[k]);
             or_apply_bcs(nv, f->rowptr, f->col, f->A[k], f->b[k], f->nbc[k], f->bc_node[k], f->pred_bc_val[k]);
-            ok &= or_gmres(nv, f->rowptr, f->col, f->A[k], f->f[4 + k], f->b[k], P->tol, P->maxit,
-                           OR_PRECOND_JACOBI, &si);
+            if (P->prediction_solver == 2)
+                ok &= or_bicgstab(nv, f->rowptr, f->col, f->A[k], f->f[4 + k], f->b[k], P->tol, P->maxit,
+                                  OR_PRECOND_JACOBI, 0, &si);
+            else if (P->gmres_orth == 1)
+                ok &= or_gmres_cgs2(nv, f->rowptr, f->col, f->A[k], f->f[4 + k], f->b[k], P->tol, P->maxit,
+                                    OR_PRECOND_JACOBI, &si);
+            else
+                ok &= or_gmres(nv, f->rowptr, f->col, f->A[k], f->f[4 + k], f->b[k], P->tol, P->maxit,
+                               OR_PRECOND_JACOBI, &si);
             if (info && it < 8) info->it_pred[k][it] = si.iterations;
         }
         memset(f->A[2], 0, sizeof(double) * nnz);
         memset(f->b[2], 0, sizeof(double) * nv);
         or_assemble_pressure(f->nc, f->tri, f->area, f->invJ, P, prx, pry, pold, f->rowptr, f->col, f->A[2], f->b[2]);
         or_apply_bcs(nv, f->rowptr, f->col, f->A[2], f->b[2], f->nbc[2], f->bc_node[2], f->bc_val[2]);
-        ok &= or_pcg(nv, f->rowptr, f->col, f->A[2], pr, f->b[2], P->tol, P->maxit, P->pressure_precond, &si);
-        if (info && it < 8) info->it_pres[it] = si.iterations;
+        double relres = 0.0;
+        const double ptol = P->pressure_tol > 0 ? P->pressure_tol : P->tol;
+        const int pmaxit = P->pressure_maxit > 0 ? P->pressure_maxit : P->maxit;
+        if (P->pressure_ordering == 0 && P->pressure_criterion == 0)
+            ok &= or_pcg(nv, f->rowptr, f->col, f->A[2], pr, f->b[2], ptol, pmaxit, P->pressure_precond, &si);
+        else
+            ok &= or_cg(nv, f->rowptr, f->col, f->A[2], pr, f->b[2], ptol, pmaxit, P->pressure_precond,
+                        P->pressure_ordering, P->pressure_criterion, &si, &relres);
+        if (info && it < 8) {
+            info->it_pres[it] = si.iterations;
+            info->res_pres[it] = relres;
+        }
         memset(f->A[3], 0, sizeof(double) * nnz); memset(f->A[4], 0, sizeof(double) * nnz);
         memset(f->b[3], 0, sizeof(double) * nv); memset(f->b[4], 0, sizeof(double) * nv);
         or_assemble_correction(f->nc, f->tri, f->area, f->invJ, P, prx, pry, pr, pold, f->rowptr, f->col,
@@ -1224,6 +1258,16 @@ int or_flow_step(or_flow* f, or_step_info* info)
 }
 
 int or_flow_particle_count(const or_flow* f) { return f->np; }
+
+void or_flow_set_solvers(or_flow* f, int pressure_precond, int pressure_ordering, int prediction_solver,
+                         int gmres_orth, int pressure_criterion)
+{
+    f->P.pressure_precond = pressure_precond;
+    f->P.pressure_ordering = pressure_ordering;
+    f->P.prediction_solver = prediction_solver;
+    f->P.gmres_orth = gmres_orth;
+    f->P.pressure_criterion = pressure_criterion;
+}
 
 void or_flow_get_field(const or_flow* f, int which, double* out) { memcpy(out, f->f[which], sizeof(double) * f->nv); }
 void or_flow_set_field(or_flow* f, int which, const double* in) { memcpy(f->f[which], in, sizeof(double) * f->nv); }

@@ -64,6 +64,22 @@ int or_pcg(int n, const int* rowptr, const int* col, const double* val, double* 
 int or_gmres(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b,
              double tol, int maxit, int precond, or_solve_info* info);
 
+/* ---- solver options of the engine beyond the reference (pf2_oracle_solvers.c) ---- */
+/* Greedy colouring in row order with Kempe-chain trimming of the tail (kempe != 0);
+ * perm[r] = row at position r of P A P^T, starts (may be NULL) gets the colour starts
+ * and n.  Returns the number of colours. */
+int or_multicolour_order(int n, const int* rowptr, const int* col, int kempe, int* perm, int* starts);
+/* CG with ordering 0 (natural) / 1 (multicolour, ILU/IC only) and criterion 0 (r^T z <
+ * tol^2, the reference's) / 1 (||r|| <= tol ||b||); rel_residual may be NULL. */
+int or_cg(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b, double tol,
+          int maxit, int precond, int ordering, int criterion, or_solve_info* info, double* rel_residual);
+/* Right-preconditioned BiCGStab, Jacobi or none; criterion 0: ||M^{-1} r|| < tol. */
+int or_bicgstab(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b,
+                double tol, int maxit, int precond, int criterion, or_solve_info* info);
+/* GMRES as or_gmres with classical Gram-Schmidt applied twice (DGKS test, 0.7). */
+int or_gmres_cgs2(int n, const int* rowptr, const int* col, const double* val, double* x, const double* b,
+                  double tol, int maxit, int precond, or_solve_info* info);
+
 /* ---- particles (src/particles/particle_handler_2d.cu) ---- */
 int or_subcell_centers(int level, double* centers3);
 int or_determine_subcell(int level, double step, const double* l3);
@@ -94,6 +110,13 @@ typedef struct {
     double lx, ly;
     int has_cylinder;
     double cx, cy, radius;
+    /* solver choices of the engine (0 everywhere: the reference's) */
+    int pressure_ordering;   /* 0 natural, 1 multicolour (ILU/IC) */
+    int prediction_solver;   /* 0 or 1: GMRES, 2: BiCGStab (Jacobi) */
+    int gmres_orth;          /* 0 modified Gram-Schmidt, 1 classical twice */
+    int pressure_criterion;  /* 0 r^T z < tol^2, 1 ||r|| <= tol ||b|| */
+    double pressure_tol;     /* 0: tol */
+    int pressure_maxit;      /* 0: maxit */
 } or_params;
 
 typedef struct {
@@ -102,6 +125,7 @@ typedef struct {
     int it_pred[2][8], it_pres[8], it_corr[2][8];
     int conv_ok;
     double cx, cy;
+    double res_pres[8]; /* ||r|| / ||b|| of each pressure solve's recursive residual at its end */
 } or_step_info;
 
 typedef struct or_flow or_flow;
@@ -112,6 +136,10 @@ or_flow* or_flow_create(int nv, const double* xy, int nc, const int* tri, const 
 void or_flow_destroy(or_flow* f);
 int or_flow_step(or_flow* f, or_step_info* info);
 int or_flow_particle_count(const or_flow* f);
+/* Changes the solver choices of the following steps (the or_params fields of the same
+ * names); the state is kept. */
+void or_flow_set_solvers(or_flow* f, int pressure_precond, int pressure_ordering, int prediction_solver,
+                         int gmres_orth, int pressure_criterion);
 /* field ids: 0 ux,1 uy,2 ux_old,3 uy_old,4 pred_x,5 pred_y,6 p,7 p_old */
 void or_flow_get_field(const or_flow* f, int which, double* out);
 void or_flow_set_field(or_flow* f, int which, const double* in);

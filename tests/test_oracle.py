@@ -126,3 +126,68 @@ def test_uniform_flow_moves_deletes_and_reseeds():
     counts = np.bincount(Q["cell"], minlength=tri.shape[0])
     assert counts.min() >= 4
     assert np.all(np.diff(Q["cell"]) >= 0)
+
+
+def test_bicgstab_restarts_an_orthogonal_shadow_residual():
+    """rhat = r0 lives on identity rows that the first iteration zeroes in r, so
+    rhat.r = 0 exactly with r != 0: the solve restarts rhat = r and converges to the
+    direct solution instead of stopping."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    from tests.helpers import shadow_breakdown_system
+    xy, tri, rp, col, val, rhs = shadow_breakdown_system()
+    n = rp.size - 1
+    A = sp.csr_matrix((val, col, rp), shape=(n, n))
+    exact = spl.spsolve(A.tocsc(), rhs)
+    for criterion in (0, 1):
+        x, info = O.bicgstab(rp, col, val, rhs, tol=1e-12, maxit=500, precond="jacobi", criterion=criterion)
+        assert info.converged == 1 and info.iterations > 1
+        assert np.abs(x - exact).max() < 1e-9 * np.abs(exact).max()
+
+
+def test_solver_options_agree_on_a_converged_system():
+    """The engine's solver options restated in the oracle (multicolour IC(0)/ILU(0) CG,
+    the relative criterion, BiCGStab, GMRES with classical Gram-Schmidt twice) reach the
+    natural-order solution of the reference's CG."""
+    xy, tri = mg.channel(64, 16, 4.0, 1.0)
+    area, invJ = O.mesh_geometry(xy, tri)
+    rp, col = O.csr_structure(xy.shape[0], tri)
+    val, rhs = O.assemble_poisson(xy, tri, area, invJ, rp, col, 1, 1.0)
+    diag = np.array([rp[i] + np.searchsorted(col[rp[i]:rp[i + 1]], i) for i in range(rp.size - 1)])
+    val[diag] += 1e-2
+    ref, _ = O.pcg(rp, col, val, rhs, tol=1e-13, maxit=5000, precond="jacobi")
+    for pc in ("jacobi", "ilu", "ic"):
+        for ordering in (0, 1):
+            x, info, rel = O.cg(rp, col, val, rhs, tol=1e-11, maxit=5000, precond=pc, ordering=ordering,
+                                criterion=1)
+            assert info.converged == 1 and rel <= 1e-11
+            assert np.abs(x - ref).max() < 1e-9 * np.abs(ref).max()
+    x, info = O.bicgstab(rp, col, val, rhs, tol=1e-11, maxit=5000, precond="jacobi", criterion=1)
+    assert info.converged == 1 and np.abs(x - ref).max() < 1e-9 * np.abs(ref).max()
+    x, info = O.gmres_cgs2(rp, col, val, rhs, tol=1e-11, maxit=2000, precond="jacobi")
+    x2, info2 = O.gmres(rp, col, val, rhs, tol=1e-11, maxit=2000, precond="jacobi")
+    assert info.converged == 1 and abs(info.iterations - info2.iterations) <= 2
+    assert np.abs(x - ref).max() < 1e-8 * np.abs(ref).max()
+
+
+def test_oracle_flow_with_the_engine_solver_choices():
+    """A cylinder flow from rest with BiCGStab for the prediction: every solve of the
+    first steps converges (the first prediction system is the one whose shadow residual
+    the first iteration makes orthogonal), and the fields agree with GMRES's within the
+    solve tolerance."""
+    xy, tri = mg.cylinder_channel(nxh=100, nyh=100, nr=6)
+    bu, bv, bp = mg.channel_boundary_nodes(xy, 2.2, 0.41, 1.5, cylinder=(0.2, 0.2, 0.05))
+    base = dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=2, n_outer=2, substeps=3, pressure_precond=2,
+                calc_loads=1, body_id=3, thickness=0.1, lx=2.2, ly=0.41, has_cylinder=1, cx=0.2, cy=0.2,
+                radius=0.05, tol=1e-12, maxit=3000, pressure_tol=1e-13, pressure_maxit=5000, pressure_criterion=1,
+                pressure_ordering=1)
+    out = {}
+    for pred in (1, 2):
+        f = O.Flow(xy, tri, O.make_params(prediction_solver=pred, **base), bu, bv, bp)
+        for _ in range(2):
+            info = f.step()
+            assert info.conv_ok == 1 and info.res_pres[0] <= 1e-13
+        out[pred] = (f.field("ux"), f.field("p"), info.cx)
+    for k in range(2):
+        assert np.abs(out[1][k] - out[2][k]).max() <= 1e-9 * np.abs(out[1][k]).max()
+    assert abs(out[1][2] - out[2][2]) <= 1e-9 * abs(out[1][2])

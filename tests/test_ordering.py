@@ -79,3 +79,20 @@ def test_3d_pattern_is_coloured_properly():
     # groups after the trimmed colours are single colours as well
     check_groups(rp, col, perm, starts, independent=True)
     assert nc == starts.size - 1
+
+
+@pytest.mark.parametrize("name,make", [("quarter", lambda: mg.cylinder_channel(nxh=350, nyh=400, nr=12)),
+                                       ("channel", lambda: mg.channel()),
+                                       ("square", lambda: mg.unit_square(64))])
+@pytest.mark.parametrize("kempe", [True, False])
+def test_oracle_restates_the_engine_colouring(name, make, kempe):
+    """The oracle's multicolour order (its restatement of greedy colouring with Kempe
+    trimming) is the engine's permutation, so the oracle can run the pressure solve
+    with the engine's IC(0)/ILU(0) ordering."""
+    xy, tri = make()
+    rp, col = O.csr_structure(xy.shape[0], tri)
+    perm, nc, starts = order(rp, col, kempe=kempe)
+    operm, ostarts = O.multicolour_order(rp, col, kempe=kempe)
+    assert np.array_equal(perm, operm)
+    if kempe:
+        assert np.array_equal(starts, ostarts)
