@@ -1,0 +1,150 @@
+"""Whole PFEM-2 steps (cases/Cylinder2D/main.cu:793-880, PoiseuilleFlow2D/main.cu:652-735)
+on the GPU against the oracle run with the same solver choices, on the configurations the
+benchmark and the workload list name:
+
+* the benchmarked cylinder configuration (Scheme B, level 4, IC(0) on the multicolour
+  order, BiCGStab(Jacobi) for the prediction) on the quarter-size cylinder mesh;
+* the FP64 path of the reference's own solver choices at the 1e-10 tolerance per step;
+* the 4 x 1 channel at its stated size (256 x 64 quads, level 3, Scheme A, ILU(0)).
+
+Every solve is converged tightly on both sides (velocity solves to an absolute 1e-12,
+about ten times their rounding floor ||M^{-1} r|| ~ 1e-16 sqrt(n) |u|; pressure to
+||r|| <= 1e-13 ||b||), so the fields of engine and oracle differ only by rounding: the
+tests assert 1e-10 relative (max-norm) per field and per step, and bit-exact particle
+cells and per-cell counts.  Each test prints its per-step errors."""
+import numpy as np
+import pytest
+
+import gpupfem2_gb300 as g
+from gpupfem2_gb300 import meshgen as mg
+from oracle import oracle as O
+from tests.helpers import rel_err
+
+pytestmark = pytest.mark.gpu
+
+FP64_STEP_TOL = 1e-10  # relative, max-norm, per field and per step
+TIGHT = dict(tolerance=1e-12, max_iterations=3000, pressure_tolerance=1e-13, pressure_max_iterations=20000,
+             pressure_criterion=1)
+FIELDS = ("ux", "uy", "p")
+
+
+def _cylinder_quarter():
+    xy, tri = mg.cylinder_channel(nxh=350, nyh=400, nr=12)
+    cyl = (0.2, 0.2, 0.05)
+    bu, bv, bp = mg.channel_boundary_nodes(xy, 2.2, 0.41, 1.5, cylinder=cyl)
+    kw = dict(rho=1.0, mu=1e-3, dt=5e-4, scheme=1, level=4, n_outer=2, substeps=3, pressure_precond=2)
+    eng_kw = dict(kw, calculate_loads=1, body_boundary_id=3, thickness=0.1, mean_velocity=1.0)
+    or_kw = dict(kw, calc_loads=1, body_id=3, thickness=0.1, lx=2.2, ly=0.41, has_cylinder=1, cx=cyl[0],
+                 cy=cyl[1], radius=cyl[2])
+    return xy, tri, (bu, bv, bp), (2.2, 0.41, cyl), eng_kw, or_kw
+
+
+def _channel(nx, ny, scheme, precond, level):
+    xy, tri = mg.channel(nx, ny, 4.0, 1.0)
+    bu, bv, bp = mg.channel_boundary_nodes(xy, 4.0, 1.0)
+    kw = dict(rho=1.0, mu=0.01, dt=0.005, scheme=scheme, level=level, n_outer=2, substeps=3,
+              pressure_precond=precond)
+    return xy, tri, (bu, bv, bp), (4.0, 1.0, None), kw, dict(kw, lx=4.0, ly=1.0)
+
+
+def _run(case, steps, eng_solver, or_solver, tight=True, label=""):
+    """Runs `steps` steps on both sides; returns the per-step errors."""
+    xy, tri, (bu, bv, bp), (lx, ly, cyl), eng_kw, or_kw = case
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(lx, ly, cyl)
+    ekw = dict(eng_kw, **eng_solver)
+    okw = dict(or_kw, **or_solver)
+    if tight:
+        ekw.update(TIGHT)
+        okw.update(tol=TIGHT["tolerance"], maxit=TIGHT["max_iterations"], pressure_tol=TIGHT["pressure_tolerance"],
+                   pressure_maxit=TIGHT["pressure_max_iterations"], pressure_criterion=1)
+    else:  # the benchmark's settings: the reference's absolute 1e-8 and 1,000 iterations
+        ekw.update(tolerance=1e-8, max_iterations=1000, pressure_criterion=0)
+        okw.update(tol=1e-8, maxit=1000, pressure_criterion=0)
+    eng = g.FlowEngine(m, g.default_params(**ekw), bu, bv, bp, capacity_factor=4.0)
+    eng.seed()
+    ref = O.Flow(xy, tri, O.make_params(**okw), bu, bv, bp, particle_cap=4 * tri.shape[0] * eng_kw["level"] ** 2)
+    rows = []
+    for s in range(steps):
+        eng.step()
+        oi = ref.step()
+        info = eng.info()
+        P, R = eng.particles.download(), ref.particles()
+        row = {"step": s + 1, "particles": int(info.particles),
+               "cells_equal": bool(P["cell"].size == R["cell"].size and np.array_equal(P["cell"], R["cell"])),
+               "counts_equal": bool(np.array_equal(np.bincount(P["cell"], minlength=tri.shape[0]),
+                                                   np.bincount(R["cell"], minlength=tri.shape[0]))),
+               "converged": (int(info.converged), int(oi.conv_ok))}
+        for f in FIELDS:
+            row[f] = rel_err(eng.field(f), ref.field(f))
+        if eng_kw.get("calculate_loads"):
+            row["cx"] = abs(info.cx - oi.cx) / abs(oi.cx)
+            row["cy"] = abs(info.cy - oi.cy) / max(abs(oi.cy), 1e-300)
+        row["x"] = float(np.abs(P["x"] - R["x"]).max()) if row["cells_equal"] else None
+        rows.append(row)
+        print("%s step %d: particles %d, cells %s, counts %s, %s" % (
+            label, s + 1, row["particles"], "equal" if row["cells_equal"] else "DIFFER",
+            "equal" if row["counts_equal"] else "DIFFER",
+            ", ".join("%s %.2e" % (k, row[k]) for k in FIELDS + ("cx", "cy") if k in row)), flush=True)
+    return rows
+
+
+def _assert_rows(rows, tol=FP64_STEP_TOL, keys=FIELDS + ("cx", "cy")):
+    for row in rows:
+        assert row["converged"] == (1, 1), row
+        assert row["cells_equal"] and row["counts_equal"], row
+        for k in keys:
+            if k in row:
+                assert row[k] <= tol, (k, row)
+
+
+def test_benchmarked_cylinder_configuration_matches_oracle(cuda):
+    """The benchmark's solver choices on both sides (IC(0) on the multicolour order with
+    the same colouring, BiCGStab(Jacobi) prediction), converged: 1e-10 per field, drag
+    and lift, particle cells and counts bit-exact, three steps from rest."""
+    rows = _run(_cylinder_quarter(), 3,
+                dict(pressure_ordering=1, prediction_solver=g.SOLVER_BICGSTAB),
+                dict(pressure_ordering=1, prediction_solver=2), label="cylinder_quarter bench-config")
+    _assert_rows(rows)
+
+
+def test_benchmarked_cylinder_settings_as_run(cuda):
+    """The same case at the benchmark's own stopping settings (absolute 1e-8, at most
+    1,000 iterations: the pressure solves stop at the limit).  Particle cells and counts
+    stay bit-exact over two steps; the fields differ by the rounding of two unconverged
+    CG runs, which the test bounds at 1e-6."""
+    rows = _run(_cylinder_quarter(), 2,
+                dict(pressure_ordering=1, prediction_solver=g.SOLVER_BICGSTAB),
+                dict(pressure_ordering=1, prediction_solver=2), tight=False,
+                label="cylinder_quarter bench-settings")
+    for row in rows:
+        assert row["cells_equal"] and row["counts_equal"], row
+        for k in FIELDS + ("cx", "cy"):
+            assert row[k] <= 1e-6, (k, row)
+
+
+@pytest.mark.parametrize("scheme,precond", [(0, 0), (1, 0), (0, 1), (1, 2)])
+def test_fp64_step_parity_reference_solvers(cuda, scheme, precond):
+    """The reference's own algorithms (natural-order preconditioners, GMRES with modified
+    Gram-Schmidt) on the 64 x 16 channel, converged: 1e-10 per field per step."""
+    rows = _run(_channel(64, 16, scheme, precond, 3), 3, dict(), dict(),
+                label="channel64x16 scheme %s precond %d" % ("AB"[scheme], precond))
+    _assert_rows(rows)
+
+
+def test_fp64_step_parity_cylinder_reference_solvers(cuda):
+    """The reference cylinder driver's solvers (GMRES(Jacobi) prediction with modified
+    Gram-Schmidt, Jacobi-CG pressure, Cylinder2D/main.cu:768-774) on the quarter-size
+    cylinder, converged: fields, drag and lift within 1e-10 per step."""
+    case = list(_cylinder_quarter())
+    case[4] = dict(case[4], pressure_precond=0)
+    case[5] = dict(case[5], pressure_precond=0)
+    rows = _run(tuple(case), 2, dict(), dict(), label="cylinder_quarter reference-solvers")
+    _assert_rows(rows)
+
+
+def test_channel_at_its_stated_size_matches_oracle(cuda):
+    """The 4 x 1 channel at its stated size: 256 x 64 quads (32,768 triangles), level 3,
+    Scheme A, ILU(0) pressure, converged solves; three steps against the oracle."""
+    rows = _run(_channel(256, 64, 0, 1, 3), 3, dict(), dict(), label="channel256x64 scheme A ILU(0)")
+    _assert_rows(rows)

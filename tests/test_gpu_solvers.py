@@ -388,3 +388,21 @@ def test_bicgstab_half_step_solution_is_converged(cuda):
         info = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-10, maxit=50, criterion=criterion).solve(A, x, b)
         assert info.converged == 1 and info.status == 0 and info.iterations == 1
         assert np.array_equal(x.cpu().numpy(), rhs / d)
+
+
+def test_bicgstab_restarts_an_orthogonal_shadow_residual(cuda):
+    """rhat = r0 supported on identity rows that the first iteration zeroes in r: the
+    engine restarts the shadow residual as the oracle does and reaches its solution."""
+    from tests.helpers import shadow_breakdown_system
+    xy, tri, rp, col, val, rhs = shadow_breakdown_system()
+    m = g.Mesh2D.from_arrays(xy, tri)
+    A = g.SparseMatrixCSR(m)
+    A.upload_values(val)
+    ox, oinfo = O.bicgstab(rp, col, val, rhs, tol=1e-12, maxit=500, precond="jacobi")
+    assert oinfo.converged == 1
+    b = torch.tensor(rhs, device="cuda")
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-12, maxit=500).solve(A, x, b)
+    assert info.converged == 1 and info.iterations > 1
+    assert abs(info.iterations - oinfo.iterations) <= 2
+    assert rel_err(x.cpu().numpy(), ox) < 1e-9
