@@ -8,9 +8,13 @@ named shape: the mesh and particles are generated, the flow starts from rest and
 `--warmup` steps run before the timed ones.
 
 Arms:
-  default           the engine (C ABI via ctypes, CUDA kernels for sm_103a)
-  --impl reference  the CPU oracle of the same step (oracle/, single-thread FP64 port of
-                    the reference's algorithm) on a bounded sample, on the host cores
+  default           the engine (C ABI via ctypes, CUDA kernels for sm_103a); beside it the
+                    reference's own CUDA build on the same workload and GPU
+                    (`reference_cuda`, oracle/build_ref_cuda.sh) and the CPU oracle from
+                    the engine's state (`cpu_baseline`)
+  --impl reference  the CPU oracle of the same step (oracle/, an FP64 C port of the
+                    reference's algorithm with the engine arm's solver choices, OpenMP on
+                    the host cores), the same warm-up from rest, then timed steps
 
 Prints ONE JSON line (rank 0).  `value` is device time per step with all state
 resident in HBM; `e2e` is the same step driven through the C ABI with the inflow
@@ -146,54 +150,175 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(name, precond, max_seconds=25.0):
-    """The oracle's step on a bounded sample of the workload (one host core)."""
+def oracle_params(name, prm):
+    """The oracle's parameters for a workload, with the engine arm's solver choices: the
+    pressure preconditioner and its ordering (the multicolour order is the engine's
+    colouring, restated in the oracle), the prediction solver, GMRES's Gram-Schmidt and
+    the stopping tests."""
     from oracle import oracle as O
-    w, xy, tri, bu, bv, bp, prm = build_case(name, precond)
-    # the oracle runs the reference's algorithm: natural-order ILU/IC, modified Gram-Schmidt
-    kw = {k: v for k, v in prm.items() if k not in ("calculate_loads", "body_boundary_id", "mean_velocity",
-                                                    "thickness", "pressure_ordering", "gmres_orthogonalization",
-                                                    "cg_variant", "prediction_solver")}
+    w = WORKLOADS[name]
     cyl = w["cyl"]
-    op = O.make_params(lx=w["lx"], ly=w["ly"], tol=1e-8, has_cylinder=int(cyl is not None),
-                       cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
-                       calc_loads=prm.get("calculate_loads", 0), body_id=prm.get("body_boundary_id", -1),
-                       thickness=prm.get("thickness", 1.0), **kw)
-    flow = O.Flow(xy, tri, op, bu, bv, bp)
+    return O.make_params(
+        rho=prm["rho"], mu=prm["mu"], dt=prm["dt"], scheme=prm["scheme"], level=prm["level"], n_outer=prm["n_outer"],
+        substeps=prm["substeps"], pressure_precond=prm["pressure_precond"], tol=prm.get("tolerance", 1e-8),
+        maxit=prm.get("max_iterations", 1000), lx=w["lx"], ly=w["ly"], has_cylinder=int(cyl is not None),
+        cx=cyl[0] if cyl else 0.2, cy=cyl[1] if cyl else 0.2, radius=cyl[2] if cyl else 0.05,
+        calc_loads=prm.get("calculate_loads", 0), body_id=prm.get("body_boundary_id", -1),
+        thickness=prm.get("thickness", 1.0), pressure_ordering=prm.get("pressure_ordering", 0),
+        prediction_solver=prm.get("prediction_solver", 1), gmres_orth=prm.get("gmres_orthogonalization", 0),
+        pressure_criterion=prm.get("pressure_criterion", 0))
+
+
+def same_solver_config(prm):
+    """True when the oracle runs exactly the engine arm's solver algorithms (the oracle
+    has the standard CG iteration only)."""
+    return prm.get("cg_variant", 0) == 0 and prm.get("pressure_precision", 0) == 0 and prm.get("pressure_x0", 0) == 0
+
+
+def _omp_threads():
+    return int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count() or 1
+
+
+def cpu_baseline(name, prm, eng, xy, tri, bu, bv, bp, max_seconds=25.0):
+    """The oracle's step, with the engine arm's solver choices, from the state the engine
+    reached (its particles and the eight node fields copied into the oracle): a bounded
+    sample of the same workload at the same step."""
+    from oracle import oracle as O
+    P = eng.particles.download()
+    np0 = int(P["cell"].size)
+    flow = O.Flow(xy, tri, oracle_params(name, prm), bu, bv, bp, particle_cap=int(1.5 * np0) + 1024)
+    flow.set_particles(P)
+    del P
+    for f in O.Flow.FIELDS:
+        flow.set_field(f, eng.field(f))
     times = []
     t_all = time.perf_counter()
-    while time.perf_counter() - t_all < max_seconds or not times:
+    while not times or (time.perf_counter() - t_all < max_seconds and len(times) < 3):
         t0 = time.perf_counter()
         flow.step()
         times.append(time.perf_counter() - t0)
-        if len(times) >= 3:
-            break
-    ms = 1000.0 * statistics.median(times)
-    threads = int(os.environ.get("OMP_NUM_THREADS", "0") or 0) or os.cpu_count() or 1
-    return {"value": ms, "unit": "ms/step", "cores": threads, "kind": "port",
-            "sample": "%d oracle step(s) of the full %s workload (%d triangles, %d particles at the start), "
-                      "median; FP64 C port, OpenMP over particles and SpMV rows (%d threads), "
-                      "the rest single-threaded" % (len(times), name, tri.shape[0], tri.shape[0] * prm["level"] ** 2,
-                                                    threads)}
+    threads = _omp_threads()
+    return {"value": 1000.0 * statistics.median(times), "unit": "ms/step", "cores": threads, "kind": "port",
+            "same_config": same_solver_config(prm),
+            "sample": "%d oracle step(s) of the full %s workload from the engine's state after its timed steps "
+                      "(%d triangles, %d particles), median; FP64 C port with the engine arm's solver choices, "
+                      "OpenMP (%d threads) over particles, SpMV rows, colour classes and vector updates"
+                      % (len(times), name, tri.shape[0], np0, threads)}
 
 
 def run_reference(args):
-    name, precond = args.workload, args.precond
-    wp = WORKLOADS[name]["params"]
-    base = cpu_baseline(name, precond, max_seconds=20.0)
-    line = {"metric": "ms per PFEM-2 step", "value": base["value"], "unit": "ms/step", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": base["value"], "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": name,
-                       "pressure_precond": PRECOND_NAMES[wp["pressure_precond"] if precond is None else precond],
-                       # the oracle follows the reference's algorithms: natural-order ILU/IC
-                       # sweeps and GMRES with modified Gram-Schmidt for the prediction
-                       "pressure_ordering": "natural", "prediction_solver": "gmres",
-                       "gmres_gram_schmidt": "modified", "scheme": "AB"[wp["scheme"]], "level": wp["level"],
-                       "n_outer": wp["n_outer"]},
+    """The reference arm: the oracle (a C port of the reference's step, with the same
+    solver choices as the engine arm) on the same workload, warmed up by the same number of
+    steps from rest, then timed step by step until --steps steps or --ref-budget seconds
+    (at least one step).  The steps actually timed are reported.  One more step from the
+    same state with the reference's own solver algorithms (natural-order ILU/IC, GMRES with
+    modified Gram-Schmidt) is reported beside it."""
+    from oracle import oracle as O
+    name = args.workload
+    w, xy, tri, bu, bv, bp, prm = build_case(name, args.precond, args.ordering, args.gs, args.cg, args.pred)
+    level = prm["level"]
+    flow = O.Flow(xy, tri, oracle_params(name, prm), bu, bv, bp, particle_cap=4 * tri.shape[0] * level * level)
+    t_start = time.perf_counter()
+    for _ in range(args.warmup):
+        flow.step()
+    warm_s = time.perf_counter() - t_start
+    times, info = [], None
+    t0 = time.perf_counter()
+    while len(times) < args.steps and (not times or time.perf_counter() - t0 < args.ref_budget):
+        t1 = time.perf_counter()
+        info = flow.step()
+        times.append(time.perf_counter() - t1)
+    ms = 1000.0 * statistics.mean(times)
+    particles = int(info.particles)
+    ref_alg_ms = None
+    if args.ref_algorithms:
+        # the reference's own algorithms from the same state
+        flow.set_solvers(prm["pressure_precond"], 0, 1, 0, 0)
+        t1 = time.perf_counter()
+        flow.step()
+        ref_alg_ms = 1000.0 * (time.perf_counter() - t1)
+    threads = _omp_threads()
+    cfg = {"workload": name, "triangles": int(tri.shape[0]), "particles": particles,
+           "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
+           "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
+           "prediction_solver": {1: "gmres", 2: "bicgstab"}[prm.get("prediction_solver", 1)],
+           "scheme": "AB"[prm["scheme"]], "level": level, "n_outer": prm["n_outer"],
+           "tolerance": prm.get("tolerance", 1e-8), "max_iterations": prm.get("max_iterations", 1000),
+           "same_config_as_engine_arm": same_solver_config(prm),
+           "steps_requested": args.steps, "timed_from_step": args.warmup + 1}
+    if prm.get("prediction_solver", 1) == 1:
+        cfg["gmres_gram_schmidt"] = ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)]
+    base = {"value": ms, "unit": "ms/step", "cores": threads, "kind": "port",
+            "sample": "%d oracle step(s) of the full %s workload, steps %d-%d after %d warm-up steps from rest "
+                      "(%.0f s), mean; FP64 C port of the reference's step with the engine arm's solver choices, "
+                      "OpenMP (%d threads) over particles, SpMV rows, colour classes and vector updates"
+                      % (len(times), name, args.warmup + 1, args.warmup + len(times), args.warmup, warm_s, threads)}
+    line = {"metric": "ms per PFEM-2 step", "value": ms, "unit": "ms/step", "n_gpus": args.gpus,
+            "steps": len(times), "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "impl": "reference", "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": ms, "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if ref_alg_ms is not None:
+        line["reference_algorithms"] = {
+            "ms_per_step": ref_alg_ms, "step": args.warmup + len(times) + 1, "pressure_ordering": "natural",
+            "prediction_solver": "gmres", "gmres_gram_schmidt": "modified",
+            "note": "one step of the reference's own solver algorithms from the same state"}
     print(json.dumps(line))
+
+
+REF_CUDA = os.path.join(ROOT, "baseline", "_ref", "bin", "ref_cylinder")
+REF_STAGE = os.path.join(ROOT, "baseline", "_ref", "gpuPfem2", "src")
+
+
+def reference_cuda(name, xy, tri, prm, precond="jacobi", warmup=5, steps=20, timeout=900):
+    """The reference's own CUDA build (its library and Cylinder2D case code, compiled for
+    sm_103a by oracle/build_ref_cuda.sh) running the same cylinder workload on this GPU:
+    per-step time from its own GpuTimer, warm mean and median over `steps` steps after
+    `warmup` steps from rest.  Returns None for workloads other than the cylinder."""
+    if name not in ("cylinder", "cylinder_quarter"):
+        return None
+    if not os.path.exists(REF_CUDA):
+        if not os.path.isdir(REF_STAGE):
+            return {"unavailable": "reference sources not staged (oracle/build_ref_cuda.sh stage)"}
+        r = subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref_cuda.sh")], capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(REF_CUDA):
+            return {"unavailable": "reference build failed: " + (r.stderr.strip().splitlines() or [""])[-1][:200]}
+    with tempfile.TemporaryDirectory() as td:
+        mesh = os.path.join(td, "mesh.dat")
+        mg.write_dat(mesh, xy, tri)
+        out = os.path.join(td, "ref.json")
+        t0 = time.perf_counter()
+        try:
+            with open(os.path.join(td, "stdout.txt"), "w") as so:
+                r = subprocess.run([REF_CUDA, mesh, str(prm["level"]), repr(prm["dt"]), str(prm["scheme"]), precond,
+                                    str(warmup), str(steps), out], cwd=td, stdout=so, stderr=subprocess.STDOUT,
+                                   timeout=timeout)
+        except subprocess.TimeoutExpired:
+            return {"unavailable": "reference run exceeded %d s" % timeout}
+        wall = time.perf_counter() - t0
+        text = open(os.path.join(td, "stdout.txt")).read()
+        if r.returncode != 0 or not os.path.exists(out):
+            return {"unavailable": "reference run failed (rc %d): %s" % (r.returncode, text[-300:])}
+        res = json.load(open(out))
+        # the solvers' own prints: iterations of the last step's solves in their order
+        # (prediction x, y, pressure, correction x, y per outer iteration)
+        last = text[text.rfind("Time step no."):]
+        its = []
+        for ln in last.splitlines():
+            if ln.startswith("Solver converged"):
+                its.append(int(ln.rsplit("=", 1)[1]))
+            elif ln.startswith("Solver failed"):
+                its.append(-1)
+        forces = [ln.split(";") for ln in open(os.path.join(td, "Forces.csv")).read().split("\n")[1:] if ln]
+    sm = res["step_ms"]
+    return {"ms_per_step": statistics.mean(sm), "ms_per_step_median": statistics.median(sm), "steps": len(sm),
+            "warmup": warmup, "pressure_precond": precond,
+            "phase_ms": {k: round(v, 3) for k, v in res["phase_ms"].items()}, "particles": res["particles"],
+            "iterations_last_step": its, "cx": float(forces[-1][1]) if forces else None,
+            "cy": float(forces[-1][2]) if forces else None, "wall_s": round(wall, 1),
+            "timer": "the reference's GpuTimer (common/gpu_timer.cuh) per step",
+            "build": "reference src/ and cases/Cylinder2D kernels for sm_103a (-O2, rdc), neighbour lists "
+                     "filled in O(N) outside the timed steps; -1 in iterations_last_step: not converged"}
 
 
 def _timed(fn):
@@ -358,6 +483,14 @@ def main():
     ap.add_argument("--pred", type=int, default=None, help="prediction solver override (1 GMRES, 2 BiCGStab)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clock-log", default=None, help="where the nvidia-smi clock samples go (default: a temp file)")
+    ap.add_argument("--ref-budget", type=float, default=120.0,
+                    help="reference arm: seconds of timed oracle steps at most (at least one step)")
+    ap.add_argument("--ref-algorithms", type=int, default=1,
+                    help="reference arm: also time one step of the reference's own solver algorithms")
+    ap.add_argument("--ref-cuda-steps", type=int, default=20, help="timed steps of the reference CUDA build (0: skip)")
+    ap.add_argument("--ref-cuda-warmup", type=int, default=5)
+    ap.add_argument("--ref-cuda-ic-steps", type=int, default=0,
+                    help="timed steps of the reference CUDA build with its IC(0) pressure solver (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--study", default=None, choices=["solver", "learned"])
     ap.add_argument("--quick", action="store_true")
@@ -456,6 +589,31 @@ def main():
     torch.cuda.synchronize()
     spmv_ms = e0.elapsed_time(e1) / 20
     spmv_bytes = 12.0 * nnz + 4.0 * (mesh.nv + 1) + 16.0 * mesh.nv
+    # ---- full assembly (five matrices and right-hand sides from the flow's fields), timed
+    # apart: the step assembles the matrices on its first step only, the right-hand sides
+    # every step
+    fld = {k: _wrap(eng.field_ptr(k), nv) for k in g.FIELDS}
+    Ax, Ay = g.SparseMatrixCSR(mesh), g.SparseMatrixCSR(mesh)
+    rx = torch.empty(nv, dtype=torch.float64, device="cuda")
+    ry = torch.empty_like(rx)
+    pold = fld["p_old"] if prm["scheme"] else None
+
+    def full_assembly():
+        g.assemble_velocity_prediction(mesh, params, fld["ux"], fld["uy"], fld["ux_old"], fld["uy_old"], pold,
+                                       Ax, Ay, rx, ry)
+        g.assemble_pressure(mesh, params, fld["pred_x"], fld["pred_y"], pold, Ax, rx)
+        g.assemble_velocity_correction(mesh, params, fld["pred_x"], fld["pred_y"], fld["p"], pold, Ax, Ay, rx, ry)
+
+    for _ in range(3):
+        full_assembly()
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(5):
+        full_assembly()
+    e1.record()
+    torch.cuda.synchronize()
+    full_asm_ms = e0.elapsed_time(e1) / 5
+    del Ax, Ay
     # ---- roofline of the dominant phase
     peak, peak_kind = measured_peaks()
     np_ = info.particles
@@ -500,14 +658,16 @@ def main():
         "config": {"workload": args.workload, "triangles": int(tri.shape[0]), "nodes": int(nv), "nnz": int(nnz),
                    "particles": int(np_), "pressure_precond": PRECOND_NAMES[prm["pressure_precond"]],
                    "pressure_ordering": ["natural", "multicolour"][prm.get("pressure_ordering", 0)],
-                   "gmres_gram_schmidt": ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)],
                    "cg_variant": ["standard", "one_reduction", "pipelined"][prm.get("cg_variant", 0)],
                    "prediction_solver": {1: "gmres", 2: "bicgstab"}[prm.get("prediction_solver", 1)],
                    "scheme": "B" if prm["scheme"] else "A", "level": prm["level"], "n_outer": prm["n_outer"],
+                   "tolerance": prm.get("tolerance", 1e-8), "max_iterations": prm.get("max_iterations", 1000),
                    "l2": "working set (particles %.1f GB) larger than L2; no flush" % (np_ * 104 / 1e9),
                    "iterations_last_step": {"prediction": [list(info.it_prediction[c])[:prm["n_outer"]]
                                                            for c in range(2)],
                                             "pressure": list(info.it_pressure)[:prm["n_outer"]],
+                                            "pressure_relative_residual": list(info.pressure_residual)[
+                                                :prm["n_outer"]],
                                             "correction": [list(info.it_correction[c])[:prm["n_outer"]]
                                                            for c in range(2)]},
                    "phase_ms": {k: round(v, 4) for k, v in phase_ms.items()}, "cx": info.cx, "cy": info.cy},
@@ -515,8 +675,12 @@ def main():
                 "d2h_bytes_per_step": int(3 * nv * 8 + 8 * 5 * 8)},
         "metrics": {
             "particles_per_s": np_ / (phase_ms["particles"] * 1e-3) if phase_ms["particles"] > 0 else None,
-            "elements_assembled_per_s": int(tri.shape[0]) * 5 * prm["n_outer"] / (1e-3 * (
+            # the timed steps assemble right-hand sides only (five per outer iteration)
+            "rhs_elements_assembled_per_s": int(tri.shape[0]) * 5 * prm["n_outer"] / (1e-3 * (
                 phase_ms["prediction_assembly"] + phase_ms["pressure_assembly"] + phase_ms["correction_assembly"])),
+            # five matrices with their right-hand sides, timed apart
+            "matrix_elements_assembled_per_s": int(tri.shape[0]) * 5 / (1e-3 * full_asm_ms),
+            "full_assembly_ms": full_asm_ms,
             "spmv_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9, "spmv_ms": spmv_ms,
             "spmv_frac_of_hbm": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peak,
             "pressure_iterations_per_solve": pres_iters / prm["n_outer"],
@@ -528,8 +692,22 @@ def main():
                      "peak_source": peak_kind, "algorithmic": unit_desc},
         "clocks": clocks.summary(),
     }
+    if prm.get("prediction_solver", 1) == 1:
+        line["config"]["gmres_gram_schmidt"] = ["modified", "classical_twice"][prm.get("gmres_orthogonalization", 0)]
+    if rank == 0 and args.ref_cuda_steps > 0:
+        rc = reference_cuda(args.workload, xy, tri, prm, "jacobi", args.ref_cuda_warmup, args.ref_cuda_steps)
+        if rc is not None:
+            if "ms_per_step" in rc:
+                rc["speedup_of_engine"] = rc["ms_per_step"] / ms
+                rc["target_speedup"] = 3.0
+            line["reference_cuda"] = rc
+        if rc is not None and args.ref_cuda_ic_steps > 0:
+            ric = reference_cuda(args.workload, xy, tri, prm, "ic", 2, args.ref_cuda_ic_steps)
+            if ric and "ms_per_step" in ric:
+                ric["speedup_of_engine"] = ric["ms_per_step"] / ms
+            line["reference_cuda_ic"] = ric
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.workload, args.precond)
+        line["cpu_baseline"] = cpu_baseline(args.workload, prm, eng, xy, tri, bu, bv, bp)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
