@@ -5,6 +5,7 @@
 #     they lie into oracle/_ref/ref_host_dump, linked against the host-memory runtime
 #     stand-in oracle/refhost/stub_cudart.c;
 #     and the 3D host setup (DAT reader, CSR pattern, quadrature) into ref_host_dump3d;
+#     and the VTU writers (data_export.cu) into ref_vtu_dump;
 #  2. the reference's GPU kernels, compiled from the same sources into linked sm_103a
 #     cubins (device code only) with the mangled name of every kernel:
 #     ref_flow.cubin (mesh, particles, Dirichlet BCs, Cylinder2D kernels) and
@@ -32,6 +33,13 @@ $NVCC -arch=sm_103a -dlink $OBJS "$OUT/obj/dump_ref_host.o" -o "$OUT/obj/dlink.o
 gcc -O2 -c "$HERE/refhost/stub_cudart.c" -o "$OUT/obj/stub_cudart.o"
 g++ -o "$OUT/ref_host_dump" $OBJS "$OUT/obj/dump_ref_host.o" "$OUT/obj/dlink.o" "$OUT/obj/stub_cudart.o" -fopenmp
 echo "built $OUT/ref_host_dump"
+# the VTU writers (data_export.cu) on the same stand-in
+$NVCC $FLAGS -c "$REF/data_export.cu" -o "$OUT/obj/data_export.o"
+$NVCC $FLAGS -c "$HERE/refhost/dump_ref_vtu.cu" -o "$OUT/obj/dump_ref_vtu.o"
+$NVCC -arch=sm_103a -dlink $OBJS "$OUT/obj/data_export.o" "$OUT/obj/dump_ref_vtu.o" -o "$OUT/obj/dlink_vtu.o"
+g++ -o "$OUT/ref_vtu_dump" $OBJS "$OUT/obj/data_export.o" "$OUT/obj/dump_ref_vtu.o" "$OUT/obj/dlink_vtu.o" \
+  "$OUT/obj/stub_cudart.o" -fopenmp
+echo "built $OUT/ref_vtu_dump"
 # the 3D host setup: DAT reader, CSR pattern, quadrature table (neighbour lists are built
 # by GPU kernels there and left out)
 OBJS3=""

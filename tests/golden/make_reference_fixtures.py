@@ -1,4 +1,5 @@
-"""Generates tests/golden/reference_host.json from the reference's own host code (2D and 3D).
+"""Generates tests/golden/reference_host.json from the reference's own host code (2D and 3D),
+and tests/golden/reference_channel8x4.{mesh,particles}.vtu from its VTU writers.
 
 Builds oracle/_ref/ref_host_dump with oracle/build_ref.sh (the reference's DAT reader,
 CSR pattern builder, vertex-sharing neighbour search, particle-handler constructor and
@@ -131,6 +132,19 @@ def main():
     with open(OUT, "w") as f:
         json.dump(fixtures, f, indent=1, sort_keys=True)
     print("wrote", OUT)
+    # the reference's VTU writers on the 8 x 4 channel (oracle/refhost/dump_ref_vtu.cu
+    # states the fields and particles it writes)
+    exe_vtu = os.path.join(ROOT, "oracle", "_ref", "ref_vtu_dump")
+    with tempfile.TemporaryDirectory() as tmp:
+        xy, tri = mg.channel(8, 4, 4.0, 1.0)
+        dat = os.path.join(tmp, "channel8x4.dat")
+        mg.write_dat(dat, xy, tri)
+        subprocess.run([exe_vtu, dat, os.path.join(tmp, "channel8x4")], check=True, capture_output=True)
+        for part in ("mesh", "particles"):
+            dst = os.path.join(ROOT, "tests", "golden", "reference_channel8x4.%s.vtu" % part)
+            with open(os.path.join(tmp, "channel8x4.%s.vtu" % part)) as src, open(dst, "w") as f:
+                f.write(src.read())
+            print("wrote", dst)
 
 
 if __name__ == "__main__":

@@ -82,3 +82,19 @@ def test_engine_matches_reference_host_code(cuda, name, tmp_path):
     arrays = {"xy": m.download("xy"), "tri": m.download("tri"), "nboff": m.download("neighbor_offsets"),
               "nbidx": m.download("neighbor_indices"), "rowptr": rp, "col": col}
     check(FIX["meshes"][name], arrays)
+
+
+def test_reference_vtu_fixtures_parse():
+    """The committed output of the reference's VTU writers: well-formed VTK XML with the
+    mesh of the 8 x 4 channel and four particles per cell."""
+    import xml.etree.ElementTree as ET
+    here = os.path.dirname(os.path.abspath(__file__))
+    xy, tri = mg.channel(8, 4, 4.0, 1.0)
+    for part, npts, ncells in (("mesh", xy.shape[0], tri.shape[0]), ("particles", 4 * tri.shape[0],
+                                                                     4 * tri.shape[0])):
+        root = ET.parse(os.path.join(here, "golden", "reference_channel8x4.%s.vtu" % part)).getroot()
+        piece = root.find("UnstructuredGrid/Piece")
+        assert int(piece.get("NumberOfPoints")) == npts and int(piece.get("NumberOfCells")) == ncells
+    root = ET.parse(os.path.join(here, "golden", "reference_channel8x4.mesh.vtu")).getroot()
+    conn = [a for a in root.iter("DataArray") if a.get("Name") == "connectivity"][0]
+    assert np.array_equal(np.array(conn.text.split(), int).reshape(-1, 3), tri)
