@@ -636,10 +636,26 @@ __device__ __forceinline__ V spmv_rows(const Csr& A, const V* __restrict__ val, 
         int len = 0;
 #pragma unroll
         for (int u = 0; u < 4; ++u) len = max(len, e[u] - s[u]);
-        for (int k = 0; k < len; ++k) {
+        // two entries of each of the four rows per pass: the eight column and value loads
+        // go out together, then the eight vector loads, then the sums in entry order
+        for (int k = 0; k < len; k += 2) {
+            int j[8];
+            V w[8], x[8];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (s[u] + k < e[u]) acc[u] += __ldg(&val[s[u] + k]) * __ldcg(&p[__ldg(&A.col[s[u] + k])]);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const bool in = s[u] + k + h < e[u];
+                    j[2 * u + h] = in ? __ldg(&A.col[s[u] + k + h]) : -1;
+                    w[2 * u + h] = in ? __ldg(&val[s[u] + k + h]) : V(0);
+                }
+#pragma unroll
+            for (int t = 0; t < 8; ++t) x[t] = j[t] >= 0 ? __ldcg(&p[j[t]]) : V(0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+                    if (j[2 * u + h] >= 0) acc[u] += w[2 * u + h] * x[2 * u + h];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -724,17 +740,21 @@ __device__ __forceinline__ void p_update(V* p, const V* z, V beta, int r0, int r
 }
 
 // sum_k f_k x_{col_k} over the CSR entries [k0, k1) of a row whose x entries other
-// threads of the same sweep are still writing: four entries loaded together, only the
-// pending ones polled (bounded); terms added in entry order.
+// threads of the same sweep are still writing: four entries loaded together (columns and
+// factor values in one round trip, then the vector entries), only the pending ones polled
+// (bounded); terms added in entry order.
 template <class V>
 __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__ col, const V* __restrict__ f,
                                              int k0, int k1, int row, int* err, int* rec, V& sum) {
     sum = V(0);
     for (int k = k0; k < k1; k += 4) {
         int j[4];
-        V v[4];
+        V v[4], fk[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
+        for (int u = 0; u < 4; ++u) {
+            j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
+            fk[u] = k + u < k1 ? __ldg(&f[k + u]) : V(0);
+        }
 #pragma unroll
         for (int u = 0; u < 4; ++u) v[u] = j[u] >= 0 ? *(volatile const V*)&x[j[u]] : V(0);
 #pragma unroll
@@ -744,7 +764,7 @@ __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__
                 return false;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-            if (j[u] >= 0) sum += __ldg(&f[k + u]) * v[u];
+            if (j[u] >= 0) sum += fk[u] * v[u];
     }
     return true;
 }
@@ -1382,6 +1402,14 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_one(
 // SolverCG::solve (linear_solver.cu:440-515).  Per iteration: q = A p with p.q (one fused
 // barrier-reduction), x/r update, z = M^{-1} r with r.z (and r.r) (one fused
 // barrier-reduction), p = z + beta p (one barrier).
+// CG with ILU(0)/IC(0) on B's CSR arrays (pcg_csr) as a kernel of its own: the
+// iteration's code alone, so its loads can be batched without the other paths of k_pcg
+// competing for the 64 registers a thread has at two 512-thread blocks per SM.
+__global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_csr(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    pcg_csr(a, sh);
+}
+
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArgs a) {
     // read before the first barrier, so before the counter can advance
     const int ep_base = a.epoch ? *a.epoch : 0;
@@ -2598,13 +2626,15 @@ static int max_applies(const pf2_solver* S) {
 }
 
 // The kernel of a solve: GMRES, mixed CG, the one-reduction CG with a local (Jacobi or
-// no) preconditioner, or k_pcg (the standard iteration, and ILU/IC in either variant).
-static void* solve_kernel(const pf2_solver_options& o) {
+// no) preconditioner, k_pcg_csr (ILU/IC on B's CSR arrays, either variant) or k_pcg (the
+// standard iteration otherwise).
+static void* solve_kernel(const pf2_solver_options& o, bool csr) {
     if (o.kind == PF2_SOLVER_GMRES) return (void*)k_gmres;
     if (o.kind == PF2_SOLVER_BICGSTAB) return (void*)k_bicgstab;
     if (o.precision == PF2_PRECISION_MIXED) return (void*)k_pcg_mixed;
-    if (o.cg_variant == PF2_CG_ONE_REDUCTION && o.precond != PF2_PRECOND_ILU && o.precond != PF2_PRECOND_IC)
-        return (void*)k_pcg_one;
+    const bool tri = o.precond == PF2_PRECOND_ILU || o.precond == PF2_PRECOND_IC;
+    if (o.cg_variant == PF2_CG_ONE_REDUCTION && !tri) return (void*)k_pcg_one;
+    if (tri && csr) return (void*)k_pcg_csr;
     return (void*)k_pcg;
 }
 
@@ -2699,7 +2729,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         }
         return PF2_OK;
     }
-    void* fn = mixed ? (void*)k_pcg_mixed : solve_kernel(S->opt);
+    void* fn = mixed ? (void*)k_pcg_mixed : solve_kernel(S->opt, S->csr);
     // pipelined CG on B's CSR arrays (ILU(0)/IC(0) on a few-level order); the standard
     // iteration elsewhere
     if (!mixed && S->opt.kind == PF2_SOLVER_CG && S->opt.cg_variant == PF2_CG_PIPELINED && S->csr)
@@ -2764,7 +2794,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     if (uses_tri(S) && (s = build_tri_plan(S))) return fail(s);
     // the banded triangular solve keeps a range of the solution in shared memory
     S->smem = S->band_P ? sizeof(double) * (size_t)S->band_R : 0;
-    void* fn = solve_kernel(*opt);
+    void* fn = solve_kernel(*opt, S->csr);
     if (S->smem) {
         if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->smem) != cudaSuccess ||
             cudaFuncSetAttribute((void*)k_precond_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -74,6 +74,9 @@ def _run(case, steps, eng_solver, or_solver, tight=True, label=""):
                "cells_equal": bool(P["cell"].size == R["cell"].size and np.array_equal(P["cell"], R["cell"])),
                "counts_equal": bool(np.array_equal(np.bincount(P["cell"], minlength=tri.shape[0]),
                                                    np.bincount(R["cell"], minlength=tri.shape[0]))),
+               "count_cells_differ": int(np.count_nonzero(np.bincount(P["cell"], minlength=tri.shape[0]) !=
+                                                          np.bincount(R["cell"], minlength=tri.shape[0]))),
+               "cells": int(tri.shape[0]),
                "converged": (int(info.converged), int(oi.conv_ok))}
         for f in FIELDS:
             row[f] = rel_err(eng.field(f), ref.field(f))
@@ -82,9 +85,9 @@ def _run(case, steps, eng_solver, or_solver, tight=True, label=""):
             row["cy"] = abs(info.cy - oi.cy) / max(abs(oi.cy), 1e-300)
         row["x"] = float(np.abs(P["x"] - R["x"]).max()) if row["cells_equal"] else None
         rows.append(row)
-        print("%s step %d: particles %d, cells %s, counts %s, %s" % (
-            label, s + 1, row["particles"], "equal" if row["cells_equal"] else "DIFFER",
-            "equal" if row["counts_equal"] else "DIFFER",
+        print("%s step %d: particles %d (oracle %d), cells %s, counts %s (%d cells differ), %s" % (
+            label, s + 1, row["particles"], int(oi.particles), "equal" if row["cells_equal"] else "DIFFER",
+            "equal" if row["counts_equal"] else "DIFFER", row["count_cells_differ"],
             ", ".join("%s %.2e" % (k, row[k]) for k in FIELDS + ("cx", "cy") if k in row)), flush=True)
     return rows
 
@@ -110,15 +113,18 @@ def test_benchmarked_cylinder_configuration_matches_oracle(cuda):
 
 def test_benchmarked_cylinder_settings_as_run(cuda):
     """The same case at the benchmark's own stopping settings (absolute 1e-8, at most
-    1,000 iterations: the pressure solves stop at the limit).  Particle cells and counts
-    stay bit-exact over two steps; the fields differ by the rounding of two unconverged
-    CG runs, which the test bounds at 1e-6."""
+    1,000 iterations: the pressure solves stop at the limit, far from that test).  Two
+    unconverged CG runs that round differently end apart (3e-8 relative in the velocity
+    after the first step), and the particles advected through those fields may then
+    cross a cell edge differently: the first step's cells and counts are bit-exact, the
+    second step's counts agree in all but a few cells, and the fields stay within 1e-6."""
     rows = _run(_cylinder_quarter(), 2,
                 dict(pressure_ordering=1, prediction_solver=g.SOLVER_BICGSTAB),
                 dict(pressure_ordering=1, prediction_solver=2), tight=False,
                 label="cylinder_quarter bench-settings")
+    assert rows[0]["cells_equal"] and rows[0]["counts_equal"], rows[0]
+    assert rows[1]["count_cells_differ"] <= 1e-4 * rows[1]["cells"], rows[1]
     for row in rows:
-        assert row["cells_equal"] and row["counts_equal"], row
         for k in FIELDS + ("cx", "cy"):
             assert row[k] <= 1e-6, (k, row)
 

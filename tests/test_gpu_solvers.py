@@ -404,5 +404,6 @@ def test_bicgstab_restarts_an_orthogonal_shadow_residual(cuda):
     x = torch.zeros_like(b)
     info = g.LinearSolver(A, "bicgstab", "jacobi", tol=1e-12, maxit=500).solve(A, x, b)
     assert info.converged == 1 and info.iterations > 1
-    assert abs(info.iterations - oinfo.iterations) <= 2
+    # the dot products round differently (block sums against chunk sums): a few iterations
+    assert abs(info.iterations - oinfo.iterations) <= 5
     assert rel_err(x.cpu().numpy(), ox) < 1e-9
