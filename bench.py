@@ -468,6 +468,47 @@ def study_learned(args):
                       "criterion": "||b - A x|| <= 1e-8 ||b||", "results": res}))
 
 
+def parabola_error(xy, ux, uy, stations=(1.0, 2.0, 3.0, 3.5), umax=1.5, ly=1.0):
+    """Max |u - 4 umax y (ly - y) / ly^2| / umax and max |v| / umax over the nodes within
+    half a cell width of each station x (the analytic Poiseuille profile of the channel)."""
+    hx = 4.0 / 256
+    out = {}
+    for xs in stations:
+        sel = np.abs(xy[:, 0] - xs) < 0.5 * hx
+        y = xy[sel, 1]
+        exact = 4.0 * umax * y * (ly - y) / (ly * ly)
+        out["x=%g" % xs] = {"u": float(np.abs(ux[sel] - exact).max() / umax),
+                            "v": float(np.abs(uy[sel]).max() / umax), "nodes": int(sel.sum())}
+    return out
+
+
+def study_channel(args):
+    """The 4 x 1 channel at its stated size (256 x 64 quads, level 3, Scheme A, ILU(0),
+    dt 0.005, 200 steps from rest): ms per step and the velocity profile against the
+    analytic parabola at four stations along the channel, every 50 steps."""
+    import torch
+    import gpupfem2_gb300 as g
+    w, xy, tri, bu, bv, bp, prm = build_case("channel")
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(w["lx"], w["ly"], w["cyl"])
+    eng = g.FlowEngine(m, g.default_params(**prm), bu, bv, bp, capacity_factor=4.0)
+    eng.seed()
+    hist, times = [], []
+    for s in range(args.channel_steps):
+        _, ms = _timed(eng.step)
+        times.append(ms)
+        if (s + 1) % 50 == 0 or s + 1 == args.channel_steps:
+            info = eng.info()
+            hist.append({"step": s + 1, "t": round((s + 1) * prm["dt"], 4), "converged": int(info.converged),
+                         "particles": int(info.particles),
+                         "profile": parabola_error(xy, eng.field("ux"), eng.field("uy"))})
+    print(json.dumps({"study": "channel", "steps": args.channel_steps, "triangles": int(tri.shape[0]),
+                      "ms_per_step_median": statistics.median(times),
+                      "config": {"scheme": "A", "level": prm["level"], "pressure_precond": "ilu", "dt": prm["dt"],
+                                 "mu": prm["mu"], "inflow_umax": 1.5},
+                      "profile_vs_parabola": hist}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -492,7 +533,8 @@ def main():
     ap.add_argument("--ref-cuda-ic-steps", type=int, default=0,
                     help="timed steps of the reference CUDA build with its IC(0) pressure solver (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--study", default=None, choices=["solver", "learned"])
+    ap.add_argument("--study", default=None, choices=["solver", "learned", "channel"])
+    ap.add_argument("--channel-steps", type=int, default=200)
     ap.add_argument("--quick", action="store_true")
     ap.add_argument("--train", type=int, default=40)
     ap.add_argument("--eval", type=int, default=40)
@@ -501,7 +543,7 @@ def main():
     if args.study:
         import torch
         torch.cuda.set_device(0)
-        (study_solver if args.study == "solver" else study_learned)(args)
+        {"solver": study_solver, "learned": study_learned, "channel": study_channel}[args.study](args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -176,6 +176,7 @@ struct GridBarrier {
     int* err;
     double* part;  // 2 x 4 x gridDim per-block partial sums (grid_reduce)
     int* rec;      // where a wait gave up: {kind, a, b, c, d}, kind 0 = none
+    long long max_polls;  // polls of a barrier wait before it gives up; 0 = kBarrierPolls
 };
 
 constexpr long long kBarrierPolls = 1ll << 22;
@@ -213,10 +214,11 @@ __device__ __forceinline__ void arrive_release_gpu(unsigned* p) {
 __device__ __forceinline__ bool arrive_and_wait(const GridBarrier& b, unsigned c0, unsigned nblocks) {
     const unsigned target = (c0 / nblocks + 1) * nblocks;
     arrive_release_gpu(b.count);
+    const long long limit = b.max_polls > 0 ? b.max_polls : kBarrierPolls;
     long long polls = 0;
     unsigned c;
     while ((int)((c = ld_acquire_gpu(b.count)) - target) < 0) {
-        if (++polls > kBarrierPolls) {
+        if (++polls > limit) {
             atomicExch(b.err, (int)DEV_TIMEOUT);
             record_timeout(b.rec, 1, (int)blockIdx.x, (int)(c0 / nblocks), (int)c, 0);
             return false;

@@ -2098,6 +2098,7 @@ struct pf2_solver {
     pf2_solver_options opt{};
     const pf2_mesh* mesh = nullptr;
     int n = 0, nnz = 0, blocks = 0, m = 0;
+    long long barrier_polls = 0;  // PF2_BARRIER_POLLS (tests): a grid-barrier wait's poll limit
     DevBuf<double> r, z, p, q, s, invd, partial, V, H, vpart, rhat, yv, tv;
     DevBuf<unsigned> bar;  // count, gen
     DevBuf<int> err;
@@ -2665,7 +2666,7 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     a.t = S->tv.p;
     a.invd = S->invd.p;
     a.partial = S->partial.p;
-    a.bar = GridBarrier{ S->bar.p, S->err.p, S->partial.p, S->rec.p };
+    a.bar = GridBarrier{ S->bar.p, S->err.p, S->partial.p, S->rec.p, S->barrier_polls };
     a.T = tri_of(S);
     a.tol = S->opt.tolerance;
     a.maxit = S->opt.max_iterations;
@@ -2812,6 +2813,9 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     // blocks per SM: fewer blocks make cheaper grid barriers (one arrival atomic per block);
     // PF2_SOLVER_BLOCKS_PER_SM overrides the default of kSolverBlocksPerSm (tuning)
     int bps = kSolverBlocksPerSm;
+    // tests: a short grid-barrier poll limit, so that a bounded wait runs out and the
+    // solve returns PF2_TIMEOUT with the place it gave up
+    if (const char* e = getenv("PF2_BARRIER_POLLS")) S->barrier_polls = std::max(1LL, atoll(e));
     if (const char* e = getenv("PF2_SOLVER_BLOCKS_PER_SM")) bps = std::max(1, atoi(e));
     if (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_PIPELINED) {
         int occ_pp = 0;
@@ -3024,7 +3028,7 @@ extern "C" pf2_status pf2_pcg_jacobi_static(const pf2_csr* A, double* x, const d
     a.invd = base + 4 * (size_t)kStaticMaxRows;
     a.partial = base + 5 * (size_t)kStaticMaxRows;
     int* err = reinterpret_cast<int*>(w.words + 2);
-    a.bar = GridBarrier{ w.words, err, a.partial, reinterpret_cast<int*>(w.words + 3) };
+    a.bar = GridBarrier{ w.words, err, a.partial, reinterpret_cast<int*>(w.words + 3), 0 };
     a.tol = tolerance;
     a.maxit = max_iterations;
     a.criterion = criterion;

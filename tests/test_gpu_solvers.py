@@ -407,3 +407,26 @@ def test_bicgstab_restarts_an_orthogonal_shadow_residual(cuda):
     # the dot products round differently (block sums against chunk sums): a few iterations
     assert abs(info.iterations - oinfo.iterations) <= 5
     assert rel_err(x.cpu().numpy(), ox) < 1e-9
+
+
+def test_barrier_wait_that_runs_out_returns_timeout(cuda, monkeypatch):
+    """A grid-barrier wait bounded to one poll (PF2_BARRIER_POLLS, read when the solver
+    is created; a test knob) gives up before the other blocks arrive: the solve returns
+    PF2_TIMEOUT with the record of the block and barrier that gave up, nothing faults, and
+    a solver made afterwards with the normal limit solves on the same context."""
+    m, A, rp, col, val, rhs = _system(128, 32)
+    b = torch.tensor(rhs, device="cuda")
+    monkeypatch.setenv("PF2_BARRIER_POLLS", "1")
+    s = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=1000)
+    monkeypatch.delenv("PF2_BARRIER_POLLS")
+    x = torch.zeros_like(b)
+    with pytest.raises(g.Pf2Error) as e:
+        s.solve(A, x, b)
+    assert e.value.status == g.TIMEOUT
+    assert "grid barrier timed out in the solver (block" in str(e.value)
+    torch.cuda.synchronize()  # the context is still usable
+    x = torch.zeros_like(b)
+    info = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=1000).solve(A, x, b)
+    assert info.converged == 1 and info.status == 0
+    ox, _ = O.pcg(rp, col, val, rhs, tol=1e-8, maxit=1000, precond="jacobi")
+    assert rel_err(x.cpu().numpy(), ox) < 1e-6
