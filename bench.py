@@ -742,6 +742,21 @@ def main():
             if "ms_per_step" in rc:
                 rc["speedup_of_engine"] = rc["ms_per_step"] / ms
                 rc["target_speedup"] = 3.0
+                # the engine with the reference case's own solver choices (Jacobi CG for the
+                # pressure, GMRES(Jacobi) with modified Gram-Schmidt for the prediction), the
+                # same warm-up: the like-for-like ratio
+                same = dict(prm, pressure_precond=0, pressure_ordering=0, prediction_solver=1,
+                            gmres_orthogonalization=0, cg_variant=0)
+                e2 = g.FlowEngine(mesh, g.default_params(**same), bu, bv, bp, capacity_factor=4.0)
+                e2.seed()
+                for _ in range(args.warmup):
+                    e2.step()
+                torch.cuda.synchronize()
+                (_, ms2) = _timed(lambda: [e2.step() for _ in range(args.ref_cuda_steps)])
+                ms2 /= args.ref_cuda_steps
+                rc["engine_with_reference_solvers_ms_per_step"] = ms2
+                rc["speedup_of_engine_same_solvers"] = rc["ms_per_step"] / ms2
+                del e2
             line["reference_cuda"] = rc
         if rc is not None and args.ref_cuda_ic_steps > 0:
             ric = reference_cuda(args.workload, xy, tri, prm, "ic", 2, args.ref_cuda_ic_steps)

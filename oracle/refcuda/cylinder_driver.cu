@@ -232,13 +232,13 @@ int main(int argc, char* argv[])
     cudaDeviceSynchronize();
     auto wallTimed = std::chrono::steady_clock::now();
     double t = hostParams.dt;
+    timer.start();  // once, as the case does: stop() then gives each step's time
     for (int s = 0; s < warmup + steps; ++s, t += hostParams.dt) {
         if (s == warmup) {
             cudaDeviceSynchronize();
             wallTimed = std::chrono::steady_clock::now();
         }
         printf("\nTime step no. %d, time = %f\n", s + 1, t);
-        timer.start();
         cudaEventRecord(ev[0]);
         particleHandler.advectParticles(integrator.getVelocitySolution(), hostParams.dt,
                                         hostParams.particleAdvectionSubsteps);

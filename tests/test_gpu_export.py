@@ -93,8 +93,9 @@ def test_vtu_files_match_the_reference_writer(cuda, tmp_path):
     c = np.repeat(np.arange(nc), 4)
     w = np.stack([(k + 1.0) / (k + 6.0), 2.0 / (k + 6.0), 3.0 / (k + 6.0)], axis=1)
     pos = (w[:, :, None] * xy[tri[c]]).sum(axis=1)
-    P = {"x": pos[:, 0], "y": pos[:, 1], "l0": w[:, 0], "l1": w[:, 1], "l2": w[:, 2], "u": 0.5 * pos[:, 0],
-         "v": 0.25 * pos[:, 1] - 1.0, "cell": c.astype(np.int32)}
+    # the engine keeps l2 = 1 - l0 - l1 (the file holds positions and velocities only)
+    P = {"x": pos[:, 0], "y": pos[:, 1], "l0": w[:, 0], "l1": w[:, 1], "l2": 1.0 - w[:, 0] - w[:, 1],
+         "u": 0.5 * pos[:, 0], "v": 0.25 * pos[:, 1] - 1.0, "cell": c.astype(np.int32)}
     ph = g.ParticleHandler2D(m, 2)
     ph.upload(P)
     ppath = tmp_path / "particles.vtu"
