@@ -249,8 +249,8 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier& b, unsigned nblocks
 // released, warp 0 of every block adds all blocks' partials in the same fixed order
 // (lane l: partials l, l + 32, ... in increasing order, then a butterfly; lane 0's
 // total), so all blocks get the same bits whatever the arrival order.  Two arrays
-// suffice: a block can be at most one barrier ahead of the slowest reader of the other
-// array.  On return v holds the totals in every thread.  sh holds at least 33 * NV
+// suffice: a block can be at most one barrier ahead of the slowest reader of
+// the other array.  On return v holds the totals in every thread.  sh holds at least 33 * NV
 // doubles; part holds 2 x 4 x gridDim doubles.
 template <int NV>
 __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV], double* sh) {

@@ -636,26 +636,10 @@ __device__ __forceinline__ V spmv_rows(const Csr& A, const V* __restrict__ val, 
         int len = 0;
 #pragma unroll
         for (int u = 0; u < 4; ++u) len = max(len, e[u] - s[u]);
-        // two entries of each of the four rows per pass: the eight column and value loads
-        // go out together, then the eight vector loads, then the sums in entry order
-        for (int k = 0; k < len; k += 2) {
-            int j[8];
-            V w[8], x[8];
+        for (int k = 0; k < len; ++k) {
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const bool in = s[u] + k + h < e[u];
-                    j[2 * u + h] = in ? __ldg(&A.col[s[u] + k + h]) : -1;
-                    w[2 * u + h] = in ? __ldg(&val[s[u] + k + h]) : V(0);
-                }
-#pragma unroll
-            for (int t = 0; t < 8; ++t) x[t] = j[t] >= 0 ? __ldcg(&p[j[t]]) : V(0);
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int h = 0; h < 2; ++h)
-                    if (j[2 * u + h] >= 0) acc[u] += w[2 * u + h] * x[2 * u + h];
+                if (s[u] + k < e[u]) acc[u] += __ldg(&val[s[u] + k]) * __ldcg(&p[__ldg(&A.col[s[u] + k])]);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -740,21 +724,17 @@ __device__ __forceinline__ void p_update(V* p, const V* z, V beta, int r0, int r
 }
 
 // sum_k f_k x_{col_k} over the CSR entries [k0, k1) of a row whose x entries other
-// threads of the same sweep are still writing: four entries loaded together (columns and
-// factor values in one round trip, then the vector entries), only the pending ones polled
-// (bounded); terms added in entry order.
+// threads of the same sweep are still writing: four entries loaded together, only the
+// pending ones polled (bounded); terms added in entry order.
 template <class V>
 __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__ col, const V* __restrict__ f,
                                              int k0, int k1, int row, int* err, int* rec, V& sum) {
     sum = V(0);
     for (int k = k0; k < k1; k += 4) {
         int j[4];
-        V v[4], fk[4];
+        V v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
-            fk[u] = k + u < k1 ? __ldg(&f[k + u]) : V(0);
-        }
+        for (int u = 0; u < 4; ++u) j[u] = k + u < k1 ? __ldg(&col[k + u]) : -1;
 #pragma unroll
         for (int u = 0; u < 4; ++u) v[u] = j[u] >= 0 ? *(volatile const V*)&x[j[u]] : V(0);
 #pragma unroll
@@ -764,7 +744,7 @@ __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__
                 return false;
 #pragma unroll
         for (int u = 0; u < 4; ++u)
-            if (j[u] >= 0) sum += fk[u] * v[u];
+            if (j[u] >= 0) sum += __ldg(&f[k + u]) * v[u];
     }
     return true;
 }
