@@ -398,6 +398,71 @@ def study_solver(args):
     print(json.dumps({"study": "pressure_solver", "criterion": "||b - A x|| <= 1e-8 ||b||", "results": out}))
 
 
+def learned_metric(args, mesh, bu, bv, bp, prm):
+    """The second headline metric: pressure-solve time to ||b - A x|| <= 1e-8 ||b|| inside
+    the flow, mixed precision with the learned initial guess against the plain FP64 PCG
+    (the same IC(0) preconditioner on the multicolour order, previous pressure as the
+    start) and against mixed precision alone.  Each variant runs the same case from rest:
+    --learned-train steps (the network trains online on the plain solver's increments of
+    those steps), then --learned-eval timed steps.  For the mixed variants every eval
+    step's final pressure is compared with an FP64 re-solve of the same system
+    (||r|| <= 1e-12 ||b||, started from it): the mixed form's error per result."""
+    import ctypes
+    import torch
+    import gpupfem2_gb300 as g
+    L = g.lib()
+    base = dict(prm, pressure_criterion=1, pressure_tolerance=1e-8, pressure_max_iterations=20000,
+                learn_steps=args.learned_train, learn_rate=1e-3)
+    variants = [("fp64_plain", dict(pressure_precision=0, pressure_x0=0)),
+                ("mixed", dict(pressure_precision=1, pressure_x0=0)),
+                ("mixed_learned", dict(pressure_precision=1, pressure_x0=1))]
+    res = {}
+    for label, kw in variants:
+        eng = g.FlowEngine(mesh, g.default_params(**dict(base, **kw)), bu, bv, bp, capacity_factor=4.0)
+        eng.seed()
+        for _ in range(args.learned_train):
+            eng.step()
+        eng.info()
+        g._check(L.pf2_flow_enable_timing(eng.h, args.learned_eval), "timing")
+        its, errs, ratios, used = [], [], [], 0
+        ref_solver = None
+        for _ in range(args.learned_eval):
+            eng.step()
+            inf = eng.info()
+            its.append(sum(inf.it_pressure[k] for k in range(prm["n_outer"])))
+            used += inf.guess_used
+            if inf.guess_residual[0] > 0:
+                ratios.append(inf.guess_residual[1] / inf.guess_residual[0])
+            if kw["pressure_precision"] == 1:
+                A, rhs = eng.system(2)
+                if ref_solver is None:
+                    ref_solver = g.LinearSolver(A, "cg", "ic", tol=1e-12, maxit=20000, criterion=g.CRITERION_REL,
+                                                ordering=1)
+                p = _wrap(eng.field_ptr("p"), mesh.nv)
+                x = p.clone()
+                ref_solver.solve(A, x, _wrap(rhs, mesh.nv), check=False)
+                errs.append(float(torch.linalg.norm(p - x) / torch.linalg.norm(x)))
+        ph = (ctypes.c_double * 9)()
+        nst = ctypes.c_int()
+        g._check(L.pf2_flow_phase_times(eng.h, ph, ctypes.byref(nst)), "phase times")
+        res[label] = {"pressure_ms_per_step": ph[5] / max(nst.value, 1),
+                      "pressure_iterations_per_step": statistics.mean(its),
+                      "start_residual_ratio": statistics.mean(ratios) if ratios else None,
+                      "guess_used_steps": used}
+        if errs:
+            res[label]["p_rel_err_vs_fp64_resolve_max"] = max(errs)
+        del ref_solver, eng
+        torch.cuda.synchronize()
+    b0 = res["fp64_plain"]["pressure_ms_per_step"]
+    for v in res.values():
+        v["time_vs_fp64_plain"] = v["pressure_ms_per_step"] / b0
+    return {"value": res["mixed_learned"]["time_vs_fp64_plain"], "target": 0.5,
+            "criterion": "||b - A x|| <= 1e-8 ||b|| per pressure solve, IC(0) multicolour",
+            "protocol": "from rest: %d training steps, then %d timed steps per variant (the full protocol trains "
+                        "500 and evaluates 2,000)" % (args.learned_train, args.learned_eval),
+            "variants": res}
+
+
 def study_learned(args):
     """Cylinder flow: the pressure solve of each step (1e-8 relative residual) with the
     plain FP64 PCG against mixed precision alone and mixed precision with the learned
@@ -524,7 +589,11 @@ def main():
     ap.add_argument("--pred", type=int, default=None, help="prediction solver override (1 GMRES, 2 BiCGStab)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--clock-log", default=None, help="where the nvidia-smi clock samples go (default: a temp file)")
-    ap.add_argument("--ref-budget", type=float, default=120.0,
+    ap.add_argument("--learned-train", type=int, default=60,
+                    help="steps the learned initial guess trains before the metric's timed steps")
+    ap.add_argument("--learned-eval", type=int, default=20,
+                    help="timed steps of the mixed + learned metric (0: skip it)")
+    ap.add_argument("--ref-budget", type=float, default=90.0,
                     help="reference arm: seconds of timed oracle steps at most (at least one step)")
     ap.add_argument("--ref-algorithms", type=int, default=1,
                     help="reference arm: also time one step of the reference's own solver algorithms")
@@ -763,6 +832,8 @@ def main():
             if ric and "ms_per_step" in ric:
                 ric["speedup_of_engine"] = ric["ms_per_step"] / ms
             line["reference_cuda_ic"] = ric
+    if rank == 0 and args.learned_eval > 0 and args.workload in ("cylinder", "cylinder_quarter"):
+        line["metrics"]["pcg_mixed_learned_vs_fp64"] = learned_metric(args, mesh, bu, bv, bp, prm)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.workload, prm, eng, xy, tri, bu, bv, bp)
     if rank == 0:
