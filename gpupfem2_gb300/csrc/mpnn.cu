@@ -6,7 +6,8 @@
 //   l = 1..3:  m_i = mean_{j in N(i)} h_j ;  h = h + relu(W_l [h ; m] + c_l)
 //   y  = w4 . h + c4
 // Master parameters are FP32; the per-node MLPs run on the tensor cores with BF16
-// weights and activations and FP32 accumulation (mma.sync m16n8k16).  Training
+// weights and activations and FP32 accumulation: the forward layer on tcgen05 (tensor
+// memory accumulator, 128 nodes per CTA), the backward GEMMs on mma.sync m16n8k16.  Training
 // (backward and AdamW) runs on the device; gradients are summed in a fixed order.
 #include <cuda_bf16.h>
 
@@ -161,6 +162,178 @@ __global__ void __launch_bounds__(kMpnnThreads) k_mpnn_layer(Graph G, const floa
         bits |= __shfl_xor_sync(0xffffffffu, bits, 2);
         if (valid && t == 0) mask[i] = bits;
     }
+}
+
+// ------------------------------------------------ fifth-generation tensor cores
+// The layer GEMM on tcgen05: one thread issues tcgen05.mma (kind::f16, BF16 operands from
+// shared memory, FP32 accumulator in tensor memory), the CTA reads the accumulator back
+// with tcgen05.ld.  Operands sit in shared memory in the canonical K-major layout without
+// swizzle: 8-row x 16-byte core matrices, element (r, k) of an R-row tile at byte
+//   ((k / 8) * (R / 8) + r / 8) * 128 + (r % 8) * 16 + (k % 8) * 2,
+// so core matrices adjacent in K are R * 16 bytes apart (the descriptor's leading byte
+// offset) and those adjacent in rows 128 bytes apart (its stride byte offset).
+constexpr int kTcTile = 128;  // nodes per CTA: the MMA's M (accumulator lanes 0..127)
+constexpr long long kTcPolls = 1ll << 24;
+// Dynamic shared memory of k_mpnn_layer_tc: A (32 KB) in a 64 KB region, W (16 KB) in a
+// 24 KB region.  The MMAs read A within [start, start + 32 KB) and W within 16 KB; the
+// regions are larger so that the descriptors' reads stay inside the CTA's shared memory
+// whichever way the two offsets are read.
+constexpr int kTcRegionA = 64 * 1024;
+constexpr int kTcRegionB = 24 * 1024;
+constexpr int kTcSmem = kTcRegionA + kTcRegionB;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ int tc_offset(int r, int k, int rows) {
+    return ((k >> 3) * (rows >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// Shared-memory matrix descriptor (no swizzle, version 1): start, leading byte offset
+// (between core matrices adjacent in K), stride byte offset (adjacent in rows).
+__device__ __forceinline__ unsigned long long tc_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+    return (unsigned long long)((addr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major,
+// N and M as given.
+__host__ __device__ constexpr unsigned tc_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(n >> 3) << 17) | ((unsigned)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(unsigned tmem_d, unsigned long long a, unsigned long long b, unsigned idesc,
+                                       int accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        :
+        : "r"(tmem_d), "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(unsigned mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" : : "r"(mbar)
+                 : "memory");
+}
+
+// Bounded wait for phase `parity` of an mbarrier; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned mbar, unsigned parity) {
+    for (long long i = 0; i < kTcPolls; ++i) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 32 consecutive accumulator columns of this warp's 32 lanes: register j of lane l holds
+// row (lane base + l), column (col + j).
+__device__ __forceinline__ void tc_ld32(unsigned taddr, float (&v)[32]) {
+    unsigned r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,"
+        "%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// One layer as k_mpnn_layer, 128 nodes per CTA on tcgen05: h_out = h_in + relu(W [h ; m]
+// + c), m (for the backward pass) and the relu mask stored.  CTA = 4 warps; warp 0 holds
+// the 64 accumulator columns of tensor memory; thread 0 issues the eight K = 16 MMAs
+// (M = 128, N = 64); warp w reads back the rows 32 w .. 32 w + 31, one row per thread.
+// A wait that runs out sets *err and skips the outputs.
+__global__ void __launch_bounds__(128) k_mpnn_layer_tc(Graph G, const float* __restrict__ Hin,
+                                                       const __nv_bfloat16* __restrict__ Wb,
+                                                       const float* __restrict__ c, float* Hout, float* M,
+                                                       unsigned long long* mask, int* err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char* sA = tc_smem;               // [node][in], canonical layout
+    unsigned char* sB = tc_smem + kTcRegionA;  // W [out][in], canonical layout
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = blockIdx.x * kTcTile;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(MH));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    for (int q = threadIdx.x; q < MH * MK; q += blockDim.x) {
+        const int o = q / MK, k = q % MK;
+        *reinterpret_cast<__nv_bfloat16*>(sB + tc_offset(o, k, MH)) = Wb[q];
+    }
+    for (int q = threadIdx.x; q < kTcTile * MH; q += blockDim.x) {
+        const int r = q / MH, o = q % MH, i = base + r;
+        float h = 0.0f, m = 0.0f;
+        if (i < G.n) {
+            h = Hin[(size_t)i * MH + o];
+            gather_mean(G, Hin, i, o, m);
+            M[(size_t)i * MH + o] = m;
+        }
+        *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(r, o, kTcTile)) = __float2bfloat16_rn(h);
+        *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(r, MH + o, kTcTile)) = __float2bfloat16_rn(m);
+    }
+    // the operands written by threads become visible to the tensor cores' async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_slot;
+    if (threadIdx.x == 0) {
+        const unsigned a0 = smem_u32(sA), b0 = smem_u32(sB);
+        constexpr unsigned idesc = tc_idesc(kTcTile, MH);
+#pragma unroll
+        for (int ks = 0; ks < MK / 16; ++ks) {
+            const unsigned long long da = tc_desc(a0 + ks * 2 * (kTcTile * 16), kTcTile * 16, 128);
+            const unsigned long long db = tc_desc(b0 + ks * 2 * (MH * 16), MH * 16, 128);
+            tc_mma(tmem, da, db, idesc, ks > 0);
+        }
+        tc_commit(smem_u32(&mbar));
+    }
+    bool ok = mbar_wait(smem_u32(&mbar), 0);
+    if (!ok) {
+        if (lane == 0) atomicExch(err, (int)DEV_TIMEOUT);
+        mbar_wait(smem_u32(&mbar), 0);  // bounded: the MMAs may still be writing
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int r = warp * 32 + lane, i = base + r;
+        unsigned long long bits = 0ull;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            float acc[32];
+            tc_ld32(tmem + ((unsigned)(warp * 32) << 16) + half * 32, acc);
+            if (i < G.n) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int o = half * 32 + j;
+                    const float z = acc[j] + c[o];
+                    if (z > 0.0f) bits |= 1ull << o;
+                    Hout[(size_t)i * MH + o] = Hin[(size_t)i * MH + o] + (z > 0.0f ? z : 0.0f);
+                }
+            }
+        }
+        if (i < G.n) mask[i] = bits;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(MH));
 }
 
 // y = w4 . h + c4; optionally loss partials and dy = 2 (y - t) / n
@@ -410,8 +583,10 @@ struct pf2_mpnn {
     DevBuf<unsigned long long> mask;
     DevBuf<__nv_bfloat16> Wb;
     DevBuf<double> loss_part;
+    DevBuf<int> err;  // a tcgen05 wait that ran out (DEV_TIMEOUT)
     int step = 0;
     int wgrid = 0;
+    bool tc = true;  // the layer GEMMs on tcgen05 (PF2_MPNN_MMA=sync: mma.sync)
     Graph graph() const { return Graph{ n, mesh->rowptr.p, mesh->col.p, dinv.p }; }
     float* Hl(int l) { return H.p + (size_t)l * n * MH; }
     float* Ml(int l) { return M.p + (size_t)l * n * MH; }
@@ -445,9 +620,14 @@ static pf2_status mpnn_forward(pf2_mpnn* N, cudaStream_t st) {
     PF2_LAUNCH_CHECK();
     const unsigned tiles = blocks_for(N->n, kTile);
     for (int l = 0; l < ML; ++l) {
-        k_mpnn_layer<<<tiles, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Wb.p + (size_t)l * MH * MK,
-                                                     N->P.p + kParamLayer0 + l * kLayerSize + MH * MK, N->Hl(l + 1),
-                                                     N->Ml(l), N->maskl(l + 1));
+        if (N->tc)
+            k_mpnn_layer_tc<<<blocks_for(N->n, kTcTile), 128, kTcSmem, st>>>(
+                G, N->Hl(l), N->Wb.p + (size_t)l * MH * MK, N->P.p + kParamLayer0 + l * kLayerSize + MH * MK,
+                N->Hl(l + 1), N->Ml(l), N->maskl(l + 1), N->err.p);
+        else
+            k_mpnn_layer<<<tiles, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Wb.p + (size_t)l * MH * MK,
+                                                         N->P.p + kParamLayer0 + l * kLayerSize + MH * MK,
+                                                         N->Hl(l + 1), N->Ml(l), N->maskl(l + 1));
         PF2_LAUNCH_CHECK();
     }
     return PF2_OK;
@@ -507,8 +687,13 @@ pf2_status pf2_mpnn_create(const pf2_mesh* mesh, unsigned long long seed, pf2_mp
         (s = N->H.alloc((ML + 1) * n * MH)) || (s = N->M.alloc(ML * n * MH)) || (s = N->dH.alloc(n * MH)) ||
         (s = N->dH2.alloc(n * MH)) || (s = N->dSelf.alloc(n * MH)) || (s = N->dMs.alloc(n * MH)) ||
         (s = N->part.alloc(part)) || (s = N->mask.alloc((ML + 1) * n)) || (s = N->Wb.alloc(ML * MH * MK)) ||
-        (s = N->loss_part.alloc(blocks_for(N->n))))
+        (s = N->loss_part.alloc(blocks_for(N->n))) || (s = N->err.alloc(1)))
         return fail(s);
+    if (const char* e = getenv("PF2_MPNN_MMA")) N->tc = strcmp(e, "sync") != 0;
+    if (cudaMemset(N->err.p, 0, sizeof(int)) != cudaSuccess ||
+        cudaFuncSetAttribute((void*)k_mpnn_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
+            cudaSuccess)
+        return fail(cuda_fail(cudaGetLastError(), "mpnn set-up", __FILE__, __LINE__));
     // He-style initialisation from a splitmix64 stream (deterministic for a seed);
     // the output layer starts at zero so the untrained guess is the extrapolation alone
     std::vector<float> h(kParams, 0.0f);
@@ -571,6 +756,9 @@ pf2_status pf2_mpnn_set_params(pf2_mpnn* N, const float* params_host) {
 pf2_status pf2_mpnn_get_params(const pf2_mpnn* N, float* params_host, float* grad_host) {
     PF2_REQUIRE(N, PF2_BAD_INPUT, "null argument");
     PF2_CUDA(cudaDeviceSynchronize());
+    int e = 0;
+    PF2_CUDA(cudaMemcpy(&e, N->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    PF2_REQUIRE(e == 0, (pf2_status)e, "a tensor-core wait timed out in the network's forward pass");
     if (params_host) PF2_CUDA(cudaMemcpy(params_host, N->P.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
     if (grad_host) PF2_CUDA(cudaMemcpy(grad_host, N->grad.p, sizeof(float) * kParams, cudaMemcpyDeviceToHost));
     return PF2_OK;

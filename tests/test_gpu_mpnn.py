@@ -66,3 +66,32 @@ def test_training_lowers_the_loss_and_is_deterministic(cuda):
     losses = runs[0][0]
     assert losses[-1] < 0.25 * losses[0]
     assert runs[0][0] == runs[1][0] and np.array_equal(runs[0][1], runs[1][1])
+
+
+def test_tcgen05_layer_matches_mma_sync(cuda, monkeypatch):
+    """The forward layer on tcgen05 (tensor-memory accumulator, 128 nodes per CTA; the
+    default) against the mma.sync layer (PF2_MPNN_MMA=sync) on a graph whose last tile is
+    ragged: the same BF16 products summed in FP32 in another order."""
+    m, rp, col, feat, t = _case(64, 24)
+    assert m.nv % 128 != 0
+    rng = np.random.default_rng(4)
+    theta = None
+    outs = {}
+    f = torch.tensor(feat, dtype=torch.float32, device="cuda")
+    for mode in ("tcgen05", "sync"):
+        if mode == "sync":
+            monkeypatch.setenv("PF2_MPNN_MMA", "sync")
+        else:
+            monkeypatch.delenv("PF2_MPNN_MMA", raising=False)
+        net = g.LearnedGuess(m, seed=3)
+        if theta is None:
+            theta = rng.normal(scale=0.15, size=net.n_params).astype(np.float32)
+        net.set_params(theta)
+        y = torch.empty(m.nv, dtype=torch.float32, device="cuda")
+        net.forward(f, y)
+        net.params()  # synchronises and reports a tensor-core wait that ran out
+        outs[mode] = y.cpu().numpy()
+    assert np.isfinite(outs["tcgen05"]).all()
+    assert _nrel(outs["tcgen05"], outs["sync"]) < 1e-3
+    oy, _ = O.mpnn_forward(rp, col, feat.astype(np.float32).astype(np.float64), theta.astype(np.float64))
+    assert _nrel(outs["tcgen05"], oy) < 2e-2
