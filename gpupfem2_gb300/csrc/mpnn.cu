@@ -6,8 +6,9 @@
 //   l = 1..3:  m_i = mean_{j in N(i)} h_j ;  h = h + relu(W_l [h ; m] + c_l)
 //   y  = w4 . h + c4
 // Master parameters are FP32; the per-node MLPs run on the tensor cores with BF16
-// weights and activations and FP32 accumulation: the forward layer on tcgen05 (tensor
-// memory accumulator, 128 nodes per CTA), the backward GEMMs on mma.sync m16n8k16.  Training
+// weights and activations and FP32 accumulation on tcgen05 (accumulators in tensor
+// memory, 128 nodes per CTA); the mma.sync m16n8k16 kernels stay as the
+// PF2_MPNN_MMA=sync path.  Training
 // (backward and AdamW) runs on the device; gradients are summed in a fixed order.
 #include <cuda_bf16.h>
 
@@ -306,9 +307,11 @@ __global__ void __launch_bounds__(128) k_mpnn_layer_tc(Graph G, const float* __r
         }
         tc_commit(smem_u32(&mbar));
     }
-    bool ok = mbar_wait(smem_u32(&mbar), 0);
+    // every thread polls; the outcome is made block-uniform (the reads below are
+    // warp-collective)
+    const bool ok = __syncthreads_and(mbar_wait(smem_u32(&mbar), 0));
     if (!ok) {
-        if (lane == 0) atomicExch(err, (int)DEV_TIMEOUT);
+        if (threadIdx.x == 0) atomicExch(err, (int)DEV_TIMEOUT);
         mbar_wait(smem_u32(&mbar), 0);  // bounded: the MMAs may still be writing
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -334,6 +337,187 @@ __global__ void __launch_bounds__(128) k_mpnn_layer_tc(Graph G, const float* __r
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(MH));
+}
+
+// The CTA's tensor-memory columns (warp 0 allocates; power of two >= 32).
+__device__ __forceinline__ void tc_alloc(unsigned* slot, int cols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+}
+
+__device__ __forceinline__ void tc_dealloc(unsigned tmem, int cols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(cols));
+}
+
+__device__ __forceinline__ void tc_sync_in() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Backward node part on tcgen05: [dself ; dm] = dz W for 128 nodes per CTA (M = 128,
+// N = 128 inputs, K = 64 outputs in four MMAs); dz = dh * mask; dm scaled by 1 / d_i.
+// Operand regions of 48 KB each (16 KB used), as k_mpnn_layer_tc.
+constexpr int kTcBnRegion = 48 * 1024;
+constexpr int kTcBnSmem = 2 * kTcBnRegion;
+__global__ void __launch_bounds__(128) k_mpnn_layer_back_nodes_tc(Graph G, const float* __restrict__ dH,
+                                                                  const unsigned long long* __restrict__ mask,
+                                                                  const __nv_bfloat16* __restrict__ Wb, float* dSelf,
+                                                                  float* dMs, int* err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char* sA = tc_smem;                // dz [node][out]
+    unsigned char* sB = tc_smem + kTcBnRegion;  // W^T [in][out]
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_slot;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = blockIdx.x * kTcTile;
+    if (warp == 0) tc_alloc(&tmem_slot, MK);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    for (int q = threadIdx.x; q < MH * MK; q += blockDim.x) {
+        const int o = q / MK, k = q % MK;
+        *reinterpret_cast<__nv_bfloat16*>(sB + tc_offset(k, o, MK)) = Wb[q];
+    }
+    for (int q = threadIdx.x; q < kTcTile * MH; q += blockDim.x) {
+        const int r = q / MH, o = q % MH, i = base + r;
+        float v = 0.0f;
+        if (i < G.n && ((mask[i] >> o) & 1ull)) v = dH[(size_t)i * MH + o];
+        *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(r, o, kTcTile)) = __float2bfloat16_rn(v);
+    }
+    tc_sync_in();
+    const unsigned tmem = tmem_slot;
+    if (threadIdx.x == 0) {
+        const unsigned a0 = smem_u32(sA), b0 = smem_u32(sB);
+        constexpr unsigned idesc = tc_idesc(kTcTile, MK);
+#pragma unroll
+        for (int ks = 0; ks < MH / 16; ++ks)
+            tc_mma(tmem, tc_desc(a0 + ks * 2 * (kTcTile * 16), kTcTile * 16, 128),
+                   tc_desc(b0 + ks * 2 * (MK * 16), MK * 16, 128), idesc, ks > 0);
+        tc_commit(smem_u32(&mbar));
+    }
+    const bool ok = __syncthreads_and(mbar_wait(smem_u32(&mbar), 0));
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, (int)DEV_TIMEOUT);
+        mbar_wait(smem_u32(&mbar), 0);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int r = warp * 32 + lane, i = base + r;
+        const float di = i < G.n ? G.deg_inv[i] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < MK / 32; ++q) {
+            float acc[32];
+            tc_ld32(tmem + ((unsigned)(warp * 32) << 16) + q * 32, acc);
+            if (i < G.n) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int k = q * 32 + j;
+                    if (k < MH) dSelf[(size_t)i * MH + k] = acc[j];
+                    else dMs[(size_t)i * MH + (k - MH)] = acc[j] * di;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, MK);
+}
+
+// Backward weight part on tcgen05: per-CTA partial dW[out][in] = sum over the CTA's node
+// tiles of [h ; m]^T dz (M = 128 inputs, N = 64 outputs, K = 128 nodes per tile,
+// accumulated in tensor memory across the tiles) and dc on the CUDA cores.  A tile's
+// operands are overwritten only after its MMAs completed (mbarrier phase per tile).
+// Operand regions as k_mpnn_layer_tc.
+__global__ void __launch_bounds__(128) k_mpnn_layer_back_weights_tc(Graph G, const float* __restrict__ Hin,
+                                                                    const float* __restrict__ M,
+                                                                    const float* __restrict__ dH,
+                                                                    const unsigned long long* __restrict__ mask,
+                                                                    float* part, int* err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char* sA = tc_smem;               // [h ; m]^T [in][node]
+    unsigned char* sB = tc_smem + kTcRegionA;  // dz^T [out][node]
+    __shared__ __align__(8) unsigned long long mbar;
+    __shared__ unsigned tmem_slot;
+    __shared__ float sC[MH];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) tc_alloc(&tmem_slot, MH);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    for (int o = threadIdx.x; o < MH; o += blockDim.x) sC[o] = 0.0f;
+    const int ntiles = (G.n + kTcTile - 1) / kTcTile;
+    unsigned phase = 0;
+    bool ok = true, issued = false;
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int base = tile * kTcTile;
+        if (issued) {  // the previous tile's MMAs have read the operands
+            ok = __syncthreads_and(mbar_wait(smem_u32(&mbar), phase));
+            phase ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (!ok) break;
+        }
+        for (int q = threadIdx.x; q < kTcTile * MH; q += blockDim.x) {
+            const int r = q / MH, o = q % MH, i = base + r;
+            float h = 0.0f, m = 0.0f, z = 0.0f;
+            if (i < G.n) {
+                h = Hin[(size_t)i * MH + o];
+                m = M[(size_t)i * MH + o];
+                if ((mask[i] >> o) & 1ull) z = dH[(size_t)i * MH + o];
+            }
+            *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(o, r, MK)) = __float2bfloat16_rn(h);
+            *reinterpret_cast<__nv_bfloat16*>(sA + tc_offset(MH + o, r, MK)) = __float2bfloat16_rn(m);
+            *reinterpret_cast<__nv_bfloat16*>(sB + tc_offset(o, r, MH)) = __float2bfloat16_rn(z);
+        }
+        tc_sync_in();
+        // dc: the outputs' sums of the rounded dz over the tile's nodes
+        for (int o = threadIdx.x; o < MH; o += blockDim.x) {
+            float s = 0.0f;
+            for (int r = 0; r < kTcTile; ++r)
+                s += __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(sB + tc_offset(o, r, MH)));
+            sC[o] += s;
+        }
+        if (threadIdx.x == 0) {
+            const unsigned a0 = smem_u32(sA), b0 = smem_u32(sB);
+            constexpr unsigned idesc = tc_idesc(MK, MH);
+#pragma unroll
+            for (int ks = 0; ks < kTcTile / 16; ++ks)
+                tc_mma(tmem_slot, tc_desc(a0 + ks * 2 * (MK * 16), MK * 16, 128),
+                       tc_desc(b0 + ks * 2 * (MH * 16), MH * 16, 128), idesc, (issued || ks > 0) ? 1 : 0);
+            tc_commit(smem_u32(&mbar));
+        }
+        issued = true;
+        __syncthreads();  // sC complete before the next tile overwrites sB
+    }
+    if (issued && ok) {
+        ok = __syncthreads_and(mbar_wait(smem_u32(&mbar), phase));
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(err, (int)DEV_TIMEOUT);
+        if (issued) mbar_wait(smem_u32(&mbar), phase);
+    }
+    float* P = part + (size_t)blockIdx.x * (MH * MK + MH);
+    const unsigned tmem = tmem_slot;
+    const int in = warp * 32 + lane;  // accumulator lane = input row of dW^T
+#pragma unroll
+    for (int q = 0; q < MH / 32; ++q) {
+        float acc[32];
+        if (issued && ok) tc_ld32(tmem + ((unsigned)(warp * 32) << 16) + q * 32, acc);
+        else
+#pragma unroll
+            for (int j = 0; j < 32; ++j) acc[j] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) P[(q * 32 + j) * MK + in] = acc[j];
+    }
+    __syncthreads();
+    for (int o = threadIdx.x; o < MH; o += blockDim.x) P[MH * MK + o] = sC[o];
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) tc_dealloc(tmem, MH);
 }
 
 // y = w4 . h + c4; optionally loss partials and dy = 2 (y - t) / n
@@ -645,13 +829,22 @@ static pf2_status mpnn_backward(pf2_mpnn* N, cudaStream_t st) {
     float* dh2 = N->dH2.p;
     for (int l = ML - 1; l >= 0; --l) {
         const __nv_bfloat16* W = N->Wb.p + (size_t)l * MH * MK;
-        k_mpnn_layer_back_weights<<<N->wgrid, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Ml(l), dh, N->maskl(l + 1),
-                                                                     N->part.p);
+        if (N->tc)
+            k_mpnn_layer_back_weights_tc<<<N->wgrid, 128, kTcSmem, st>>>(G, N->Hl(l), N->Ml(l), dh, N->maskl(l + 1),
+                                                                         N->part.p, N->err.p);
+        else
+            k_mpnn_layer_back_weights<<<N->wgrid, kMpnnThreads, 0, st>>>(G, N->Hl(l), N->Ml(l), dh,
+                                                                         N->maskl(l + 1), N->part.p);
         PF2_LAUNCH_CHECK();
         k_reduce_cols<<<blocks_for(kLayerSize), kThreads, 0, st>>>(N->part.p, N->wgrid, kLayerSize, N->grad.p,
                                                                    kParamLayer0 + l * kLayerSize);
         PF2_LAUNCH_CHECK();
-        k_mpnn_layer_back_nodes<<<tiles, kMpnnThreads, 0, st>>>(G, dh, N->maskl(l + 1), W, N->dSelf.p, N->dMs.p);
+        if (N->tc)
+            k_mpnn_layer_back_nodes_tc<<<blocks_for(N->n, kTcTile), 128, kTcBnSmem, st>>>(
+                G, dh, N->maskl(l + 1), W, N->dSelf.p, N->dMs.p, N->err.p);
+        else
+            k_mpnn_layer_back_nodes<<<tiles, kMpnnThreads, 0, st>>>(G, dh, N->maskl(l + 1), W, N->dSelf.p,
+                                                                    N->dMs.p);
         PF2_LAUNCH_CHECK();
         k_mpnn_agg_back<<<blocks_for((long long)N->n * MH), kThreads, 0, st>>>(G, dh, N->dSelf.p, N->dMs.p, dh2);
         PF2_LAUNCH_CHECK();
@@ -692,7 +885,11 @@ pf2_status pf2_mpnn_create(const pf2_mesh* mesh, unsigned long long seed, pf2_mp
     if (const char* e = getenv("PF2_MPNN_MMA")) N->tc = strcmp(e, "sync") != 0;
     if (cudaMemset(N->err.p, 0, sizeof(int)) != cudaSuccess ||
         cudaFuncSetAttribute((void*)k_mpnn_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem) !=
-            cudaSuccess)
+            cudaSuccess ||
+        cudaFuncSetAttribute((void*)k_mpnn_layer_back_nodes_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTcBnSmem) != cudaSuccess ||
+        cudaFuncSetAttribute((void*)k_mpnn_layer_back_weights_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             kTcSmem) != cudaSuccess)
         return fail(cuda_fail(cudaGetLastError(), "mpnn set-up", __FILE__, __LINE__));
     // He-style initialisation from a splitmix64 stream (deterministic for a seed);
     // the output layer starts at zero so the untrained guess is the extrapolation alone
