@@ -154,3 +154,28 @@ def test_channel_at_its_stated_size_matches_oracle(cuda):
     Scheme A, ILU(0) pressure, converged solves; three steps against the oracle."""
     rows = _run(_channel(256, 64, 0, 1, 3), 3, dict(), dict(), label="channel256x64 scheme A ILU(0)")
     _assert_rows(rows)
+
+
+def test_channel_keeps_the_poiseuille_profile(cuda):
+    """Started on the analytic parabola u = 6 y (1 - y) (the steady solution of the 4 x 1
+    channel with the inflow profile of Umax 1.5), 60 steps of the 128 x 32 channel (level
+    3, Scheme A, ILU(0)) keep it: |u - parabola| / Umax below 2 % and |v| / Umax below 1 %
+    at every node away from the outlet's last cell column."""
+    xy, tri, (bu, bv, bp), (lx, ly, cyl), eng_kw, _ = _channel(128, 32, 0, 1, 3)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    m.set_channel_boundary_ids(lx, ly, cyl)
+    eng = g.FlowEngine(m, g.default_params(**eng_kw), bu, bv, bp, capacity_factor=4.0)
+    y = xy[:, 1]
+    exact = 6.0 * y * (1.0 - y)
+    eng.set_field("ux", exact)
+    eng.seed()
+    for _ in range(60):
+        eng.step()
+        assert eng.info().converged == 1
+    ux, uy = eng.field("ux"), eng.field("uy")
+    keep = xy[:, 0] < lx - 4.0 / 128
+    du = np.abs(ux - exact)[keep].max() / 1.5
+    dv = np.abs(uy)[keep].max() / 1.5
+    print("channel128x32 from the parabola, 60 steps: max |u - parabola| / Umax %.2e, max |v| / Umax %.2e"
+          % (du, dv))
+    assert du < 2e-2 and dv < 1e-2
