@@ -544,6 +544,35 @@ struct SolveOut {
     double relres;  // ||r|| / ||b|| at the end (the iterated residual; the true one for MIXED)
 };
 
+// ------------------------------------------------------------ partitioned CG
+// CG with the rows cut into one part per block (a breadth-first recursive bisection of the
+// matrix graph, one block per SM): a part's rows are consecutive in the part order Q (by
+// part, then sweep group, then B's order), and their r, p, q, t, z live in the block's
+// shared memory for the whole solve.  Only a part's boundary rows (rows with a neighbour in
+// another part) go through global memory: their p (read by neighbours' SpMV after a grid
+// barrier) and their forward and backward results t and z (read by neighbours' sweeps,
+// polled on the pending marker as in the CSR sweeps).  Inside a part the sweep groups
+// (colours) follow one another behind a __syncthreads.  Each row's arithmetic (SpMV entry
+// order, sweep sums, vector updates) is that of k_pcg (Jacobi / none) and pcg_csr
+// (ILU(0) / IC(0) on B); the reductions sum the blocks' rows in another order.
+struct PartCg {
+    int P;                    // parts (the grid's blocks)
+    int R;                    // rows of the largest part (shared-memory vector length)
+    int ng;                   // sweep groups per part (1 with Jacobi / none)
+    const int* qs;            // group starts: part p group g holds rows qs[p ng + g] .. qs[p ng + g + 1]
+    const int* rp;            // CSR in Q order, each row's entries in B's (or A's) order
+    const int* col;
+    const int* diag;
+    const int* qa;            // Q row -> row of A
+    const unsigned char* bnd; // 1: the row has a neighbour in another part
+    const double* val;        // A's values in Q order (gathered per solve)
+    const double* f;          // factors in Q order (B's fsym layout: L left, upper right, 1 / pivot on the diagonal)
+    double* x;                // x in Q order (the solve's iterate)
+    double* gp;               // boundary rows' p, t, z (t and z start as the pending marker)
+    double* gt;
+    double* gz;
+};
+
 struct KArgs {
     Csr A;
     int precond;
@@ -576,6 +605,7 @@ struct KArgs {
     double* pipe;  // pipelined CG: u, w, z and three m arrays (6 n)
     double inner_eta;     // inner solves stop at ||r_inner|| <= eta ||r_outer||
     int max_outer;
+    PartCg part;  // partitioned CG (k_pcg_part)
 };
 
 __device__ __forceinline__ void row_range(int n, int& r0, int& r1) {
@@ -757,8 +787,8 @@ __device__ __forceinline__ bool csr_dot_wait(const V* x, const int* __restrict__
 // x += alpha p, r -= alpha q (q = A p); MODE 2 (one-reduction CG, q = A z) p = z + beta p,
 // s = q + beta s, x += alpha p, r -= alpha s (first: p = z, s = q).  Writes the forward
 // result and resets the row of z to the pending marker for the backward sweep.  Returns
-// the thread's r.r terms (x) and t.t terms of the forward result t (y): with IC(0),
-// t = L^{-1} r and z = L^{-T} t, so r.z = t.t.
+// the thread's r.r terms (x; zero unless want_rr) and t.t terms of the forward result t
+// (y): with IC(0), t = L^{-1} r and z = L^{-T} t, so r.z = t.t.
 template <class V> struct CsrVecs;
 template <> struct CsrVecs<double> {
     __device__ static double* tmp(const Tri& T) { return T.tmp; }
@@ -771,7 +801,7 @@ template <> struct CsrVecs<float> {
 
 template <int MODE, class V = double>
 __device__ double2 csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, const V* q, V* x, V* p, V* sv, V* z,
-                           int* err) {
+                           int* err, bool want_rr = true) {
     V* tmp = CsrVecs<V>::tmp(T);
     const V* fsym = CsrVecs<V>::fsym(T);
     const int n = T.B.n;
@@ -810,7 +840,7 @@ __device__ double2 csr_fwd(const Tri& T, V alpha, V beta, bool first, V* r, cons
             ra -= alpha * sr;
             __stcg(&r[row], ra);
         }
-        rr += (double)ra * (double)ra;
+        if (want_rr) rr += (double)ra * (double)ra;
         V sum;
         if (!csr_dot_wait(tmp, T.B.col, fsym, k0, d, row, err, T.rec, sum)) break;
         const V v = unit ? ra - sum : (ra - sum) * __ldg(&fsym[d]);
@@ -958,23 +988,41 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
             // IC(0): r.z = |L^{-1} r|^2 is known after the forward sweep, so one reduction
             // of r.z and r.r follows it and the backward sweep carries the direction update
             // (three barriers per iteration)
-            const double2 f = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err);
-            double gt[2] = { f.y, f.x };
-            if (!grid_reduce<2>(a.bar, gt, sh)) return;
-            rr = gt[1];
-            if (done_test(gt[0], rr)) { gamma = gt[0]; conv = true; break; }
-            beta = gt[0] / gamma;
-            gamma = gt[0];
+            // with the absolute criterion (a test of r.z alone) r.r is not formed per
+            // iteration: one FP64 term per row and one reduced value fewer; it is
+            // reduced once after the loop
+            const double2 f = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err,
+                                                 rel);
+            double tt;
+            if (rel) {
+                double gt[2] = { f.y, f.x };
+                if (!grid_reduce<2>(a.bar, gt, sh)) return;
+                tt = gt[0];
+                rr = gt[1];
+            } else {
+                double gt[1] = { f.y };
+                if (!grid_reduce<1>(a.bar, gt, sh)) return;
+                tt = gt[0];
+            }
+            if (done_test(tt, rr)) { gamma = tt; conv = true; break; }
+            beta = tt / gamma;
+            gamma = tt;
             csr_bwd<double, true>(T, nullptr, a.z, pc, a.bar.err, beta);
             if (!grid_sync(a.bar, gridDim.x)) return;
             continue;
         }
-        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err).x;
+        g2[1] = csr_fwd<1, double>(T, alpha, 0.0, false, a.r, a.q, xB, pc, nullptr, a.z, a.bar.err, rel).x;
         if (!grid_sync(a.bar, gridDim.x)) return;
         g2[0] = csr_bwd<double>(T, a.r, a.z, nullptr, a.bar.err);
-        if (!grid_reduce<2>(a.bar, g2, sh)) return;
+        if (rel) {
+            if (!grid_reduce<2>(a.bar, g2, sh)) return;
+            rr = g2[1];
+        } else {
+            double g1[1] = { g2[0] };
+            if (!grid_reduce<1>(a.bar, g1, sh)) return;
+            g2[0] = g1[0];
+        }
         const double gnew = g2[0];
-        rr = g2[1];
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
         beta = gnew / gamma;
         gamma = gnew;
@@ -982,6 +1030,16 @@ __device__ void pcg_csr(const KArgs& a, double* sh) {
             p_update(pc, a.z, beta, r0, r1);
             if (!grid_sync(a.bar, gridDim.x)) return;
         }
+    }
+    // the absolute criterion left r.r out of the iterations: the final residual's norm
+    if (!rel && !one && it > 0) {
+        double f[1] = { 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double ri = __ldcg(&a.r[i]);
+            f[0] += ri * ri;
+        }
+        if (!grid_reduce<1>(a.bar, f, sh)) return;
+        rr = f[0];
     }
     // every x update happened before the last reduction's barrier
     for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) a.x[__ldg(&T.perm[i])] = __ldcg(&xB[i]);
@@ -1374,6 +1432,364 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_pipe
     }
 }
 
+// The part's shared memory: r, p, q and t of its rows (Jacobi / none: t = 1 / a_ii and a
+// separate z; ILU / IC: z shares t's array, since a row's forward result is dead once the
+// backward sweep has read it and the backward sweep reads only its own row's t), the
+// reduction scratch, and (kPartMetaSmem) the rows' entry ranges, diagonal positions and
+// boundary flags.  x stays in global memory: the smaller shared-memory carve-out leaves
+// more of the SM's 256 KB to the L1 that caches the matrix and factor streams (measured:
+// IC(0) CG at 499,288 rows 57.9 us per iteration with x in shared memory, 51.7 without).
+struct PartSm {
+    double *r, *p, *q, *t, *z, *red;
+    const int* rp;   // np + 1 absolute entry positions
+    const int* dg;   // diagonal positions
+    const unsigned char* bnd;
+};
+
+constexpr int kPartThreads = 1024;  // one block per SM
+constexpr bool kPartMetaSmem = true;
+
+// Shared-memory bytes of a part of R rows (the layout of part_sm; tri: z shares t).
+__host__ __device__ constexpr size_t part_smem_bytes(int R, bool tri) {
+    return sizeof(double) * ((tri ? 4 : 5) * (size_t)R + 2 * kPartThreads) +
+           (kPartMetaSmem ? sizeof(int) * (2 * (size_t)R + 1) + (size_t)R : 0);
+}
+
+__device__ __forceinline__ PartSm part_sm(const PartCg& C, double* base, int R, bool tri, int p0) {
+    PartSm S;
+    S.r = base;
+    S.p = base + R;
+    S.q = base + 2 * R;
+    S.t = base + 3 * R;
+    S.z = tri ? S.t : base + 4 * R;
+    S.red = base + (tri ? 4 : 5) * R;
+    if (kPartMetaSmem) {
+        int* rp = reinterpret_cast<int*>(S.red + 2 * kPartThreads);
+        S.rp = rp;
+        S.dg = rp + R + 1;
+        S.bnd = reinterpret_cast<const unsigned char*>(rp + 2 * R + 1);
+    } else {
+        S.rp = C.rp + p0;
+        S.dg = C.diag + p0;
+        S.bnd = C.bnd + p0;
+    }
+    return S;
+}
+
+// Grid-wide sums of NV <= 2 values, fused with the grid barrier, for blocks of
+// kPartThreads threads (a multiple of 128, at most 1024).  The block's values go to shared
+// memory and a fixed tree adds them with few FP64 instructions (one FP64 warp instruction
+// per ~64 clocks on an SM sub-partition, against five per value in every warp for warp
+// butterflies): a quarter of the threads per value add 4 values each, a sixteenth add 4 of
+// those, one warp adds up to 2 and finishes with a butterfly.  Thread 0 stores the block
+// sums in one of two partial arrays (by the barrier's parity) and arrives on the grid
+// barrier; after the release warp j adds value j's partials in block order (lane l:
+// partials l, l + 32, ...; butterfly).  The order depends on no arrival order: the sums
+// are reproducible bit for bit.
+template <int NV>
+__device__ __forceinline__ bool part_reduce(const GridBarrier& b, double (&v)[NV], double* sh, double* red) {
+    static_assert(NV >= 1 && NV <= 2, "part_reduce sums one or two values");
+    static_assert(kPartThreads % 128 == 0 && kPartThreads <= 1024, "block size of the tree");
+    __shared__ int s_ok, s_par;
+    constexpr int BT = kPartThreads;
+    const unsigned G = gridDim.x;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    unsigned c0 = 0;
+    if (tid == 0) c0 = ld_relaxed_gpu(b.count);
+    __syncthreads();  // the previous call's readers of red and sh are done
+#pragma unroll
+    for (int j = 0; j < NV; ++j) red[j * BT + tid] = v[j];
+    __syncthreads();
+    if (tid < NV * (BT / 4)) {
+        const int j = tid / (BT / 4), u = tid % (BT / 4);
+        double* c = red + j * BT + u;
+        c[0] = ((c[0] + c[BT / 4]) + c[BT / 2]) + c[3 * BT / 4];
+    }
+    __syncthreads();
+    if (tid < NV * (BT / 16)) {
+        const int j = tid / (BT / 16), u = tid % (BT / 16);
+        double* c = red + j * BT + u;
+        c[0] = ((c[0] + c[BT / 16]) + c[BT / 8]) + c[3 * BT / 16];
+    }
+    __syncthreads();
+    if (w < NV) {
+        const double s = warp_sum(red[w * BT + lane] + (lane + 32 < BT / 16 ? red[w * BT + lane + 32] : 0.0));
+        if (lane == 0) sh[w] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned kb = c0 / G;
+        double* part = b.part + (size_t)(kb & 1u) * 4 * G;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], sh[j]);
+        s_ok = arrive_and_wait(b, c0, G) ? 1 : 0;
+        s_par = (int)(kb & 1u);
+    }
+    __syncthreads();
+    if (w < NV) {
+        const double* part = b.part + (size_t)s_par * 4 * G + w * G;
+        double t = 0.0;
+        for (unsigned q = lane; q < G; q += 32) t += __ldcg(&part[q]);
+        t = warp_sum(t);
+        if (lane == 0) sh[16 + w] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = sh[16 + j];
+    return s_ok != 0;
+}
+
+// v[j] for row j of a sweep: the part's own rows from shared memory, other parts' rows
+// from the global copy, polled on the pending marker (bounded).  A failed wait records
+// DEV_TIMEOUT and yields 0: the caller goes on to the next __syncthreads and the kernel
+// returns at its next grid barrier.
+__device__ __forceinline__ double part_dep(int j, int p0, int np, const double* sv, const double* gv, int* err,
+                                           int* rec, int row) {
+    if ((unsigned)(j - p0) < (unsigned)np) return sv[j - p0];
+    double v = *(volatile const double*)&gv[j];
+    if (Pending<double>::bits(v) == Pending<double>::kBits && !wait_value(gv, j, v, err, rec, row)) v = 0.0;
+    return v;
+}
+
+// q = A p over the part's rows (each row's entries in order, as spmv_rows); other parts'
+// p from the global copy.  Returns the thread's p.q terms.
+__device__ __forceinline__ double part_spmv(const PartCg& C, const PartSm& S, int p0, int np) {
+    double pq = 0.0;
+    for (int l = threadIdx.x; l < np; l += kPartThreads) {
+        const int s = S.rp[l], e = S.rp[l + 1];
+        double acc = 0.0;
+        for (int k = s; k < e; ++k) {
+            const int j = __ldg(&C.col[k]);
+            const double pj = (unsigned)(j - p0) < (unsigned)np ? S.p[j - p0] : __ldcg(&C.gp[j]);
+            acc += __ldg(&C.val[k]) * pj;
+        }
+        S.q[l] = acc;
+        pq += S.p[l] * acc;
+    }
+    return pq;
+}
+
+// A sweep row's dependency entries and pivot pulled into L1 before the group's barrier
+// (they do not depend on the earlier groups).
+__device__ __forceinline__ void sweep_prefetch(const PartCg& C, int k0, int k1, int d) {
+    if (k1 > k0) {
+        prefetch_l1(&C.col[k0]);
+        prefetch_l1(&C.f[k0]);
+    }
+    prefetch_l1(&C.f[d]);
+}
+
+// sum_k f_k v[col_k] over the dependency entries [k0, k1), in entry order.
+__device__ __forceinline__ double sweep_sum(const PartCg& C, int k0, int k1, int p0, int np, const double* sv,
+                                            const double* gv, int* err, int* rec, int row) {
+    double sum = 0.0;
+    for (int k = k0; k < k1; ++k) sum += __ldg(&C.f[k]) * part_dep(__ldg(&C.col[k]), p0, np, sv, gv, err, rec, row);
+    return sum;
+}
+
+// Forward sweep over the part's groups (csr_fwd): first: t = L^{-1} r; else first the
+// updates r -= alpha q, x += alpha p.  Returns the r.r terms (want_rr) and the t.t terms.
+template <bool IC>
+__device__ double2 part_fwd(const PartCg& C, const PartSm& S, int p0, int np, bool first, double alpha, bool want_rr,
+                            int* err, int* rec) {
+    double rr = 0.0, tt = 0.0;
+    const int* qs = C.qs + blockIdx.x * C.ng;
+    for (int g = 0; g < C.ng; ++g) {
+        const int g0 = qs[g] - p0, g1 = qs[g + 1] - p0;
+        if (g0 + (int)threadIdx.x < g1) {
+            const int l = g0 + threadIdx.x;
+            sweep_prefetch(C, S.rp[l], S.dg[l], S.dg[l]);
+        }
+        __syncthreads();  // the part's earlier groups are done
+        for (int l = g0 + threadIdx.x; l < g1; l += kPartThreads) {
+            const int d = S.dg[l];
+            double ra = S.r[l];
+            if (!first) {
+                ra -= alpha * S.q[l];
+                S.r[l] = ra;
+            }
+            if (want_rr) rr += ra * ra;
+            const double sum = sweep_sum(C, S.rp[l], d, p0, np, S.t, C.gt, err, rec, p0 + l);
+            const double v = IC ? (ra - sum) * __ldg(&C.f[d]) : ra - sum;
+            S.t[l] = v;
+            if (S.bnd[l]) {
+                __stcg(&C.gt[p0 + l], v);
+                __stcg(&C.gz[p0 + l], Pending<double>::marker());
+            }
+            tt += v * v;
+            // x += alpha p last: its global load is off the sweep's dependency chain
+            if (!first) __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + alpha * S.p[l]);
+        }
+    }
+    return make_double2(rr, tt);
+}
+
+// Backward sweep over the part's groups in reverse (csr_bwd): z = U^{-1} t; PMODE 0: no
+// direction, 1: p = z (the first), 2: p = z + beta p (IC's three-step iteration).
+// Returns the r.z terms (PMODE != 2).
+template <int PMODE>
+__device__ double part_bwd(const PartCg& C, const PartSm& S, int p0, int np, double beta, int* err, int* rec) {
+    double rz = 0.0;
+    const int* qs = C.qs + blockIdx.x * C.ng;
+    for (int g = C.ng - 1; g >= 0; --g) {
+        const int g0 = qs[g] - p0, g1 = qs[g + 1] - p0;
+        if (g0 + (int)threadIdx.x < g1) {
+            const int l = g0 + threadIdx.x;
+            sweep_prefetch(C, S.dg[l] + 1, S.rp[l + 1], S.dg[l]);
+        }
+        __syncthreads();  // the part's later groups are done
+        for (int l = g0 + threadIdx.x; l < g1; l += kPartThreads) {
+            const int d = S.dg[l];
+            const double in = S.t[l];
+            const double sum = sweep_sum(C, d + 1, S.rp[l + 1], p0, np, S.z, C.gz, err, rec, p0 + l);
+            const double v = (in - sum) * __ldg(&C.f[d]);
+            S.z[l] = v;
+            double pn = 0.0;
+            if (PMODE == 1) pn = v;
+            if (PMODE == 2) pn = fma_rn(beta, S.p[l], v);
+            if (PMODE) S.p[l] = pn;
+            if (S.bnd[l]) {
+                __stcg(&C.gz[p0 + l], v);
+                if (PMODE) __stcg(&C.gp[p0 + l], pn);
+                __stcg(&C.gt[p0 + l], Pending<double>::marker());
+            }
+            if (PMODE != 2) rz += S.r[l] * v;
+        }
+    }
+    return rz;
+}
+
+// MODE 0: Jacobi or no preconditioner (k_pcg's iteration: p.q reduction, x/r/z update
+// with r.z, p update and barrier); 1: IC(0) (pcg_csr's three grid-wide steps); 2: ILU(0)
+// (pcg_csr's four).
+template <int MODE>
+__device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
+    const PartCg& C = a.part;
+    const int p0 = C.qs[blockIdx.x * C.ng], p1 = C.qs[(blockIdx.x + 1) * C.ng], np = p1 - p0;
+    const PartSm S = part_sm(C, smem, C.R, MODE != 0, p0);
+    const int tid = threadIdx.x;
+    int* err = a.bar.err;
+    int* rec = a.bar.rec;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    const bool jac = a.precond == PF2_PRECOND_JACOBI;
+    for (int l = tid; l < np; l += kPartThreads) {
+        const int i = p0 + l;
+        if (kPartMetaSmem) {
+            const_cast<int*>(S.rp)[l] = __ldg(&C.rp[i]);
+            const_cast<int*>(S.dg)[l] = __ldg(&C.diag[i]);
+            const_cast<unsigned char*>(S.bnd)[l] = __ldg(&C.bnd[i]);
+        }
+        __stcg(&C.x[i], a.x[__ldg(&C.qa[i])]);
+    }
+    if (kPartMetaSmem && tid == 0) const_cast<int*>(S.rp)[np] = __ldg(&C.rp[p1]);
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    double red[3] = { 0.0, 0.0, 0.0 };  // r.z, b.b, r.r
+    for (int l = tid; l < np; l += kPartThreads) {
+        const double bi = a.b[__ldg(&C.qa[p0 + l])];
+        double v = 0.0;
+        for (int k = S.rp[l]; k < S.rp[l + 1]; ++k) v += __ldg(&C.val[k]) * __ldcg(&C.x[__ldg(&C.col[k])]);
+        S.r[l] = bi - v;
+        red[1] += bi * bi;
+        if (MODE == 0) S.t[l] = 1.0 / __ldg(&C.val[S.dg[l]]);
+    }
+    __syncthreads();
+    if (MODE == 0) {
+        for (int l = tid; l < np; l += kPartThreads) {
+            const double ri = S.r[l];
+            const double zi = jac ? ri * S.t[l] : ri;
+            S.z[l] = zi;
+            S.p[l] = zi;
+            if (S.bnd[l]) __stcg(&C.gp[p0 + l], zi);
+            red[0] += ri * zi;
+            red[2] += ri * ri;
+        }
+    } else {
+        red[2] = part_fwd<MODE == 1>(C, S, p0, np, true, 0.0, true, err, rec).x;
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        red[0] = part_bwd<1>(C, S, p0, np, 0.0, err, rec);
+    }
+    double r2[2] = { red[0], red[1] }, r1[1] = { red[2] };
+    if (!part_reduce<2>(a.bar, r2, sh, S.red) || !part_reduce<1>(a.bar, r1, sh, S.red)) return;
+    double gamma = r2[0];
+    const double bnorm = sqrt(r2[1]);
+    double rr = r1[0];
+    const double tol2 = a.tol * a.tol;
+    auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
+    int it = 0;
+    bool conv = done_test(gamma, rr);
+    while (!conv && it < a.maxit) {
+        ++it;
+        double pq[1] = { part_spmv(C, S, p0, np) };
+        if (!part_reduce<1>(a.bar, pq, sh, S.red)) return;
+        const double alpha = gamma / pq[0];
+        // with the absolute criterion (a test of r.z alone) r.r is reduced once after the loop
+        double g2[2] = { 0.0, 0.0 };  // r.z (IC: t.t), r.r
+        if (MODE == 0) {
+            for (int l = tid; l < np; l += kPartThreads) {
+                __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + alpha * S.p[l]);
+                const double ri = S.r[l] - alpha * S.q[l];
+                const double zi = jac ? ri * S.t[l] : ri;
+                S.r[l] = ri;
+                S.z[l] = zi;
+                g2[0] += ri * zi;
+                if (rel) g2[1] += ri * ri;
+            }
+        } else if (MODE == 1) {
+            const double2 f = part_fwd<true>(C, S, p0, np, false, alpha, rel, err, rec);
+            g2[0] = f.y;
+            g2[1] = f.x;
+        } else {
+            g2[1] = part_fwd<false>(C, S, p0, np, false, alpha, rel, err, rec).x;
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            g2[0] = part_bwd<0>(C, S, p0, np, 0.0, err, rec);
+        }
+        if (rel) {
+            if (!part_reduce<2>(a.bar, g2, sh, S.red)) return;
+            rr = g2[1];
+        } else {
+            double g1[1] = { g2[0] };
+            if (!part_reduce<1>(a.bar, g1, sh, S.red)) return;
+            g2[0] = g1[0];
+        }
+        const double gnew = g2[0];
+        if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
+        const double beta = gnew / gamma;
+        gamma = gnew;
+        if (MODE == 1) {
+            part_bwd<2>(C, S, p0, np, beta, err, rec);
+        } else {
+            for (int l = tid; l < np; l += kPartThreads) {
+                const double pn = S.z[l] + beta * S.p[l];
+                S.p[l] = pn;
+                if (S.bnd[l]) __stcg(&C.gp[p0 + l], pn);
+            }
+        }
+        if (!grid_sync(a.bar, gridDim.x)) return;
+    }
+    if (!rel && it > 0) {
+        double f[1] = { 0.0 };
+        for (int l = tid; l < np; l += kPartThreads) f[0] += S.r[l] * S.r[l];
+        if (!part_reduce<1>(a.bar, f, sh, S.red)) return;
+        rr = f[0];
+    }
+    for (int l = tid; l < np; l += kPartThreads) a.x[__ldg(&C.qa[p0 + l])] = __ldcg(&C.x[p0 + l]);
+    if (blockIdx.x == 0 && tid == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rel ? sqrt(rr) / (bnorm > 0 ? bnorm : 1.0) : sqrt(gamma);
+        a.out->relres = sqrt(rr) / (bnorm > 0 ? bnorm : 1.0);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kPartThreads, 1) k_pcg_part(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    extern __shared__ double part_smem[];
+    pcg_part<MODE>(a, sh, part_smem);
+}
+
+
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_one(KArgs a) {
     __shared__ double sh[kShDoubles];
     pcg_one_reduction(a, sh);
@@ -1455,7 +1871,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
             for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
                 const double ri = a.r[i];
                 g2[0] += ri * __ldcg(&a.z[i]);
-                g2[1] += ri * ri;
+                if (rel) g2[1] += ri * ri;
             }
         } else {
             // two rows per pass, all loads issued before the stores
@@ -1482,18 +1898,35 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg(KArg
                     a.r[i] = ri;
                     a.z[i] = zi;
                     g2[0] += ri * zi;
-                    g2[1] += ri * ri;
+                    if (rel) g2[1] += ri * ri;
                 }
             }
         }
-        if (!grid_reduce<2>(a.bar, g2, sh)) return;
+        // with the absolute criterion (a test of r.z alone) r.r is reduced once after
+        // the loop, not per iteration
+        if (rel || fused) {
+            if (!grid_reduce<2>(a.bar, g2, sh)) return;
+            rr = g2[1];
+        } else {
+            double g1[1] = { g2[0] };
+            if (!grid_reduce<1>(a.bar, g1, sh)) return;
+            g2[0] = g1[0];
+        }
         const double gnew = g2[0];
-        rr = g2[1];
         if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
         const double beta = gnew / gamma;
         gamma = gnew;
         p_update(a.p, a.z, beta, r0, r1);
         if (!grid_sync(a.bar, gridDim.x)) return;
+    }
+    if (!rel && !fused && it > 0) {
+        double f[1] = { 0.0 };
+        for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
+            const double ri = __ldcg(&a.r[i]);
+            f[0] += ri * ri;
+        }
+        if (!grid_reduce<1>(a.bar, f, sh)) return;
+        rr = f[0];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
@@ -2110,6 +2543,16 @@ struct pf2_solver {
     int ngroups = 0;
     DevBuf<int> cstart;
     int levels_fwd = 0, levels_bwd = 0, colors = 0;
+    // partitioned CG (k_pcg_part): group starts per part, CSR in the part order Q with the
+    // positions of its entries in A (values) and in B (factors), Q -> A rows, boundary
+    // flags, x in Q order and the boundary rows' global copies of p, t, z
+    bool part = false;
+    int part_P = 0, part_R = 0, part_ng = 0;
+    size_t part_smem = 0;
+    long long part_boundary_rows = 0;
+    DevBuf<int> q_s, q_rp, q_col, q_diag, q_a, q_amap, q_fmap;
+    DevBuf<unsigned char> q_bnd;
+    DevBuf<double> q_val, q_f, q_x, q_gp, q_gt, q_gz;
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
 };
@@ -2233,6 +2676,176 @@ static int multicolour_order(int n, const int* rp, const int* col, bool kempe, s
     perm.assign(n, 0);
     for (int i = 0; i < n; ++i) perm[cnt[color[i]]++] = i;
     return nc;
+}
+
+// Recursive bisection of the graph of a symmetric pattern into P parts whose sizes differ
+// by at most one row per level: a subset is ordered breadth-first from a pseudo-peripheral
+// node (the last node a breadth-first search from the subset's first node reaches; a
+// disconnected subset continues from its next unreached node) and cut after the rows of
+// its first P / 2 parts.  part[i] receives the part of row i.
+static void graph_parts(int n, const std::vector<int>& rp, const std::vector<int>& col, int P, std::vector<int>& part) {
+    part.assign(n, 0);
+    std::vector<int> order(n), tmp(n), subset(n, -1), seen(n, -1);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    struct Job { int lo, hi, P, first; };
+    std::vector<Job> jobs{ { 0, n, P, 0 } };
+    int sid = 0, stamp = 0;
+    auto bfs = [&](int lo, int hi, int start) {
+        ++stamp;
+        int w = lo, next = lo;
+        tmp[w++] = start;
+        seen[start] = stamp;
+        for (int h = lo; h < hi; ++h) {
+            if (h == w) {  // the reached component is exhausted: the subset's next unreached row
+                while (seen[order[next]] == stamp) ++next;
+                tmp[w++] = order[next];
+                seen[order[next]] = stamp;
+            }
+            const int v = tmp[h];
+            for (int k = rp[v]; k < rp[v + 1]; ++k) {
+                const int u = col[k];
+                if (subset[u] == sid && seen[u] != stamp) {
+                    seen[u] = stamp;
+                    tmp[w++] = u;
+                }
+            }
+        }
+        return tmp[hi - 1];
+    };
+    while (!jobs.empty()) {
+        const Job j = jobs.back();
+        jobs.pop_back();
+        if (j.P <= 1 || j.hi - j.lo <= 1) {
+            for (int q = j.lo; q < j.hi; ++q) part[order[q]] = j.first;
+            continue;
+        }
+        ++sid;
+        for (int q = j.lo; q < j.hi; ++q) subset[order[q]] = sid;
+        const int far = bfs(j.lo, j.hi, order[j.lo]);
+        bfs(j.lo, j.hi, far);
+        std::copy(tmp.begin() + j.lo, tmp.begin() + j.hi, order.begin() + j.lo);
+        const int P1 = j.P / 2;
+        const int mid = j.lo + (int)((long long)(j.hi - j.lo) * P1 / j.P);
+        jobs.push_back({ mid, j.hi, j.P - P1, j.first + P1 });
+        jobs.push_back({ j.lo, mid, P1, j.first });
+    }
+}
+
+// The partitioned CG plan (k_pcg_part) for the pattern of B = P A P^T (brp, bcol; bmap:
+// position in A of each entry of B; bdiag; perm: row of A at each row of B) with sweep
+// groups `groups` of B's rows: parts from graph_parts on A's pattern (rp, col), one per SM
+// (at least kPartMinRows rows each), the part order Q, the CSR arrays in Q order and the
+// boundary flags.  Leaves S->part false where the plan does not apply: a group whose rows
+// depend on one another, or a part too large for the shared-memory vectors.
+constexpr int kPartMinRows = 512;
+static pf2_status build_part_plan(pf2_solver* S, const std::vector<int>& rp, const std::vector<int>& col,
+                                  const std::vector<int>& brp, const std::vector<int>& bcol,
+                                  const std::vector<int>& bmap, const std::vector<int>& bdiag,
+                                  const std::vector<int>& perm, const std::vector<int>& groups, bool tri) {
+    S->part = false;
+    const int n = S->n, nnz = S->nnz;
+    const int ng = (int)groups.size() - 1;
+    std::vector<int> grp(n);
+    for (int g = 0; g < ng; ++g)
+        for (int r = groups[g]; r < groups[g + 1]; ++r) grp[r] = g;
+    if (tri)  // the rows of a group must depend only on earlier groups
+        for (int r = 0; r < n; ++r)
+            for (int k = brp[r]; k < bdiag[r]; ++k)
+                if (grp[bcol[k]] >= grp[r]) return PF2_OK;
+    int P = std::max(1, std::min(num_sms(), n / kPartMinRows));
+    if (const char* e = getenv("PF2_CG_PARTS")) P = std::max(1, std::min(num_sms(), atoi(e)));  // tests, tuning
+    std::vector<int> part;
+    graph_parts(n, rp, col, P, part);
+    // boundary rows (a neighbour in another part), in A's numbering
+    std::vector<unsigned char> bnd_a(n, 0);
+    for (int i = 0; i < n; ++i)
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (part[col[k]] != part[i]) bnd_a[i] = 1;
+    // Q: by part, then group, then the group's boundary rows before its interior rows (the
+    // threads that wait on other parts' values share warps with as few others as possible),
+    // then B's order
+    std::vector<int> cls((size_t)P * ng * 2 + 1, 0);
+    auto cell = [&](int r) { return ((size_t)part[perm[r]] * ng + grp[r]) * 2 + (bnd_a[perm[r]] ? 0 : 1); };
+    for (int r = 0; r < n; ++r) cls[cell(r) + 1]++;
+    for (size_t c = 0; c + 1 < cls.size(); ++c) cls[c + 1] += cls[c];
+    std::vector<int> qs((size_t)P * ng + 1);
+    for (size_t c = 0; c < qs.size(); ++c) qs[c] = cls[2 * c];
+    std::vector<int> fill(cls.begin(), cls.end() - 1), bq(n), qa(n), qb(n);
+    for (int r = 0; r < n; ++r) {
+        const int q = fill[cell(r)]++;
+        bq[r] = q;
+        qb[q] = r;
+        qa[q] = perm[r];
+    }
+    int R = 0;
+    for (int p = 0; p < P; ++p) R = std::max(R, qs[(size_t)(p + 1) * ng] - qs[(size_t)p * ng]);
+    int optin = 0;
+    PF2_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
+    const size_t smem = (part_smem_bytes(R, tri) + 15) / 16 * 16;
+    if (smem + 2048 > (size_t)optin) return PF2_OK;
+    std::vector<int> qrp(n + 1, 0), qcol(std::max(nnz, 1)), qdiag(n), qamap(std::max(nnz, 1)),
+        qfmap(std::max(nnz, 1));
+    std::vector<unsigned char> bnd(n, 0);
+    long long nb = 0;
+    for (int q = 0; q < n; ++q) {
+        const int r = qb[q];
+        const int len = brp[r + 1] - brp[r];
+        qrp[q + 1] = qrp[q] + len;
+        const int pr = part[perm[r]];
+        for (int e = 0; e < len; ++e) {
+            const int kb = brp[r] + e, kq = qrp[q] + e;
+            qcol[kq] = bq[bcol[kb]];
+            qamap[kq] = bmap[kb];
+            qfmap[kq] = kb;
+            if (part[perm[bcol[kb]]] != pr) bnd[q] = 1;
+        }
+        qdiag[q] = qrp[q] + (bdiag[r] - brp[r]);
+        nb += bnd[q];
+    }
+    auto up = [&](auto& d, const auto& h) -> pf2_status {
+        PF2_TRY(d.alloc(h.size()));
+        PF2_CUDA(cudaMemcpy(d.p, h.data(), sizeof(h[0]) * h.size(), cudaMemcpyHostToDevice));
+        return PF2_OK;
+    };
+    PF2_TRY(up(S->q_s, qs));
+    PF2_TRY(up(S->q_rp, qrp));
+    PF2_TRY(up(S->q_col, qcol));
+    PF2_TRY(up(S->q_diag, qdiag));
+    PF2_TRY(up(S->q_a, qa));
+    PF2_TRY(up(S->q_amap, qamap));
+    PF2_TRY(up(S->q_bnd, bnd));
+    PF2_TRY(S->q_val.alloc(std::max(nnz, 1)));
+    if (tri) {
+        PF2_TRY(up(S->q_fmap, qfmap));
+        PF2_TRY(S->q_f.alloc(std::max(nnz, 1)));
+    }
+    PF2_TRY(S->q_x.alloc(n));
+    PF2_TRY(S->q_gp.alloc(n));
+    PF2_TRY(S->q_gt.alloc(n));
+    PF2_TRY(S->q_gz.alloc(n));
+    S->part = true;
+    S->part_P = P;
+    S->part_R = R;
+    S->part_ng = ng;
+    S->part_smem = smem;
+    S->part_boundary_rows = nb;
+    return PF2_OK;
+}
+
+// Whether a solve with these options may run as k_pcg_part: FP64 standard CG;
+// PF2_CG_PART=0 keeps the other kernels (tuning, comparisons).
+static bool part_eligible(const pf2_solver* S) {
+    if (const char* e = getenv("PF2_CG_PART"))
+        if (atoi(e) == 0) return false;
+    return S->opt.kind == PF2_SOLVER_CG && S->opt.precision == PF2_PRECISION_FP64 &&
+           S->opt.cg_variant == PF2_CG_STANDARD;
+}
+
+// The partitioned CG kernel of the solver's preconditioner.
+static void* part_kernel(const pf2_solver* S) {
+    if (S->opt.precond == PF2_PRECOND_IC) return (void*)k_pcg_part<1>;
+    if (S->opt.precond == PF2_PRECOND_ILU) return (void*)k_pcg_part<2>;
+    return (void*)k_pcg_part<0>;
 }
 
 static pf2_status build_tri_plan(pf2_solver* S) {
@@ -2402,6 +3015,8 @@ static pf2_status build_tri_plan(pf2_solver* S) {
             PF2_TRY(S->bval32.alloc(nnz));
             PF2_TRY(S->fsym32.alloc(nnz));
         }
+        if (S->opt.ordering == PF2_ORDERING_MULTICOLOR && part_eligible(S))
+            PF2_TRY(build_part_plan(S, rp, col, brp, bcol, bmap, bdiag, perm, groups, true));
     }
     if (K <= kBandMaxDeps) {
         const int R = banded ? std::min(n, band_rows) : n;
@@ -2581,6 +3196,11 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
         k_fsym<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->tpos.p, S->fact.p,
                                                                                     S->fsym.p);
         PF2_LAUNCH_CHECK();
+        if (S->part) {
+            k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
+                S->nnz, S->fsym.p, S->q_fmap.p, S->q_f.p);
+            PF2_LAUNCH_CHECK();
+        }
         if (mixed) {
             k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fsym.p,
                                                                                             S->fsym32.p);
@@ -2677,6 +3297,24 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
         a.max_outer = kMaxOuter;
     }
     const int applies = max_applies(S);
+    if (S->part && !precond_only) {
+        // A's values in Q order for this solve's matrix; t and z start as pending markers
+        k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
+            S->nnz, a.A.val, S->q_amap.p, S->q_val.p);
+        PF2_LAUNCH_CHECK();
+        if (uses_tri(S)) {
+            PF2_CUDA(cudaMemsetAsync(S->q_gt.p, 0xff, S->q_gt.bytes(), st));
+            PF2_CUDA(cudaMemsetAsync(S->q_gz.p, 0xff, S->q_gz.bytes(), st));
+        }
+        a.part = PartCg{ S->part_P, S->part_R, S->part_ng, S->q_s.p, S->q_rp.p, S->q_col.p, S->q_diag.p, S->q_a.p,
+                         S->q_bnd.p, S->q_val.p, S->q_f.p, S->q_x.p, S->q_gp.p, S->q_gt.p, S->q_gz.p };
+        PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
+        PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
+        PF2_CUDA(cudaMemsetAsync(S->rec.p, 0, 5 * sizeof(int), st));
+        void* args[] = { &a };
+        PF2_COOP_LAUNCH(part_kernel(S), dim3(S->part_P), dim3(kPartThreads), args, S->part_smem, st);
+        return PF2_OK;
+    }
     if (S->csr && !precond_only) {  // A's values in B's numbering, for this solve's matrix
         k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
             S->nnz, a.A.val, S->bmap.p, S->bval.p);
@@ -2723,6 +3361,20 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
     return PF2_OK;
 }
 
+// The partitioned CG plan of a Jacobi / no-preconditioner solve: B = A, one group.
+static pf2_status build_part_plan_local(pf2_solver* S) {
+    const pf2_mesh* M = S->mesh;
+    const int n = S->n, nnz = S->nnz;
+    std::vector<int> rp(n + 1), col(nnz), dg(n), ident(n), kmap(nnz);
+    PF2_CUDA(cudaMemcpy(rp.data(), M->rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost));
+    PF2_CUDA(cudaMemcpy(col.data(), M->col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost));
+    PF2_CUDA(cudaMemcpy(dg.data(), M->diag.p, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) ident[i] = i;
+    for (int k = 0; k < nnz; ++k) kmap[k] = k;
+    const std::vector<int> groups{ 0, n };
+    return build_part_plan(S, rp, col, rp, col, kmap, dg, ident, groups, false);
+}
+
 extern "C" {
 
 pf2_status pf2_multicolour_order(int n, const int* rowptr, const int* col, int kempe, int* perm, int* ncolours,
@@ -2736,6 +3388,18 @@ pf2_status pf2_multicolour_order(int n, const int* rowptr, const int* col, int k
     std::copy(p.begin(), p.end(), perm);
     *nstarts = (int)groups.size();
     if (starts) std::copy(groups.begin(), groups.end(), starts);
+    return PF2_OK;
+}
+
+pf2_status pf2_graph_parts(int n, const int* rowptr, const int* col, int parts, int* part) {
+    PF2_REQUIRE(n > 0 && rowptr && col && part, PF2_BAD_INPUT, "null argument");
+    PF2_REQUIRE(parts >= 1, PF2_BAD_INPUT, "parts %d < 1", parts);
+    for (int i = 0; i < n; ++i)
+        for (int k = rowptr[i]; k < rowptr[i + 1]; ++k)
+            PF2_REQUIRE(col[k] >= 0 && col[k] < n, PF2_BAD_INPUT, "column %d of row %d out of range", col[k], i);
+    std::vector<int> p;
+    graph_parts(n, std::vector<int>(rowptr, rowptr + n + 1), std::vector<int>(col, col + rowptr[n]), parts, p);
+    std::copy(p.begin(), p.end(), part);
     return PF2_OK;
 }
 
@@ -2773,6 +3437,15 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
     pf2_status s;
     const bool mixed = opt->precision == PF2_PRECISION_MIXED;
     if (uses_tri(S) && (s = build_tri_plan(S))) return fail(s);
+    if (!uses_tri(S) && part_eligible(S) && (s = build_part_plan_local(S))) return fail(s);
+    if (S->part) {
+        int occ_p = 0;
+        void* pf = part_kernel(S);
+        if (cudaFuncSetAttribute(pf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->part_smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, pf, kPartThreads, S->part_smem) != cudaSuccess)
+            return fail(cuda_fail(cudaGetLastError(), "partitioned CG attributes", __FILE__, __LINE__));
+        if (occ_p < 1) S->part = false;  // the other kernels then
+    }
     // the banded triangular solve keeps a range of the solution in shared memory
     S->smem = S->band_P ? sizeof(double) * (size_t)S->band_R : 0;
     void* fn = solve_kernel(*opt, S->csr);
@@ -2813,7 +3486,7 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
         (opt->kind == PF2_SOLVER_CG && opt->cg_variant == PF2_CG_PIPELINED && (s = S->pipe.alloc(6 * S->n))) ||
         (opt->kind == PF2_SOLVER_BICGSTAB && ((s = S->s.alloc(S->n)) || (s = S->rhat.alloc(S->n)) ||
                                                (s = S->yv.alloc(S->n)) || (s = S->tv.alloc(S->n)))) ||
-        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)S->blocks)) || (s = S->bar.alloc(2)) ||
+        (s = S->invd.alloc(S->n)) || (s = S->partial.alloc(8 * (size_t)std::max(S->blocks, S->part_P))) || (s = S->bar.alloc(2)) ||
         (s = S->err.alloc(1)) || (s = S->rec.alloc(5)) || (s = S->out.alloc(1)) || (s = S->h_out.alloc(1)))
         return fail(s);
     if (mixed && ((s = S->val32.alloc(S->nnz)) || (s = S->d32.alloc(S->n)) || (s = S->r32.alloc(S->n)) ||

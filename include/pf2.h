@@ -318,6 +318,14 @@ typedef struct pf2_solver_options {
 pf2_status pf2_multicolour_order(int n, const int* rowptr, const int* col, int kempe, int* perm, int* ncolours,
                                  int* nstarts, int* starts);
 
+/* The row partition of the partitioned CG solve (host arrays; no GPU work): part[i] in
+ * [0, parts) for each row of a symmetric CSR pattern, by recursive bisection of its graph
+ * in breadth-first order from a pseudo-peripheral node; part sizes differ by at most one
+ * row per bisection level.  The solver cuts a CG system into one part per SM (at least
+ * 512 rows each) and keeps each part's vectors in that block's shared memory; no
+ * reference counterpart (the reference's CG runs on cuSPARSE / cuBLAS). */
+pf2_status pf2_graph_parts(int n, const int* rowptr, const int* col, int parts, int* part);
+
 typedef struct pf2_solve_info {
     int iterations;      /* total inner iterations */
     int converged;

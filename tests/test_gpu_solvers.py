@@ -409,13 +409,16 @@ def test_bicgstab_restarts_an_orthogonal_shadow_residual(cuda):
     assert rel_err(x.cpu().numpy(), ox) < 1e-9
 
 
-def test_barrier_wait_that_runs_out_returns_timeout(cuda, monkeypatch):
+@pytest.mark.parametrize("part", ["1", "0"])
+def test_barrier_wait_that_runs_out_returns_timeout(cuda, monkeypatch, part):
     """A grid-barrier wait bounded to one poll (PF2_BARRIER_POLLS, read when the solver
     is created; a test knob) gives up before the other blocks arrive: the solve returns
     PF2_TIMEOUT with the record of the block and barrier that gave up, nothing faults, and
-    a solver made afterwards with the normal limit solves on the same context."""
+    a solver made afterwards with the normal limit solves on the same context.  Both the
+    partitioned kernel (the default) and k_pcg (PF2_CG_PART=0)."""
     m, A, rp, col, val, rhs = _system(128, 32)
     b = torch.tensor(rhs, device="cuda")
+    monkeypatch.setenv("PF2_CG_PART", part)
     monkeypatch.setenv("PF2_BARRIER_POLLS", "1")
     s = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=1000)
     monkeypatch.delenv("PF2_BARRIER_POLLS")
@@ -430,3 +433,82 @@ def test_barrier_wait_that_runs_out_returns_timeout(cuda, monkeypatch):
     assert info.converged == 1 and info.status == 0
     ox, _ = O.pcg(rp, col, val, rhs, tol=1e-8, maxit=1000, precond="jacobi")
     assert rel_err(x.cpu().numpy(), ox) < 1e-6
+
+
+def _cylinder_system():
+    """The Poisson matrix of the quarter-size cylinder mesh (125,364 nodes) with a small
+    shift, the size class of the flow's pressure solves."""
+    xy, tri = mg.cylinder_channel(nxh=350, nyh=400, nr=12)
+    m = g.Mesh2D.from_arrays(xy, tri)
+    A = g.SparseMatrixCSR(m)
+    area, invJ = O.mesh_geometry(xy, tri)
+    rp, col = O.csr_structure(xy.shape[0], tri)
+    val, rhs = O.assemble_poisson(xy, tri, area, invJ, rp, col, 1, 1.0)
+    diag = np.array([rp[i] + np.searchsorted(col[rp[i]:rp[i + 1]], i) for i in range(rp.size - 1)])
+    val[diag] += 1e-2
+    A.upload_values(val)
+    return m, A, rp, col, val, rhs
+
+
+def _solve_both(monkeypatch, A, rhs, pc, ordering, parts="", **kw):
+    """The same solve by the partitioned kernel and by the kernels it replaces."""
+    b = torch.tensor(rhs, device="cuda")
+    out = {}
+    for part in ("1", "0"):
+        monkeypatch.setenv("PF2_CG_PART", part)
+        if parts:
+            monkeypatch.setenv("PF2_CG_PARTS", parts)
+        x = torch.zeros_like(b)
+        info = g.LinearSolver(A, "cg", pc, ordering=ordering, **kw).solve(A, x, b, check=False)
+        out[part] = (x.cpu().numpy(), info)
+    return out
+
+
+@pytest.mark.parametrize("pc,ordering", [("none", 0), ("jacobi", 0), ("ic", 1), ("ilu", 1)])
+@pytest.mark.parametrize("parts", ["", "7"])
+def test_partitioned_cg_matches_the_other_kernels(cuda, monkeypatch, pc, ordering, parts):
+    """The partitioned CG (one part per block with its vectors in shared memory; 4 parts
+    of the 2,193-row system, or 7 with PF2_CG_PARTS) against k_pcg / pcg_csr
+    (PF2_CG_PART=0) and the oracle, converged to an absolute 1e-12: each row's arithmetic
+    is the same, the reductions' order differs, so the solutions agree to 1e-10 and the
+    iteration counts within 2."""
+    m, A, rp, col, val, rhs = _system(128, 16)
+    out = _solve_both(monkeypatch, A, rhs, pc, ordering, parts, tol=1e-12, maxit=5000)
+    (xp, ip), (xo, io) = out["1"], out["0"]
+    assert ip.converged == 1 and io.converged == 1 and ip.status == 0
+    assert abs(ip.iterations - io.iterations) <= 2
+    assert rel_err(xp, xo) < 1e-10
+    if pc in ("none", "jacobi"):
+        ox, oi = O.pcg(rp, col, val, rhs, tol=1e-12, maxit=5000, precond=pc)
+        assert oi.converged == 1 and rel_err(xp, ox) < 1e-10
+
+
+@pytest.mark.parametrize("pc,ordering", [("jacobi", 0), ("ic", 1)])
+def test_partitioned_cg_relative_criterion_and_cap(cuda, monkeypatch, pc, ordering):
+    """The relative criterion (r.r reduced every iteration) converges like the other
+    kernels; at an iteration cap far from convergence (40 iterations) both paths stop with
+    the same count, report the same ||r|| / ||b||, and their iterates agree to 1e-9."""
+    m, A, rp, col, val, rhs = _system(128, 16)
+    out = _solve_both(monkeypatch, A, rhs, pc, ordering, tol=1e-10, maxit=5000, criterion=g.CRITERION_REL)
+    (xp, ip), (xo, io) = out["1"], out["0"]
+    assert ip.converged == 1 and io.converged == 1 and abs(ip.iterations - io.iterations) <= 2
+    assert ip.residual <= 1e-10 and rel_err(xp, xo) < 1e-8
+    res = np.linalg.norm(rhs - O.spmv(rp, col, val, xp)) / np.linalg.norm(rhs)
+    assert res <= 2e-10
+    out = _solve_both(monkeypatch, A, rhs, pc, ordering, tol=1e-30, maxit=40)
+    (xp, ip), (xo, io) = out["1"], out["0"]
+    assert ip.converged == 0 and io.converged == 0 and ip.iterations == io.iterations == 40
+    assert rel_err(xp, xo) < 1e-9
+
+
+def test_partitioned_cg_on_the_cylinder_mesh(cuda, monkeypatch):
+    """IC(0) on the multicolour order, 152 parts (one per SM) of the 125,364-row cylinder
+    system: the partitioned kernel and pcg_csr reach the same converged solution (1e-10)
+    in the same number of iterations (within 2)."""
+    m, A, rp, col, val, rhs = _cylinder_system()
+    out = _solve_both(monkeypatch, A, rhs, "ic", 1, tol=1e-12, maxit=20000)
+    (xp, ip), (xo, io) = out["1"], out["0"]
+    print("cylinder IC(0): partitioned %d iterations, pcg_csr %d, rel diff %.2e" % (
+        ip.iterations, io.iterations, rel_err(xp, xo)))
+    assert ip.converged == 1 and io.converged == 1 and abs(ip.iterations - io.iterations) <= 2
+    assert rel_err(xp, xo) < 1e-10
