@@ -7,6 +7,7 @@
 // expressions into fused multiply-adds.  The CPU oracle calls fma() at the same places.
 #pragma once
 
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -298,6 +299,82 @@ __device__ __forceinline__ bool grid_reduce(const GridBarrier& b, double (&v)[NV
     __syncthreads();
 #pragma unroll
     for (int j = 0; j < NV; ++j) v[j] = sh[32 * NV + j];
+    return s_ok != 0;
+}
+
+struct NoPost {
+    __device__ void operator()(const double*, double*) const {}
+};
+
+// Grid-wide sums of NV <= 4 values fused with the grid barrier, for blocks of BT threads
+// (BT a multiple of 128, at most 1024), with few FP64 instructions: on GB300 an SM issues
+// one FP64 warp instruction per ~19 clocks (~64 per sub-partition), so warp butterflies
+// in every warp (five FP64 additions per value per warp) cost microseconds per reduction.
+// The block's values go to red (NV x BT doubles of shared memory) and a fixed tree adds
+// them: a quarter of the threads per value add 4 values each, a sixteenth add 4 of those,
+// one warp per value adds up to 2 and finishes with a butterfly.  Thread 0 stores the block
+// sums in one of two partial arrays (by the barrier's parity) and arrives on the grid
+// barrier; after the release warp j adds value j's partials in block order (lane l:
+// partials l, l + 32, ...; butterfly).  The order depends on no arrival order: the sums
+// are reproducible bit for bit.  Post (not NoPost): thread 0 alone then derives the
+// iteration's scalars from the totals (post(totals, out), out = sh + 24, up to 8 doubles),
+// which every thread reads after the call: an FP64 division or square root is tens of
+// FP64 instructions and would cost microseconds computed by every warp.  sh holds at least
+// 32 doubles.
+template <int BT, int NV, class Post = NoPost>
+__device__ __forceinline__ bool grid_reduce_tree(const GridBarrier& b, double (&v)[NV], double* sh, double* red,
+                                                 Post post = Post()) {
+    static_assert(NV >= 1 && NV <= 4, "grid_reduce_tree sums one to four values");
+    static_assert(BT % 128 == 0 && BT <= 1024, "block size of the tree");
+    __shared__ int s_ok, s_par;
+    const unsigned G = gridDim.x;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    unsigned c0 = 0;
+    if (tid == 0) c0 = ld_relaxed_gpu(b.count);
+    __syncthreads();  // the previous call's readers of red and sh are done
+#pragma unroll
+    for (int j = 0; j < NV; ++j) red[j * BT + tid] = v[j];
+    __syncthreads();
+    for (int t = tid; t < NV * (BT / 4); t += BT) {
+        const int j = t / (BT / 4), u = t % (BT / 4);
+        double* c = red + j * BT + u;
+        c[0] = ((c[0] + c[BT / 4]) + c[BT / 2]) + c[3 * BT / 4];
+    }
+    __syncthreads();
+    if (tid < NV * (BT / 16)) {
+        const int j = tid / (BT / 16), u = tid % (BT / 16);
+        double* c = red + j * BT + u;
+        c[0] = ((c[0] + c[BT / 16]) + c[BT / 8]) + c[3 * BT / 16];
+    }
+    __syncthreads();
+    if (w < NV) {
+        const double s = warp_sum(red[w * BT + lane] + (lane + 32 < BT / 16 ? red[w * BT + lane + 32] : 0.0));
+        if (lane == 0) sh[w] = s;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned kb = c0 / G;
+        double* part = b.part + (size_t)(kb & 1u) * 4 * G;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], sh[j]);
+        s_ok = arrive_and_wait(b, c0, G) ? 1 : 0;
+        s_par = (int)(kb & 1u);
+    }
+    __syncthreads();
+    if (w < NV) {
+        const double* part = b.part + (size_t)s_par * 4 * G + w * G;
+        double t = 0.0;
+        for (unsigned q = lane; q < G; q += 32) t += __ldcg(&part[q]);
+        t = warp_sum(t);
+        if (lane == 0) sh[16 + w] = t;
+    }
+    __syncthreads();
+    if (!std::is_same<Post, NoPost>::value) {
+        if (tid == 0) post(sh + 16, sh + 24);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int j = 0; j < NV; ++j) v[j] = sh[16 + j];
     return s_ok != 0;
 }
 

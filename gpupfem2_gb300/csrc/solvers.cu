@@ -15,6 +15,7 @@
 #include <mutex>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -571,6 +572,12 @@ struct PartCg {
     double* gp;               // boundary rows' p, t, z (t and z start as the pending marker)
     double* gt;
     double* gz;
+    // mixed precision: FP32 values and factors in Q order, FP32 boundary copies
+    const float* val32;
+    const float* f32;
+    float* gp32;
+    float* gt32;
+    float* gz32;
 };
 
 struct KArgs {
@@ -1132,6 +1139,7 @@ __device__ void pcg_one_reduction(const KArgs& a, double* sh) {
 // residual.  x changes every iteration (x += alpha y + omega z).
 __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab(KArgs a) {
     __shared__ double sh[kShDoubles];
+    __shared__ double red_s[4 * kSolverThreads];  // grid_reduce_tree's block tree
     int r0, r1;
     row_range(a.A.n, r0, r1);
     const bool jac = a.precond == PF2_PRECOND_JACOBI;
@@ -1153,16 +1161,24 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
         red[2] += (ri * di) * (ri * di);
         red[3] += bi * bi;
     }
-    if (!grid_reduce<4>(a.bar, red, sh)) return;
-    const double bnorm = sqrt(red[3]);
-    auto done_test = [&](double rr, double mm) { return rel ? sqrt(rr) <= a.tol * bnorm : sqrt(mm) < a.tol; };
+    // the iteration's scalars (divisions, square roots) by thread 0 (grid_reduce_tree)
+    double bnorm = 0.0;
+    auto test = [&](const double* t) { return rel ? sqrt(t[1]) <= a.tol * bnorm : sqrt(t[2]) < a.tol; };
+    if (!grid_reduce_tree<kSolverThreads, 4>(a.bar, red, sh, red_s, [&](const double* t, double* o) {
+            bnorm = sqrt(t[3]);
+            o[0] = bnorm;
+            o[1] = test(t);
+            o[2] = (t[0] / 1.0) * (1.0 / 1.0);  // beta of the first iteration (rho_old = alpha = omega = 1)
+        }))
+        return;
+    bnorm = sh[24];
     double rho_old = 1.0, alpha = 1.0, omega = 1.0;
     double rho = red[0], rr = red[1], mm = red[2];
     int it = 0;
-    bool conv = done_test(rr, mm);
+    bool conv = sh[25] != 0.0;
+    double beta = sh[26];
     while (!conv && it < a.maxit) {
         ++it;
-        const double beta = (rho / rho_old) * (alpha / omega);
         // p = r + beta (p - omega v); y = M^{-1} p
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const double pi = a.r[i] + beta * (a.p[i] - omega * a.q[i]);
@@ -1177,9 +1193,12 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             a.q[i] = vi;
             rv[0] += a.rhat[i] * vi;
         }
-        if (!grid_reduce<1>(a.bar, rv, sh)) return;
+        if (!grid_reduce_tree<kSolverThreads, 1>(a.bar, rv, sh, red_s, [&](const double* t, double* o) {
+                o[0] = t[0] == 0.0 ? 0.0 : rho / t[0];
+            }))
+            return;
         if (rv[0] == 0.0) break;  // breakdown: ends unconverged
-        alpha = rho / rv[0];
+        alpha = sh[24];
         // s = r - alpha v; z = M^{-1} s
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
             const double si = a.r[i] - alpha * a.q[i];
@@ -1195,11 +1214,14 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             ts[0] += ti * a.s[i];
             ts[1] += ti * ti;
         }
-        if (!grid_reduce<2>(a.bar, ts, sh)) return;
         // t = A M^{-1} s is zero only where s is: the half step alpha y already solves
         // the system, so take it (omega = 0: x += alpha y, r = s) and let the test below
         // decide; a nonzero s that A M^{-1} maps to zero ends the solve unconverged
-        omega = ts[1] == 0.0 ? 0.0 : ts[0] / ts[1];
+        if (!grid_reduce_tree<kSolverThreads, 2>(a.bar, ts, sh, red_s, [&](const double* t, double* o) {
+                o[0] = t[1] == 0.0 ? 0.0 : t[0] / t[1];
+            }))
+            return;
+        omega = sh[24];
         // x += alpha y + omega z; r = s - omega t; rhat.r, r.r, |M^{-1} r|^2
         double g3[3] = { 0.0, 0.0, 0.0 };
         for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
@@ -1211,12 +1233,19 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             g3[1] += ri * ri;
             g3[2] += (ri * di) * (ri * di);
         }
-        if (!grid_reduce<3>(a.bar, g3, sh)) return;
+        // the test and the next iteration's beta (after a shadow-residual restart: rho = r.r
+        // with rho_old = alpha = omega = 1)
+        if (!grid_reduce_tree<kSolverThreads, 3>(a.bar, g3, sh, red_s, [&](const double* t, double* o) {
+                o[0] = test(t);
+                o[1] = t[0] == 0.0 ? (t[1] / 1.0) * (1.0 / 1.0) : (t[0] / rho) * (alpha / omega);
+            }))
+            return;
         rho_old = rho;
         rho = g3[0];
         rr = g3[1];
         mm = g3[2];
-        conv = done_test(rr, mm);
+        conv = sh[24] != 0.0;
+        beta = sh[25];
         if (!conv && omega == 0.0) break;
         if (!conv && rho == 0.0) {
             // r orthogonal to rhat: with rhat = r0 supported on the Dirichlet rows alone
@@ -1234,6 +1263,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
             omega = 1.0;
         }
     }
+    (void)rho_old;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
@@ -1432,15 +1462,18 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_pipe
     }
 }
 
-// The part's shared memory: r, p, q and t of its rows (Jacobi / none: t = 1 / a_ii and a
-// separate z; ILU / IC: z shares t's array, since a row's forward result is dead once the
-// backward sweep has read it and the backward sweep reads only its own row's t), the
-// reduction scratch, and (kPartMetaSmem) the rows' entry ranges, diagonal positions and
-// boundary flags.  x stays in global memory: the smaller shared-memory carve-out leaves
-// more of the SM's 256 KB to the L1 that caches the matrix and factor streams (measured:
-// IC(0) CG at 499,288 rows 57.9 us per iteration with x in shared memory, 51.7 without).
+// The part's shared memory: r, p, q and t of its rows in the solve's arithmetic type V
+// (Jacobi / none: t = 1 / a_ii and a separate z; ILU / IC: z shares t's array, since a
+// row's forward result is dead once the backward sweep has read it and the backward sweep
+// reads only its own row's t), the mixed-precision solve's update d, the reduction scratch
+// and (kPartMetaSmem) the rows' entry ranges, diagonal positions and boundary flags.  x
+// stays in global memory: the smaller shared-memory carve-out leaves more of the SM's
+// 256 KB to the L1 that caches the matrix and factor streams (measured: IC(0) CG at
+// 499,288 rows 57.9 us per iteration with x in shared memory, 51.7 without).
+template <class V>
 struct PartSm {
-    double *r, *p, *q, *t, *z, *red;
+    V *r, *p, *q, *t, *z, *d;
+    double* red;
     const int* rp;   // np + 1 absolute entry positions
     const int* dg;   // diagonal positions
     const unsigned char* bnd;
@@ -1449,20 +1482,28 @@ struct PartSm {
 constexpr int kPartThreads = 1024;  // one block per SM
 constexpr bool kPartMetaSmem = true;
 
-// Shared-memory bytes of a part of R rows (the layout of part_sm; tri: z shares t).
-__host__ __device__ constexpr size_t part_smem_bytes(int R, bool tri) {
-    return sizeof(double) * ((tri ? 4 : 5) * (size_t)R + 2 * kPartThreads) +
+__host__ __device__ constexpr size_t part_vec_bytes(int R, bool tri, size_t vsz, bool mixed) {
+    return ((4 + (tri ? 0 : 1) + (mixed ? 1 : 0)) * (size_t)R * vsz + 15) / 16 * 16;
+}
+
+// Shared-memory bytes of a part of R rows (the layout of part_sm).
+__host__ __device__ constexpr size_t part_smem_bytes(int R, bool tri, size_t vsz, bool mixed) {
+    return part_vec_bytes(R, tri, vsz, mixed) + sizeof(double) * 2 * kPartThreads +
            (kPartMetaSmem ? sizeof(int) * (2 * (size_t)R + 1) + (size_t)R : 0);
 }
 
-__device__ __forceinline__ PartSm part_sm(const PartCg& C, double* base, int R, bool tri, int p0) {
-    PartSm S;
-    S.r = base;
-    S.p = base + R;
-    S.q = base + 2 * R;
-    S.t = base + 3 * R;
-    S.z = tri ? S.t : base + 4 * R;
-    S.red = base + (tri ? 4 : 5) * R;
+template <class V>
+__device__ __forceinline__ PartSm<V> part_sm(const PartCg& C, unsigned char* base, int R, bool tri, bool mixed,
+                                             int p0) {
+    PartSm<V> S;
+    V* v = reinterpret_cast<V*>(base);
+    S.r = v;
+    S.p = v + R;
+    S.q = v + 2 * R;
+    S.t = v + 3 * R;
+    S.z = tri ? S.t : v + 4 * R;
+    S.d = mixed ? v + (tri ? 4 : 5) * R : nullptr;
+    S.red = reinterpret_cast<double*>(base + part_vec_bytes(R, tri, sizeof(V), mixed));
     if (kPartMetaSmem) {
         int* rp = reinterpret_cast<int*>(S.red + 2 * kPartThreads);
         S.rp = rp;
@@ -1476,149 +1517,134 @@ __device__ __forceinline__ PartSm part_sm(const PartCg& C, double* base, int R, 
     return S;
 }
 
-// Grid-wide sums of NV <= 2 values, fused with the grid barrier, for blocks of
-// kPartThreads threads (a multiple of 128, at most 1024).  The block's values go to shared
-// memory and a fixed tree adds them with few FP64 instructions (one FP64 warp instruction
-// per ~64 clocks on an SM sub-partition, against five per value in every warp for warp
-// butterflies): a quarter of the threads per value add 4 values each, a sixteenth add 4 of
-// those, one warp adds up to 2 and finishes with a butterfly.  Thread 0 stores the block
-// sums in one of two partial arrays (by the barrier's parity) and arrives on the grid
-// barrier; after the release warp j adds value j's partials in block order (lane l:
-// partials l, l + 32, ...; butterfly).  The order depends on no arrival order: the sums
-// are reproducible bit for bit.
-template <int NV>
-__device__ __forceinline__ bool part_reduce(const GridBarrier& b, double (&v)[NV], double* sh, double* red) {
+// The matrix, factor and boundary arrays of the solve's arithmetic type.
+template <class V> struct PartVecs;
+template <> struct PartVecs<double> {
+    __device__ static const double* val(const PartCg& C) { return C.val; }
+    __device__ static const double* f(const PartCg& C) { return C.f; }
+    __device__ static double* gp(const PartCg& C) { return C.gp; }
+    __device__ static double* gt(const PartCg& C) { return C.gt; }
+    __device__ static double* gz(const PartCg& C) { return C.gz; }
+};
+template <> struct PartVecs<float> {
+    __device__ static const float* val(const PartCg& C) { return C.val32; }
+    __device__ static const float* f(const PartCg& C) { return C.f32; }
+    __device__ static float* gp(const PartCg& C) { return C.gp32; }
+    __device__ static float* gt(const PartCg& C) { return C.gt32; }
+    __device__ static float* gz(const PartCg& C) { return C.gz32; }
+};
+
+// Grid-wide sums of NV <= 2 values for the partitioned kernels (grid_reduce_tree on
+// kPartThreads threads; red: 2 x kPartThreads doubles of the part's shared memory).
+template <int NV, class Post = NoPost>
+__device__ __forceinline__ bool part_reduce(const GridBarrier& b, double (&v)[NV], double* sh, double* red,
+                                            Post post = Post()) {
     static_assert(NV >= 1 && NV <= 2, "part_reduce sums one or two values");
-    static_assert(kPartThreads % 128 == 0 && kPartThreads <= 1024, "block size of the tree");
-    __shared__ int s_ok, s_par;
-    constexpr int BT = kPartThreads;
-    const unsigned G = gridDim.x;
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    unsigned c0 = 0;
-    if (tid == 0) c0 = ld_relaxed_gpu(b.count);
-    __syncthreads();  // the previous call's readers of red and sh are done
-#pragma unroll
-    for (int j = 0; j < NV; ++j) red[j * BT + tid] = v[j];
-    __syncthreads();
-    if (tid < NV * (BT / 4)) {
-        const int j = tid / (BT / 4), u = tid % (BT / 4);
-        double* c = red + j * BT + u;
-        c[0] = ((c[0] + c[BT / 4]) + c[BT / 2]) + c[3 * BT / 4];
-    }
-    __syncthreads();
-    if (tid < NV * (BT / 16)) {
-        const int j = tid / (BT / 16), u = tid % (BT / 16);
-        double* c = red + j * BT + u;
-        c[0] = ((c[0] + c[BT / 16]) + c[BT / 8]) + c[3 * BT / 16];
-    }
-    __syncthreads();
-    if (w < NV) {
-        const double s = warp_sum(red[w * BT + lane] + (lane + 32 < BT / 16 ? red[w * BT + lane + 32] : 0.0));
-        if (lane == 0) sh[w] = s;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const unsigned kb = c0 / G;
-        double* part = b.part + (size_t)(kb & 1u) * 4 * G;
-#pragma unroll
-        for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], sh[j]);
-        s_ok = arrive_and_wait(b, c0, G) ? 1 : 0;
-        s_par = (int)(kb & 1u);
-    }
-    __syncthreads();
-    if (w < NV) {
-        const double* part = b.part + (size_t)s_par * 4 * G + w * G;
-        double t = 0.0;
-        for (unsigned q = lane; q < G; q += 32) t += __ldcg(&part[q]);
-        t = warp_sum(t);
-        if (lane == 0) sh[16 + w] = t;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < NV; ++j) v[j] = sh[16 + j];
-    return s_ok != 0;
+    return grid_reduce_tree<kPartThreads, NV>(b, v, sh, red, post);
 }
 
 // v[j] for row j of a sweep: the part's own rows from shared memory, other parts' rows
 // from the global copy, polled on the pending marker (bounded).  A failed wait records
 // DEV_TIMEOUT and yields 0: the caller goes on to the next __syncthreads and the kernel
 // returns at its next grid barrier.
-__device__ __forceinline__ double part_dep(int j, int p0, int np, const double* sv, const double* gv, int* err,
-                                           int* rec, int row) {
+template <class V>
+__device__ __forceinline__ V part_dep(int j, int p0, int np, const V* sv, const V* gv, int* err, int* rec, int row) {
     if ((unsigned)(j - p0) < (unsigned)np) return sv[j - p0];
-    double v = *(volatile const double*)&gv[j];
-    if (Pending<double>::bits(v) == Pending<double>::kBits && !wait_value(gv, j, v, err, rec, row)) v = 0.0;
+    V v = *(volatile const V*)&gv[j];
+    if (Pending<V>::bits(v) == Pending<V>::kBits && !wait_value(gv, j, v, err, rec, row)) v = V(0);
     return v;
 }
 
 // q = A p over the part's rows (each row's entries in order, as spmv_rows); other parts'
-// p from the global copy.  Returns the thread's p.q terms.
-__device__ __forceinline__ double part_spmv(const PartCg& C, const PartSm& S, int p0, int np) {
+// p from the global copy.  Returns the thread's p.q terms (in FP64).
+template <class V>
+__device__ __forceinline__ double part_spmv(const PartCg& C, const PartSm<V>& S, int p0, int np) {
+    const V* val = PartVecs<V>::val(C);
+    const V* gp = PartVecs<V>::gp(C);
     double pq = 0.0;
     for (int l = threadIdx.x; l < np; l += kPartThreads) {
         const int s = S.rp[l], e = S.rp[l + 1];
-        double acc = 0.0;
+        V acc = V(0);
         for (int k = s; k < e; ++k) {
             const int j = __ldg(&C.col[k]);
-            const double pj = (unsigned)(j - p0) < (unsigned)np ? S.p[j - p0] : __ldcg(&C.gp[j]);
-            acc += __ldg(&C.val[k]) * pj;
+            const V pj = (unsigned)(j - p0) < (unsigned)np ? S.p[j - p0] : __ldcg(&gp[j]);
+            acc += __ldg(&val[k]) * pj;
         }
         S.q[l] = acc;
-        pq += S.p[l] * acc;
+        pq += (double)S.p[l] * (double)acc;
     }
     return pq;
 }
 
 // A sweep row's dependency entries and pivot pulled into L1 before the group's barrier
 // (they do not depend on the earlier groups).
+template <class V>
 __device__ __forceinline__ void sweep_prefetch(const PartCg& C, int k0, int k1, int d) {
+    const V* f = PartVecs<V>::f(C);
     if (k1 > k0) {
         prefetch_l1(&C.col[k0]);
-        prefetch_l1(&C.f[k0]);
+        prefetch_l1(&f[k0]);
     }
-    prefetch_l1(&C.f[d]);
+    prefetch_l1(&f[d]);
 }
 
-// sum_k f_k v[col_k] over the dependency entries [k0, k1), in entry order.
-__device__ __forceinline__ double sweep_sum(const PartCg& C, int k0, int k1, int p0, int np, const double* sv,
-                                            const double* gv, int* err, int* rec, int row) {
-    double sum = 0.0;
-    for (int k = k0; k < k1; ++k) sum += __ldg(&C.f[k]) * part_dep(__ldg(&C.col[k]), p0, np, sv, gv, err, rec, row);
+// sum_k f_k v[col_k] over the dependency entries [k0, k1), in entry order; LOCAL (the
+// partition-local factors, zero outside the part): the part's own entries only.
+template <class V, bool LOCAL = false>
+__device__ __forceinline__ V sweep_sum(const PartCg& C, int k0, int k1, int p0, int np, const V* sv, const V* gv,
+                                       int* err, int* rec, int row) {
+    const V* f = PartVecs<V>::f(C);
+    V sum = V(0);
+    for (int k = k0; k < k1; ++k) {
+        const int j = __ldg(&C.col[k]);
+        if (LOCAL && (unsigned)(j - p0) >= (unsigned)np) continue;
+        sum += __ldg(&f[k]) * part_dep(j, p0, np, sv, gv, err, rec, row);
+    }
     return sum;
 }
 
-// Forward sweep over the part's groups (csr_fwd): first: t = L^{-1} r; else first the
-// updates r -= alpha q, x += alpha p.  Returns the r.r terms (want_rr) and the t.t terms.
-template <bool IC>
-__device__ double2 part_fwd(const PartCg& C, const PartSm& S, int p0, int np, bool first, double alpha, bool want_rr,
+// Forward sweep over the part's groups (csr_fwd): first: t = L^{-1} r; else the updates
+// r -= alpha q and x += alpha p (MIXED: the inner update d += alpha p) with it.  Returns
+// the r.r terms (want_rr) and the t.t terms, in FP64.  LOCAL: partition-local factors, no
+// boundary copies.
+template <bool IC, class V = double, bool MIXED = false, bool LOCAL = false>
+__device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np, bool first, V alpha, bool want_rr,
                             int* err, int* rec) {
+    V* gt = PartVecs<V>::gt(C);
+    V* gz = PartVecs<V>::gz(C);
+    const V* f = PartVecs<V>::f(C);
     double rr = 0.0, tt = 0.0;
     const int* qs = C.qs + blockIdx.x * C.ng;
     for (int g = 0; g < C.ng; ++g) {
         const int g0 = qs[g] - p0, g1 = qs[g + 1] - p0;
         if (g0 + (int)threadIdx.x < g1) {
             const int l = g0 + threadIdx.x;
-            sweep_prefetch(C, S.rp[l], S.dg[l], S.dg[l]);
+            sweep_prefetch<V>(C, S.rp[l], S.dg[l], S.dg[l]);
         }
         __syncthreads();  // the part's earlier groups are done
         for (int l = g0 + threadIdx.x; l < g1; l += kPartThreads) {
             const int d = S.dg[l];
-            double ra = S.r[l];
+            V ra = S.r[l];
             if (!first) {
                 ra -= alpha * S.q[l];
                 S.r[l] = ra;
             }
-            if (want_rr) rr += ra * ra;
-            const double sum = sweep_sum(C, S.rp[l], d, p0, np, S.t, C.gt, err, rec, p0 + l);
-            const double v = IC ? (ra - sum) * __ldg(&C.f[d]) : ra - sum;
+            if (want_rr) rr += (double)ra * (double)ra;
+            const V sum = sweep_sum<V, LOCAL>(C, S.rp[l], d, p0, np, S.t, gt, err, rec, p0 + l);
+            const V v = IC ? (ra - sum) * __ldg(&f[d]) : ra - sum;
             S.t[l] = v;
-            if (S.bnd[l]) {
-                __stcg(&C.gt[p0 + l], v);
-                __stcg(&C.gz[p0 + l], Pending<double>::marker());
+            if (!LOCAL && S.bnd[l]) {
+                __stcg(&gt[p0 + l], v);
+                __stcg(&gz[p0 + l], Pending<V>::marker());
             }
-            tt += v * v;
+            tt += (double)v * (double)v;
             // x += alpha p last: its global load is off the sweep's dependency chain
-            if (!first) __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + alpha * S.p[l]);
+            if (!first) {
+                if (MIXED)
+                    S.d[l] = S.d[l] + alpha * S.p[l];
+                else
+                    __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + (double)alpha * (double)S.p[l]);
+            }
         }
     }
     return make_double2(rr, tt);
@@ -1626,53 +1652,63 @@ __device__ double2 part_fwd(const PartCg& C, const PartSm& S, int p0, int np, bo
 
 // Backward sweep over the part's groups in reverse (csr_bwd): z = U^{-1} t; PMODE 0: no
 // direction, 1: p = z (the first), 2: p = z + beta p (IC's three-step iteration).
-// Returns the r.z terms (PMODE != 2).
-template <int PMODE>
-__device__ double part_bwd(const PartCg& C, const PartSm& S, int p0, int np, double beta, int* err, int* rec) {
+// Returns the r.z terms (PMODE != 2), in FP64.  LOCAL: partition-local factors.
+template <int PMODE, class V = double, bool LOCAL = false>
+__device__ double part_bwd(const PartCg& C, const PartSm<V>& S, int p0, int np, V beta, int* err, int* rec) {
+    V* gp = PartVecs<V>::gp(C);
+    V* gt = PartVecs<V>::gt(C);
+    V* gz = PartVecs<V>::gz(C);
+    const V* f = PartVecs<V>::f(C);
     double rz = 0.0;
     const int* qs = C.qs + blockIdx.x * C.ng;
     for (int g = C.ng - 1; g >= 0; --g) {
         const int g0 = qs[g] - p0, g1 = qs[g + 1] - p0;
         if (g0 + (int)threadIdx.x < g1) {
             const int l = g0 + threadIdx.x;
-            sweep_prefetch(C, S.dg[l] + 1, S.rp[l + 1], S.dg[l]);
+            sweep_prefetch<V>(C, S.dg[l] + 1, S.rp[l + 1], S.dg[l]);
         }
         __syncthreads();  // the part's later groups are done
         for (int l = g0 + threadIdx.x; l < g1; l += kPartThreads) {
             const int d = S.dg[l];
-            const double in = S.t[l];
-            const double sum = sweep_sum(C, d + 1, S.rp[l + 1], p0, np, S.z, C.gz, err, rec, p0 + l);
-            const double v = (in - sum) * __ldg(&C.f[d]);
+            const V in = S.t[l];
+            const V sum = sweep_sum<V, LOCAL>(C, d + 1, S.rp[l + 1], p0, np, S.z, gz, err, rec, p0 + l);
+            const V v = (in - sum) * __ldg(&f[d]);
             S.z[l] = v;
-            double pn = 0.0;
+            V pn = V(0);
             if (PMODE == 1) pn = v;
             if (PMODE == 2) pn = fma_rn(beta, S.p[l], v);
             if (PMODE) S.p[l] = pn;
             if (S.bnd[l]) {
-                __stcg(&C.gz[p0 + l], v);
-                if (PMODE) __stcg(&C.gp[p0 + l], pn);
-                __stcg(&C.gt[p0 + l], Pending<double>::marker());
+                if (!LOCAL) {
+                    __stcg(&gz[p0 + l], v);
+                    __stcg(&gt[p0 + l], Pending<V>::marker());
+                }
+                if (PMODE) __stcg(&gp[p0 + l], pn);
             }
-            if (PMODE != 2) rz += S.r[l] * v;
+            if (PMODE != 2) rz += (double)S.r[l] * (double)v;
         }
     }
     return rz;
 }
 
-// MODE 0: Jacobi or no preconditioner (k_pcg's iteration: p.q reduction, x/r/z update
-// with r.z, p update and barrier); 1: IC(0) (pcg_csr's three grid-wide steps); 2: ILU(0)
-// (pcg_csr's four).
-template <int MODE>
-__device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
+// p = z + beta p over the part's rows (p_update), boundary rows also to the global copy.
+template <class V>
+__device__ __forceinline__ void part_p_update(const PartCg& C, const PartSm<V>& S, int p0, int np, V beta) {
+    V* gp = PartVecs<V>::gp(C);
+    for (int l = threadIdx.x; l < np; l += kPartThreads) {
+        const V pn = S.z[l] + beta * S.p[l];
+        S.p[l] = pn;
+        if (S.bnd[l]) __stcg(&gp[p0 + l], pn);
+    }
+}
+
+// The part's row metadata to shared memory and x (A's numbering) to the global iterate in
+// Q order.
+template <class V>
+__device__ __forceinline__ void part_load(const KArgs& a, const PartSm<V>& S, int p0, int p1) {
     const PartCg& C = a.part;
-    const int p0 = C.qs[blockIdx.x * C.ng], p1 = C.qs[(blockIdx.x + 1) * C.ng], np = p1 - p0;
-    const PartSm S = part_sm(C, smem, C.R, MODE != 0, p0);
-    const int tid = threadIdx.x;
-    int* err = a.bar.err;
-    int* rec = a.bar.rec;
-    const bool rel = a.criterion == PF2_CRITERION_REL;
-    const bool jac = a.precond == PF2_PRECOND_JACOBI;
-    for (int l = tid; l < np; l += kPartThreads) {
+    const int np = p1 - p0;
+    for (int l = threadIdx.x; l < np; l += kPartThreads) {
         const int i = p0 + l;
         if (kPartMetaSmem) {
             const_cast<int*>(S.rp)[l] = __ldg(&C.rp[i]);
@@ -1681,14 +1717,37 @@ __device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
         }
         __stcg(&C.x[i], a.x[__ldg(&C.qa[i])]);
     }
-    if (kPartMetaSmem && tid == 0) const_cast<int*>(S.rp)[np] = __ldg(&C.rp[p1]);
+    if (kPartMetaSmem && threadIdx.x == 0) const_cast<int*>(S.rp)[np] = __ldg(&C.rp[p1]);
+}
+
+// b - A x in FP64 for the part's row l (x from the global iterate in Q order).
+__device__ __forceinline__ double part_residual(const KArgs& a, const int* rp, int p0, int l, double& bi) {
+    const PartCg& C = a.part;
+    bi = a.b[__ldg(&C.qa[p0 + l])];
+    double v = 0.0;
+    for (int k = rp[l]; k < rp[l + 1]; ++k) v += __ldg(&C.val[k]) * __ldcg(&C.x[__ldg(&C.col[k])]);
+    return bi - v;
+}
+
+// MODE 0: Jacobi or no preconditioner (k_pcg's iteration: p.q reduction, x/r/z update
+// with r.z, p update and barrier); 1: IC(0) (pcg_csr's three grid-wide steps); 2: ILU(0)
+// (pcg_csr's four).
+template <int MODE>
+__device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
+    const PartCg& C = a.part;
+    const int p0 = C.qs[blockIdx.x * C.ng], p1 = C.qs[(blockIdx.x + 1) * C.ng], np = p1 - p0;
+    const PartSm<double> S = part_sm<double>(C, smem, C.R, MODE != 0, false, p0);
+    const int tid = threadIdx.x;
+    int* err = a.bar.err;
+    int* rec = a.bar.rec;
+    const bool rel = a.criterion == PF2_CRITERION_REL;
+    const bool jac = a.precond == PF2_PRECOND_JACOBI;
+    part_load(a, S, p0, p1);
     if (!grid_sync(a.bar, gridDim.x)) return;
     double red[3] = { 0.0, 0.0, 0.0 };  // r.z, b.b, r.r
     for (int l = tid; l < np; l += kPartThreads) {
-        const double bi = a.b[__ldg(&C.qa[p0 + l])];
-        double v = 0.0;
-        for (int k = S.rp[l]; k < S.rp[l + 1]; ++k) v += __ldg(&C.val[k]) * __ldcg(&C.x[__ldg(&C.col[k])]);
-        S.r[l] = bi - v;
+        double bi;
+        S.r[l] = part_residual(a, S.rp, p0, l, bi);
         red[1] += bi * bi;
         if (MODE == 0) S.t[l] = 1.0 / __ldg(&C.val[S.dg[l]]);
     }
@@ -1709,19 +1768,24 @@ __device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
         red[0] = part_bwd<1>(C, S, p0, np, 0.0, err, rec);
     }
     double r2[2] = { red[0], red[1] }, r1[1] = { red[2] };
-    if (!part_reduce<2>(a.bar, r2, sh, S.red) || !part_reduce<1>(a.bar, r1, sh, S.red)) return;
+    if (!part_reduce<2>(a.bar, r2, sh, S.red)) return;
+    // bnorm and the first test (thread 0; see part_reduce)
+    if (!part_reduce<1>(a.bar, r1, sh, S.red, [&](const double* tot, double* out) {
+            out[0] = sqrt(r2[1]);
+            out[1] = rel ? (sqrt(tot[0]) <= a.tol * out[0]) : (r2[0] < a.tol * a.tol);
+        }))
+        return;
     double gamma = r2[0];
-    const double bnorm = sqrt(r2[1]);
+    const double bnorm = sh[24];
     double rr = r1[0];
-    const double tol2 = a.tol * a.tol;
-    auto done_test = [&](double gm, double rr_) { return rel ? (sqrt(rr_) <= a.tol * bnorm) : (gm < tol2); };
     int it = 0;
-    bool conv = done_test(gamma, rr);
+    bool conv = sh[25] != 0.0;
     while (!conv && it < a.maxit) {
         ++it;
         double pq[1] = { part_spmv(C, S, p0, np) };
-        if (!part_reduce<1>(a.bar, pq, sh, S.red)) return;
-        const double alpha = gamma / pq[0];
+        if (!part_reduce<1>(a.bar, pq, sh, S.red, [&](const double* tot, double* out) { out[0] = gamma / tot[0]; }))
+            return;
+        const double alpha = sh[24];
         // with the absolute criterion (a test of r.z alone) r.r is reduced once after the loop
         double g2[2] = { 0.0, 0.0 };  // r.z (IC: t.t), r.r
         if (MODE == 0) {
@@ -1743,27 +1807,31 @@ __device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
             if (!grid_sync(a.bar, gridDim.x)) return;
             g2[0] = part_bwd<0>(C, S, p0, np, 0.0, err, rec);
         }
+        // the test and beta = r.z / (previous r.z) (thread 0; see part_reduce)
         if (rel) {
-            if (!part_reduce<2>(a.bar, g2, sh, S.red)) return;
+            if (!part_reduce<2>(a.bar, g2, sh, S.red, [&](const double* tot, double* out) {
+                    out[0] = sqrt(tot[1]) <= a.tol * bnorm;
+                    out[1] = tot[0] / gamma;
+                }))
+                return;
             rr = g2[1];
         } else {
             double g1[1] = { g2[0] };
-            if (!part_reduce<1>(a.bar, g1, sh, S.red)) return;
+            if (!part_reduce<1>(a.bar, g1, sh, S.red, [&](const double* tot, double* out) {
+                    out[0] = tot[0] < a.tol * a.tol;
+                    out[1] = tot[0] / gamma;
+                }))
+                return;
             g2[0] = g1[0];
         }
         const double gnew = g2[0];
-        if (done_test(gnew, rr)) { gamma = gnew; conv = true; break; }
-        const double beta = gnew / gamma;
+        if (sh[24] != 0.0) { gamma = gnew; conv = true; break; }
+        const double beta = sh[25];
         gamma = gnew;
-        if (MODE == 1) {
+        if (MODE == 1)
             part_bwd<2>(C, S, p0, np, beta, err, rec);
-        } else {
-            for (int l = tid; l < np; l += kPartThreads) {
-                const double pn = S.z[l] + beta * S.p[l];
-                S.p[l] = pn;
-                if (S.bnd[l]) __stcg(&C.gp[p0 + l], pn);
-            }
-        }
+        else
+            part_p_update(C, S, p0, np, beta);
         if (!grid_sync(a.bar, gridDim.x)) return;
     }
     if (!rel && it > 0) {
@@ -1782,11 +1850,153 @@ __device__ void pcg_part(const KArgs& a, double* sh, double* smem) {
     }
 }
 
+// Mixed-precision CG on the parts (pcg_csr_mixed's algorithm): FP32 SpMV, FP32 IC(0) or
+// ILU(0) sweeps and FP32 vectors in shared memory, FP64-accumulated dot products, inside an
+// FP64 iterative refinement: when the iterated residual has dropped by inner_eta (or
+// below the target) the update d is added to x in FP64, r = b - A x is recomputed in FP64
+// with A's FP64 values, and the relative test ||r|| <= tol ||b|| runs in FP64; CG then
+// continues from the true residual, keeping its search direction.  LOCAL: the factors of
+// each part's diagonal block alone (IC(0) / ILU(0) of A with the couplings between parts
+// dropped, a block-Jacobi preconditioner with one block per part): the sweeps wait on no
+// other part and run in shared memory only; the FP64 refinement keeps the solve's target.
+template <bool IC, bool LOCAL>
+__device__ void pcg_part_mixed(const KArgs& a, double* sh, unsigned char* smem) {
+    const PartCg& C = a.part;
+    const int p0 = C.qs[blockIdx.x * C.ng], p1 = C.qs[(blockIdx.x + 1) * C.ng], np = p1 - p0;
+    const PartSm<float> S = part_sm<float>(C, smem, C.R, true, true, p0);
+    const int tid = threadIdx.x;
+    int* err = a.bar.err;
+    int* rec = a.bar.rec;
+    part_load(a, S, p0, p1);
+    for (int l = tid; l < np; l += kPartThreads) S.d[l] = 0.0f;
+    if (!grid_sync(a.bar, gridDim.x)) return;
+    // r = b - A x in FP64; the refinement's form
+    auto residual = [&](double& rr_, double* bb_) {
+        for (int l = tid; l < np; l += kPartThreads) {
+            double bi;
+            const double ri = part_residual(a, S.rp, p0, l, bi);
+            S.r[l] = (float)ri;
+            rr_ += ri * ri;
+            if (bb_) *bb_ += bi * bi;
+        }
+    };
+    double red[2] = { 0.0, 0.0 };  // b.b, r.r
+    residual(red[1], &red[0]);
+    // square roots by thread 0 (see part_reduce)
+    if (!part_reduce<2>(a.bar, red, sh, S.red, [&](const double* tot, double* out) {
+            out[0] = sqrt(tot[0]);
+            out[1] = sqrt(tot[1]);
+        }))
+        return;
+    const double bnorm = sh[24];
+    const double target = a.tol * bnorm;
+    double rnorm = sh[25];
+    double rlast = rnorm;
+    int it = 0, refinements = 1;
+    bool conv = rnorm <= target;
+    if (!conv) {
+        // z = M^{-1} r, p = z, gamma = r.z
+        part_fwd<IC, float, true, LOCAL>(C, S, p0, np, true, 0.0f, false, err, rec);
+        if (!grid_sync(a.bar, gridDim.x)) return;
+        double g[1] = { part_bwd<1, float, LOCAL>(C, S, p0, np, 0.0f, err, rec) };
+        if (!part_reduce<1>(a.bar, g, sh, S.red)) return;
+        double gamma = g[0];
+        while (it < a.maxit) {
+            double pq[1] = { part_spmv(C, S, p0, np) };
+            ++it;
+            if (!part_reduce<1>(a.bar, pq, sh, S.red, [&](const double* tot, double* out) {
+                    out[0] = (double)(float)(gamma / tot[0]);
+                }))
+                return;
+            const float alpha = (float)sh[24];
+            double g2[2];  // r.z (IC: t.t), r.r
+            if (IC) {
+                const double2 f = part_fwd<true, float, true, LOCAL>(C, S, p0, np, false, alpha, true, err, rec);
+                g2[0] = f.y;
+                g2[1] = f.x;
+            } else {
+                g2[1] = part_fwd<false, float, true, LOCAL>(C, S, p0, np, false, alpha, true, err, rec).x;
+                if (!LOCAL && !grid_sync(a.bar, gridDim.x)) return;
+                g2[0] = part_bwd<0, float, LOCAL>(C, S, p0, np, 0.0f, err, rec);
+            }
+            // refinement test and beta (thread 0; see part_reduce)
+            if (!part_reduce<2>(a.bar, g2, sh, S.red, [&](const double* tot, double* out) {
+                    const double rit = sqrt(tot[1]);
+                    out[0] = rit <= a.inner_eta * rlast || rit <= target;
+                    out[1] = (double)(float)(tot[0] / gamma);
+                }))
+                return;
+            double gnew = g2[0];
+            float beta = (float)sh[25];
+            if (sh[24] != 0.0) {
+                // refinement: x += d, r = b - A x and the test in FP64; the boundary rows'
+                // forward results back to the marker for the forward sweep on the new r
+                for (int l = tid; l < np; l += kPartThreads) {
+                    __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + (double)S.d[l]);
+                    S.d[l] = 0.0f;
+                    if (!LOCAL && S.bnd[l]) __stcg(&C.gt32[p0 + l], Pending<float>::marker());
+                }
+                if (!grid_sync(a.bar, gridDim.x)) return;
+                double rr[1] = { 0.0 };
+                residual(rr[0], nullptr);
+                if (!part_reduce<1>(a.bar, rr, sh, S.red, [&](const double* tot, double* out) {
+                        out[0] = sqrt(tot[0]);
+                    }))
+                    return;
+                ++refinements;
+                rnorm = sh[24];
+                if (rnorm <= target) { conv = true; break; }
+                rlast = rnorm;
+                // continue from the true residual, keeping the search direction
+                double g3[1];
+                if (IC) {
+                    g3[0] = part_fwd<true, float, true, LOCAL>(C, S, p0, np, true, 0.0f, false, err, rec).y;
+                } else {
+                    part_fwd<false, float, true, LOCAL>(C, S, p0, np, true, 0.0f, false, err, rec);
+                    if (!LOCAL && !grid_sync(a.bar, gridDim.x)) return;
+                    g3[0] = part_bwd<0, float, LOCAL>(C, S, p0, np, 0.0f, err, rec);
+                }
+                if (!part_reduce<1>(a.bar, g3, sh, S.red, [&](const double* tot, double* out) {
+                        out[0] = (double)(float)(tot[0] / gamma);
+                    }))
+                    return;
+                gnew = g3[0];
+                beta = (float)sh[24];
+            }
+            gamma = gnew;
+            if (IC)
+                part_bwd<2, float, LOCAL>(C, S, p0, np, beta, err, rec);
+            else
+                part_p_update(C, S, p0, np, beta);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+        }
+        if (!conv)  // iteration limit: keep the accumulated update
+            for (int l = tid; l < np; l += kPartThreads)
+                __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + (double)S.d[l]);
+    }
+    for (int l = tid; l < np; l += kPartThreads) a.x[__ldg(&C.qa[p0 + l])] = __ldcg(&C.x[p0 + l]);
+    if (blockIdx.x == 0 && tid == 0) {
+        a.out->iterations = it;
+        a.out->converged = conv ? 1 : 0;
+        a.out->residual = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->relres = rnorm / (bnorm > 0 ? bnorm : 1.0);
+        a.out->status = conv ? DEV_OK : DEV_NOT_CONVERGED;
+        a.out->pad = refinements;
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kPartThreads, 1) k_pcg_part(KArgs a) {
     __shared__ double sh[kShDoubles];
-    extern __shared__ double part_smem[];
+    extern __shared__ __align__(16) unsigned char part_smem[];
     pcg_part<MODE>(a, sh, part_smem);
+}
+
+template <bool IC, bool LOCAL>
+__global__ void __launch_bounds__(kPartThreads, 1) k_pcg_part_mixed(KArgs a) {
+    __shared__ double sh[kShDoubles];
+    extern __shared__ __align__(16) unsigned char part_smem[];
+    pcg_part_mixed<IC, LOCAL>(a, sh, part_smem);
 }
 
 
@@ -2547,12 +2757,16 @@ struct pf2_solver {
     // positions of its entries in A (values) and in B (factors), Q -> A rows, boundary
     // flags, x in Q order and the boundary rows' global copies of p, t, z
     bool part = false;
+    bool part_local = false;  // mixed precision: partition-local factors (A's values through bmap_local)
+    DevBuf<int> bmap_local;   // bmap with the entries that couple two parts set to -1
+    const char* part_why = "not planned";  // why the partitioned kernel does not apply
     int part_P = 0, part_R = 0, part_ng = 0;
     size_t part_smem = 0;
     long long part_boundary_rows = 0;
     DevBuf<int> q_s, q_rp, q_col, q_diag, q_a, q_amap, q_fmap;
     DevBuf<unsigned char> q_bnd;
     DevBuf<double> q_val, q_f, q_x, q_gp, q_gt, q_gz;
+    DevBuf<float> q_val32, q_f32, q_gp32, q_gt32, q_gz32;  // mixed precision
     bool factored = false;
     const pf2_csr* last = nullptr;  // matrix of the last setup / solve
 };
@@ -2751,7 +2965,10 @@ static pf2_status build_part_plan(pf2_solver* S, const std::vector<int>& rp, con
     if (tri)  // the rows of a group must depend only on earlier groups
         for (int r = 0; r < n; ++r)
             for (int k = brp[r]; k < bdiag[r]; ++k)
-                if (grp[bcol[k]] >= grp[r]) return PF2_OK;
+                if (grp[bcol[k]] >= grp[r]) {
+                    S->part_why = "a sweep group's rows depend on one another";
+                    return PF2_OK;
+                }
     int P = std::max(1, std::min(num_sms(), n / kPartMinRows));
     if (const char* e = getenv("PF2_CG_PARTS")) P = std::max(1, std::min(num_sms(), atoi(e)));  // tests, tuning
     std::vector<int> part;
@@ -2781,8 +2998,12 @@ static pf2_status build_part_plan(pf2_solver* S, const std::vector<int>& rp, con
     for (int p = 0; p < P; ++p) R = std::max(R, qs[(size_t)(p + 1) * ng] - qs[(size_t)p * ng]);
     int optin = 0;
     PF2_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
-    const size_t smem = (part_smem_bytes(R, tri) + 15) / 16 * 16;
-    if (smem + 2048 > (size_t)optin) return PF2_OK;
+    const bool mixed = S->opt.precision == PF2_PRECISION_MIXED;
+    const size_t smem = (part_smem_bytes(R, tri, mixed ? sizeof(float) : sizeof(double), mixed) + 15) / 16 * 16;
+    if (smem + 2048 > (size_t)optin) {
+        S->part_why = "a part's vectors exceed the shared memory of a block";
+        return PF2_OK;
+    }
     std::vector<int> qrp(n + 1, 0), qcol(std::max(nnz, 1)), qdiag(n), qamap(std::max(nnz, 1)),
         qfmap(std::max(nnz, 1));
     std::vector<unsigned char> bnd(n, 0);
@@ -2823,6 +3044,28 @@ static pf2_status build_part_plan(pf2_solver* S, const std::vector<int>& rp, con
     PF2_TRY(S->q_gp.alloc(n));
     PF2_TRY(S->q_gt.alloc(n));
     PF2_TRY(S->q_gz.alloc(n));
+    // mixed precision, PF2_CG_PART_LOCAL=1: partition-local factors (block-Jacobi IC(0) /
+    // ILU(0), one block per part).  Not the default: at 499,288 rows (152 parts) the sweeps
+    // get 17 % cheaper but the solve takes twice the iterations (1,428 against 712 to 1e-8)
+    S->part_local = false;
+    if (mixed && tri) {
+        const char* e = getenv("PF2_CG_PART_LOCAL");
+        if (e && atoi(e) != 0) {
+            std::vector<int> bl(std::max(nnz, 1));
+            for (int r = 0; r < n; ++r)
+                for (int k = brp[r]; k < brp[r + 1]; ++k)
+                    bl[k] = part[perm[bcol[k]]] == part[perm[r]] ? bmap[k] : -1;
+            PF2_TRY(up(S->bmap_local, bl));
+            S->part_local = true;
+        }
+    }
+    if (mixed) {
+        PF2_TRY(S->q_val32.alloc(std::max(nnz, 1)));
+        PF2_TRY(S->q_f32.alloc(std::max(nnz, 1)));
+        PF2_TRY(S->q_gp32.alloc(n));
+        PF2_TRY(S->q_gt32.alloc(n));
+        PF2_TRY(S->q_gz32.alloc(n));
+    }
     S->part = true;
     S->part_P = P;
     S->part_R = R;
@@ -2832,17 +3075,26 @@ static pf2_status build_part_plan(pf2_solver* S, const std::vector<int>& rp, con
     return PF2_OK;
 }
 
-// Whether a solve with these options may run as k_pcg_part: FP64 standard CG;
-// PF2_CG_PART=0 keeps the other kernels (tuning, comparisons).
+// Whether a solve with these options may run on the parts: standard CG, FP64 (k_pcg_part)
+// or, with ILU(0) / IC(0), mixed precision (k_pcg_part_mixed); PF2_CG_PART=0 keeps the
+// other kernels (tuning, comparisons).
 static bool part_eligible(const pf2_solver* S) {
     if (const char* e = getenv("PF2_CG_PART"))
         if (atoi(e) == 0) return false;
-    return S->opt.kind == PF2_SOLVER_CG && S->opt.precision == PF2_PRECISION_FP64 &&
-           S->opt.cg_variant == PF2_CG_STANDARD;
+    const bool tri = S->opt.precond == PF2_PRECOND_ILU || S->opt.precond == PF2_PRECOND_IC;
+    return S->opt.kind == PF2_SOLVER_CG && S->opt.cg_variant == PF2_CG_STANDARD &&
+           (S->opt.precision == PF2_PRECISION_FP64 || (S->opt.precision == PF2_PRECISION_MIXED && tri));
 }
 
 // The partitioned CG kernel of the solver's preconditioner.
 static void* part_kernel(const pf2_solver* S) {
+    if (S->opt.precision == PF2_PRECISION_MIXED) {
+        if (S->part_local)
+            return S->opt.precond == PF2_PRECOND_IC ? (void*)k_pcg_part_mixed<true, true>
+                                                    : (void*)k_pcg_part_mixed<false, true>;
+        return S->opt.precond == PF2_PRECOND_IC ? (void*)k_pcg_part_mixed<true, false>
+                                                : (void*)k_pcg_part_mixed<false, false>;
+    }
     if (S->opt.precond == PF2_PRECOND_IC) return (void*)k_pcg_part<1>;
     if (S->opt.precond == PF2_PRECOND_ILU) return (void*)k_pcg_part<2>;
     return (void*)k_pcg_part<0>;
@@ -3017,6 +3269,8 @@ static pf2_status build_tri_plan(pf2_solver* S) {
         }
         if (S->opt.ordering == PF2_ORDERING_MULTICOLOR && part_eligible(S))
             PF2_TRY(build_part_plan(S, rp, col, brp, bcol, bmap, bdiag, perm, groups, true));
+        else
+            S->part_why = "ILU(0) / IC(0) in the natural order";
     }
     if (K <= kBandMaxDeps) {
         const int R = banded ? std::min(n, band_rows) : n;
@@ -3121,10 +3375,13 @@ static bool uses_tri(const pf2_solver* S) {
 // Preconditioner::initialize(A): ILU/IC factorise a copy of A's values.
 __global__ void k_epoch_advance(int* epoch, int delta) { *epoch += delta; }
 
+// out[k] = val[map[k]] (0 where map[k] < 0).
 __global__ void k_gather_values(long long nnz, const double* __restrict__ val, const int* __restrict__ map,
                                 double* __restrict__ out) {
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x)
-        out[k] = val[map[k]];
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
+        const int m = map[k];
+        out[k] = m >= 0 ? val[m] : 0.0;
+    }
 }
 
 __global__ void k_inv_diag(int n, const double* __restrict__ val, const int* __restrict__ diag, double* invd) {
@@ -3172,8 +3429,9 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
         return PF2_OK;
     }
     if (!uses_tri(S)) return PF2_OK;
-    k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, A->val.p,
-                                                                                           S->bmap.p, S->fact.p);
+    // (partition-local factors: the entries coupling two parts factor as zeros)
+    k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
+        S->nnz, A->val.p, S->part_local ? S->bmap_local.p : S->bmap.p, S->fact.p);
     PF2_LAUNCH_CHECK();
     PF2_CUDA(cudaMemsetAsync(S->tickets.p, 0, sizeof(unsigned), st));
     PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
@@ -3200,6 +3458,11 @@ static pf2_status factorize(pf2_solver* S, const pf2_csr* A, cudaStream_t st) {
             k_gather_values<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(
                 S->nnz, S->fsym.p, S->q_fmap.p, S->q_f.p);
             PF2_LAUNCH_CHECK();
+            if (S->q_f32.p) {
+                k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->q_f.p,
+                                                                                                S->q_f32.p);
+                PF2_LAUNCH_CHECK();
+            }
         }
         if (mixed) {
             k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->fsym.p,
@@ -3306,8 +3569,16 @@ static pf2_status launch_solver(pf2_solver* S, const pf2_csr* A, double* x, cons
             PF2_CUDA(cudaMemsetAsync(S->q_gt.p, 0xff, S->q_gt.bytes(), st));
             PF2_CUDA(cudaMemsetAsync(S->q_gz.p, 0xff, S->q_gz.bytes(), st));
         }
+        if (S->q_val32.p) {
+            k_to_float<<<std::min((int)blocks_for(S->nnz), num_sms() * 8), kThreads, 0, st>>>(S->nnz, S->q_val.p,
+                                                                                            S->q_val32.p);
+            PF2_LAUNCH_CHECK();
+            PF2_CUDA(cudaMemsetAsync(S->q_gt32.p, 0xff, S->q_gt32.bytes(), st));
+            PF2_CUDA(cudaMemsetAsync(S->q_gz32.p, 0xff, S->q_gz32.bytes(), st));
+        }
         a.part = PartCg{ S->part_P, S->part_R, S->part_ng, S->q_s.p, S->q_rp.p, S->q_col.p, S->q_diag.p, S->q_a.p,
-                         S->q_bnd.p, S->q_val.p, S->q_f.p, S->q_x.p, S->q_gp.p, S->q_gt.p, S->q_gz.p };
+                         S->q_bnd.p, S->q_val.p, S->q_f.p, S->q_x.p, S->q_gp.p, S->q_gt.p, S->q_gz.p,
+                         S->q_val32.p, S->q_f32.p, S->q_gp32.p, S->q_gt32.p, S->q_gz32.p };
         PF2_CUDA(cudaMemsetAsync(S->bar.p, 0, 2 * sizeof(unsigned), st));
         PF2_CUDA(cudaMemsetAsync(S->err.p, 0, sizeof(int), st));
         PF2_CUDA(cudaMemsetAsync(S->rec.p, 0, 5 * sizeof(int), st));
@@ -3444,8 +3715,18 @@ pf2_status pf2_solver_create(const pf2_csr* A, const pf2_solver_options* opt, pf
         if (cudaFuncSetAttribute(pf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->part_smem) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_p, pf, kPartThreads, S->part_smem) != cudaSuccess)
             return fail(cuda_fail(cudaGetLastError(), "partitioned CG attributes", __FILE__, __LINE__));
-        if (occ_p < 1) S->part = false;  // the other kernels then
+        if (occ_p < 1) {  // the other kernels then
+            S->part = false;
+            S->part_why = "no block of the partitioned kernel fits on an SM";
+        }
     }
+    // PF2_CG_PART=2 (tests): require the partitioned kernel
+    if (const char* e = getenv("PF2_CG_PART"))
+        if (atoi(e) == 2 && !S->part) {
+            set_error("the partitioned CG kernel does not apply: %s", part_eligible(S) ? S->part_why :
+                      "solver kind, variant, precision or preconditioner");
+            return fail(PF2_BAD_INPUT);
+        }
     // the banded triangular solve keeps a range of the solution in shared memory
     S->smem = S->band_P ? sizeof(double) * (size_t)S->band_R : 0;
     void* fn = solve_kernel(*opt, S->csr);

@@ -40,12 +40,20 @@ def _system(nx, ny):
 
 
 @pytest.mark.parametrize("criterion", [g.CRITERION_ABS, g.CRITERION_REL])
-def test_static_pcg_matches_allocating_solver_twice(cuda, criterion):
+def test_static_pcg_matches_allocating_solver_twice(cuda, monkeypatch, criterion):
+    """The static entry point runs k_pcg, the allocating solver's kernel when the
+    partitioned kernel is off (PF2_CG_PART=0): the same bits; the partitioned kernel (the
+    allocating solver's default) sums its reductions in another order and agrees to the
+    solve's tolerance."""
     m, A, rp, col, val, rhs = _system(128, 32)
     b = torch.tensor(rhs, device="cuda")
+    x_part = torch.zeros_like(b)
+    part = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=criterion).solve(A, x_part, b)
+    monkeypatch.setenv("PF2_CG_PART", "0")
     x_ref = torch.zeros_like(b)
     ref = g.LinearSolver(A, "cg", "jacobi", tol=1e-8, maxit=5000, criterion=criterion).solve(A, x_ref, b)
-    assert ref.converged == 1
+    assert ref.converged == 1 and part.converged == 1 and abs(part.iterations - ref.iterations) <= 2
+    assert rel_err(x_part.cpu().numpy(), x_ref.cpu().numpy()) < 1e-6
     free = []
     xs = [torch.zeros_like(b) for _ in range(3)]  # torch's allocations come before the calls
     for x in xs:  # calls in a row reuse the same storage
