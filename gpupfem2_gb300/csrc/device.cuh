@@ -212,9 +212,8 @@ __device__ __forceinline__ void arrive_release_gpu(unsigned* p) {
 
 // Thread 0 arrives at barrier k (the counter read before arriving, c0, lies in
 // [k G, (k + 1) G)) and waits for the other blocks.  False on a timeout or an error.
-__device__ __forceinline__ bool arrive_and_wait(const GridBarrier& b, unsigned c0, unsigned nblocks) {
+__device__ __forceinline__ bool barrier_wait(const GridBarrier& b, unsigned c0, unsigned nblocks) {
     const unsigned target = (c0 / nblocks + 1) * nblocks;
-    arrive_release_gpu(b.count);
     const long long limit = b.max_polls > 0 ? b.max_polls : kBarrierPolls;
     long long polls = 0;
     unsigned c;
@@ -227,6 +226,11 @@ __device__ __forceinline__ bool arrive_and_wait(const GridBarrier& b, unsigned c
         if ((polls & 255) == 0 && *(volatile int*)b.err != 0) return false;
     }
     return *(volatile int*)b.err == 0;
+}
+
+__device__ __forceinline__ bool arrive_and_wait(const GridBarrier& b, unsigned c0, unsigned nblocks) {
+    arrive_release_gpu(b.count);
+    return barrier_wait(b, c0, nblocks);
 }
 
 // The counter is read before the block's __syncthreads, whose wait hides the load: the
@@ -321,12 +325,15 @@ struct NoPost {
 // which every thread reads after the call: an FP64 division or square root is tens of
 // FP64 instructions and would cost microseconds computed by every warp.  sh holds at least
 // 32 doubles.
-template <int BT, int NV, class Post = NoPost>
-__device__ __forceinline__ bool grid_reduce_tree(const GridBarrier& b, double (&v)[NV], double* sh, double* red,
-                                                 Post post = Post()) {
+// The first half of grid_reduce_tree: the block tree, the block sums stored and the
+// arrival.  Returns the barrier ticket (thread 0's counter read; meaningful in thread 0
+// only) for grid_reduce_tree_wait; work that needs no other block's contribution to this
+// reduction may run in between (the wait is split from the arrival so that it overlaps).
+template <int BT, int NV>
+__device__ __forceinline__ unsigned grid_reduce_tree_arrive(const GridBarrier& b, const double (&v)[NV], double* sh,
+                                                            double* red) {
     static_assert(NV >= 1 && NV <= 4, "grid_reduce_tree sums one to four values");
     static_assert(BT % 128 == 0 && BT <= 1024, "block size of the tree");
-    __shared__ int s_ok, s_par;
     const unsigned G = gridDim.x;
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     unsigned c0 = 0;
@@ -353,12 +360,25 @@ __device__ __forceinline__ bool grid_reduce_tree(const GridBarrier& b, double (&
     }
     __syncthreads();
     if (tid == 0) {
-        const unsigned kb = c0 / G;
-        double* part = b.part + (size_t)(kb & 1u) * 4 * G;
+        double* part = b.part + (size_t)((c0 / G) & 1u) * 4 * G;
 #pragma unroll
         for (int j = 0; j < NV; ++j) __stcg(&part[j * G + blockIdx.x], sh[j]);
-        s_ok = arrive_and_wait(b, c0, G) ? 1 : 0;
-        s_par = (int)(kb & 1u);
+        arrive_release_gpu(b.count);
+    }
+    return c0;
+}
+
+// The second half: thread 0 waits for the other blocks (bounded), warp j adds value j's
+// partials in block order, thread 0 runs post, and every thread gets the totals in v.
+template <int BT, int NV, class Post = NoPost>
+__device__ __forceinline__ bool grid_reduce_tree_wait(const GridBarrier& b, unsigned c0, double (&v)[NV], double* sh,
+                                                      Post post = Post()) {
+    __shared__ int s_ok, s_par;
+    const unsigned G = gridDim.x;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    if (tid == 0) {
+        s_ok = barrier_wait(b, c0, G) ? 1 : 0;
+        s_par = (int)((c0 / G) & 1u);
     }
     __syncthreads();
     if (w < NV) {
@@ -376,6 +396,13 @@ __device__ __forceinline__ bool grid_reduce_tree(const GridBarrier& b, double (&
 #pragma unroll
     for (int j = 0; j < NV; ++j) v[j] = sh[16 + j];
     return s_ok != 0;
+}
+
+template <int BT, int NV, class Post = NoPost>
+__device__ __forceinline__ bool grid_reduce_tree(const GridBarrier& b, double (&v)[NV], double* sh, double* red,
+                                                 Post post = Post()) {
+    const unsigned c0 = grid_reduce_tree_arrive<BT, NV>(b, v, sh, red);
+    return grid_reduce_tree_wait<BT, NV>(b, c0, v, sh, post);
 }
 
 }  // namespace pf2

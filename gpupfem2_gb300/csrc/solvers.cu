@@ -1172,7 +1172,7 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
         }))
         return;
     bnorm = sh[24];
-    double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+    double alpha = 1.0, omega = 1.0;
     double rho = red[0], rr = red[1], mm = red[2];
     int it = 0;
     bool conv = sh[25] != 0.0;
@@ -1240,7 +1240,6 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
                 o[1] = t[0] == 0.0 ? (t[1] / 1.0) * (1.0 / 1.0) : (t[0] / rho) * (alpha / omega);
             }))
             return;
-        rho_old = rho;
         rho = g3[0];
         rr = g3[1];
         mm = g3[2];
@@ -1258,12 +1257,10 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_bicgstab
                 a.q[i] = 0.0;
             }
             rho = rr;
-            rho_old = 1.0;
             alpha = 1.0;
             omega = 1.0;
         }
     }
-    (void)rho_old;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->iterations = it;
         a.out->converged = conv ? 1 : 0;
@@ -1469,7 +1466,10 @@ __global__ void __launch_bounds__(kSolverThreads, kSolverBlocksPerSm) k_pcg_pipe
 // and (kPartMetaSmem) the rows' entry ranges, diagonal positions and boundary flags.  x
 // stays in global memory: the smaller shared-memory carve-out leaves more of the SM's
 // 256 KB to the L1 that caches the matrix and factor streams (measured: IC(0) CG at
-// 499,288 rows 57.9 us per iteration with x in shared memory, 51.7 without).
+// 499,288 rows 57.9 us per iteration with x in shared memory, 51.7 without).  The groups
+// of a sweep follow one another behind a __syncthreads (measured against rows polling
+// their own part's results in shared memory, with no barrier between the groups: 47 against
+// 56 us per IC(0) iteration).
 template <class V>
 struct PartSm {
     V *r, *p, *q, *t, *z, *d;
@@ -1556,13 +1556,21 @@ __device__ __forceinline__ V part_dep(int j, int p0, int np, const V* sv, const 
 }
 
 // q = A p over the part's rows (each row's entries in order, as spmv_rows); other parts'
-// p from the global copy.  Returns the thread's p.q terms (in FP64).
+// p from the global copy.  Returns the thread's p.q terms (in FP64).  reset_z: the
+// boundary rows' backward results back to the pending marker.  This is the place for it:
+// the SpMV follows the grid barrier that ends an iteration, so every part has finished
+// the backward sweep that read them, and the next backward sweep (which may start before
+// other parts end their forward sweep: it overlaps the t.t reduction) follows the p.q
+// reduction's barrier.
 template <class V>
-__device__ __forceinline__ double part_spmv(const PartCg& C, const PartSm<V>& S, int p0, int np) {
+__device__ __forceinline__ double part_spmv(const PartCg& C, const PartSm<V>& S, int p0, int np,
+                                            bool reset_z = false) {
     const V* val = PartVecs<V>::val(C);
     const V* gp = PartVecs<V>::gp(C);
+    V* gz = PartVecs<V>::gz(C);
     double pq = 0.0;
     for (int l = threadIdx.x; l < np; l += kPartThreads) {
+        if (reset_z && S.bnd[l]) __stcg(&gz[p0 + l], Pending<V>::marker());
         const int s = S.rp[l], e = S.rp[l + 1];
         V acc = V(0);
         for (int k = s; k < e; ++k) {
@@ -1611,7 +1619,6 @@ template <bool IC, class V = double, bool MIXED = false, bool LOCAL = false>
 __device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np, bool first, V alpha, bool want_rr,
                             int* err, int* rec) {
     V* gt = PartVecs<V>::gt(C);
-    V* gz = PartVecs<V>::gz(C);
     const V* f = PartVecs<V>::f(C);
     double rr = 0.0, tt = 0.0;
     const int* qs = C.qs + blockIdx.x * C.ng;
@@ -1633,10 +1640,7 @@ __device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np,
             const V sum = sweep_sum<V, LOCAL>(C, S.rp[l], d, p0, np, S.t, gt, err, rec, p0 + l);
             const V v = IC ? (ra - sum) * __ldg(&f[d]) : ra - sum;
             S.t[l] = v;
-            if (!LOCAL && S.bnd[l]) {
-                __stcg(&gt[p0 + l], v);
-                __stcg(&gz[p0 + l], Pending<V>::marker());
-            }
+            if (!LOCAL && S.bnd[l]) __stcg(&gt[p0 + l], v);
             tt += (double)v * (double)v;
             // x += alpha p last: its global load is off the sweep's dependency chain
             if (!first) {
@@ -1651,8 +1655,10 @@ __device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np,
 }
 
 // Backward sweep over the part's groups in reverse (csr_bwd): z = U^{-1} t; PMODE 0: no
-// direction, 1: p = z (the first), 2: p = z + beta p (IC's three-step iteration).
-// Returns the r.z terms (PMODE != 2), in FP64.  LOCAL: partition-local factors.
+// direction, 1: p = z (the first), 2: p = z + beta p (IC's three-step iteration), 3: z
+// alone (IC's iteration with the sweep overlapping the t.t reduction; the caller updates p
+// and resets the boundary rows' t afterwards).  Returns the r.z terms (PMODE 0 and 1), in
+// FP64.  LOCAL: partition-local factors.
 template <int PMODE, class V = double, bool LOCAL = false>
 __device__ double part_bwd(const PartCg& C, const PartSm<V>& S, int p0, int np, V beta, int* err, int* rec) {
     V* gp = PartVecs<V>::gp(C);
@@ -1677,18 +1683,37 @@ __device__ double part_bwd(const PartCg& C, const PartSm<V>& S, int p0, int np, 
             V pn = V(0);
             if (PMODE == 1) pn = v;
             if (PMODE == 2) pn = fma_rn(beta, S.p[l], v);
-            if (PMODE) S.p[l] = pn;
+            if (PMODE == 1 || PMODE == 2) S.p[l] = pn;
             if (S.bnd[l]) {
                 if (!LOCAL) {
                     __stcg(&gz[p0 + l], v);
-                    __stcg(&gt[p0 + l], Pending<V>::marker());
+                    if (PMODE != 3) __stcg(&gt[p0 + l], Pending<V>::marker());
                 }
-                if (PMODE) __stcg(&gp[p0 + l], pn);
+                if (PMODE == 1 || PMODE == 2) __stcg(&gp[p0 + l], pn);
             }
-            if (PMODE != 2) rz += (double)S.r[l] * (double)v;
+            if (PMODE <= 1) rz += (double)S.r[l] * (double)v;
         }
     }
     return rz;
+}
+
+// IC's direction update after a backward sweep that overlapped the t.t reduction (PMODE
+// 3): p = z + beta p (part_bwd's PUPD arithmetic) over the part's rows, boundary rows also
+// to the global copy, and the boundary rows' forward results back to the marker (every
+// part has passed its forward sweep: the reduction's barrier is behind).
+template <class V>
+__device__ __forceinline__ void part_p_after_bwd(const PartCg& C, const PartSm<V>& S, int p0, int np, V beta,
+                                                 bool reset_t) {
+    V* gp = PartVecs<V>::gp(C);
+    V* gt = PartVecs<V>::gt(C);
+    for (int l = threadIdx.x; l < np; l += kPartThreads) {
+        const V pn = fma_rn(beta, S.p[l], S.z[l]);
+        S.p[l] = pn;
+        if (S.bnd[l]) {
+            __stcg(&gp[p0 + l], pn);
+            if (reset_t) __stcg(&gt[p0 + l], Pending<V>::marker());
+        }
+    }
 }
 
 // p = z + beta p over the part's rows (p_update), boundary rows also to the global copy.
@@ -1782,7 +1807,7 @@ __device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
     bool conv = sh[25] != 0.0;
     while (!conv && it < a.maxit) {
         ++it;
-        double pq[1] = { part_spmv(C, S, p0, np) };
+        double pq[1] = { part_spmv(C, S, p0, np, MODE != 0) };
         if (!part_reduce<1>(a.bar, pq, sh, S.red, [&](const double* tot, double* out) { out[0] = gamma / tot[0]; }))
             return;
         const double alpha = sh[24];
@@ -1799,9 +1824,40 @@ __device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
                 if (rel) g2[1] += ri * ri;
             }
         } else if (MODE == 1) {
+            // z = L^{-T} t does not depend on beta: the backward sweep runs between this
+            // block's arrival at the t.t (and r.r) reduction and the wait for the others,
+            // and the direction update p = z + beta p follows the wait
             const double2 f = part_fwd<true>(C, S, p0, np, false, alpha, rel, err, rec);
-            g2[0] = f.y;
-            g2[1] = f.x;
+            bool done = false, ok;
+            double beta = 0.0;
+            if (rel) {
+                double g[2] = { f.y, f.x };
+                const unsigned tk = grid_reduce_tree_arrive<kPartThreads, 2>(a.bar, g, sh, S.red);
+                part_bwd<3>(C, S, p0, np, 0.0, err, rec);
+                ok = grid_reduce_tree_wait<kPartThreads, 2>(a.bar, tk, g, sh, [&](const double* tot, double* out) {
+                    out[0] = sqrt(tot[1]) <= a.tol * bnorm;
+                    out[1] = tot[0] / gamma;
+                });
+                g2[0] = g[0];
+                rr = g[1];
+            } else {
+                double g[1] = { f.y };
+                const unsigned tk = grid_reduce_tree_arrive<kPartThreads, 1>(a.bar, g, sh, S.red);
+                part_bwd<3>(C, S, p0, np, 0.0, err, rec);
+                ok = grid_reduce_tree_wait<kPartThreads, 1>(a.bar, tk, g, sh, [&](const double* tot, double* out) {
+                    out[0] = tot[0] < a.tol * a.tol;
+                    out[1] = tot[0] / gamma;
+                });
+                g2[0] = g[0];
+            }
+            if (!ok) return;
+            done = sh[24] != 0.0;
+            beta = sh[25];
+            if (done) { gamma = g2[0]; conv = true; break; }
+            gamma = g2[0];
+            part_p_after_bwd(C, S, p0, np, beta, true);
+            if (!grid_sync(a.bar, gridDim.x)) return;
+            continue;
         } else {
             g2[1] = part_fwd<false>(C, S, p0, np, false, alpha, rel, err, rec).x;
             if (!grid_sync(a.bar, gridDim.x)) return;
@@ -1828,10 +1884,7 @@ __device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
         if (sh[24] != 0.0) { gamma = gnew; conv = true; break; }
         const double beta = sh[25];
         gamma = gnew;
-        if (MODE == 1)
-            part_bwd<2>(C, S, p0, np, beta, err, rec);
-        else
-            part_p_update(C, S, p0, np, beta);
+        part_p_update(C, S, p0, np, beta);
         if (!grid_sync(a.bar, gridDim.x)) return;
     }
     if (!rel && it > 0) {
@@ -1902,7 +1955,7 @@ __device__ void pcg_part_mixed(const KArgs& a, double* sh, unsigned char* smem) 
         if (!part_reduce<1>(a.bar, g, sh, S.red)) return;
         double gamma = g[0];
         while (it < a.maxit) {
-            double pq[1] = { part_spmv(C, S, p0, np) };
+            double pq[1] = { part_spmv(C, S, p0, np, !LOCAL) };
             ++it;
             if (!part_reduce<1>(a.bar, pq, sh, S.red, [&](const double* tot, double* out) {
                     out[0] = (double)(float)(gamma / tot[0]);
@@ -1910,22 +1963,27 @@ __device__ void pcg_part_mixed(const KArgs& a, double* sh, unsigned char* smem) 
                 return;
             const float alpha = (float)sh[24];
             double g2[2];  // r.z (IC: t.t), r.r
+            // refinement test and beta (thread 0; see part_reduce)
+            auto post = [&](const double* tot, double* out) {
+                const double rit = sqrt(tot[1]);
+                out[0] = rit <= a.inner_eta * rlast || rit <= target;
+                out[1] = (double)(float)(tot[0] / gamma);
+            };
             if (IC) {
+                // the backward sweep (z alone) overlaps the reduction, as in pcg_part
                 const double2 f = part_fwd<true, float, true, LOCAL>(C, S, p0, np, false, alpha, true, err, rec);
                 g2[0] = f.y;
                 g2[1] = f.x;
+                const unsigned tk = grid_reduce_tree_arrive<kPartThreads, 2>(a.bar, g2, sh, S.red);
+                part_bwd<3, float, LOCAL>(C, S, p0, np, 0.0f, err, rec);
+                if (!grid_reduce_tree_wait<kPartThreads, 2>(a.bar, tk, g2, sh, post)) return;
             } else {
                 g2[1] = part_fwd<false, float, true, LOCAL>(C, S, p0, np, false, alpha, true, err, rec).x;
                 if (!LOCAL && !grid_sync(a.bar, gridDim.x)) return;
                 g2[0] = part_bwd<0, float, LOCAL>(C, S, p0, np, 0.0f, err, rec);
+                if (!part_reduce<2>(a.bar, g2, sh, S.red, post)) return;
             }
-            // refinement test and beta (thread 0; see part_reduce)
-            if (!part_reduce<2>(a.bar, g2, sh, S.red, [&](const double* tot, double* out) {
-                    const double rit = sqrt(tot[1]);
-                    out[0] = rit <= a.inner_eta * rlast || rit <= target;
-                    out[1] = (double)(float)(tot[0] / gamma);
-                }))
-                return;
+            bool refined = false;
             double gnew = g2[0];
             float beta = (float)sh[25];
             if (sh[24] != 0.0) {
@@ -1937,6 +1995,10 @@ __device__ void pcg_part_mixed(const KArgs& a, double* sh, unsigned char* smem) 
                     if (!LOCAL && S.bnd[l]) __stcg(&C.gt32[p0 + l], Pending<float>::marker());
                 }
                 if (!grid_sync(a.bar, gridDim.x)) return;
+                // (after the barrier: every part has ended the backward sweep that read them)
+                if (!LOCAL)
+                    for (int l = tid; l < np; l += kPartThreads)
+                        if (S.bnd[l]) __stcg(&C.gz32[p0 + l], Pending<float>::marker());
                 double rr[1] = { 0.0 };
                 residual(rr[0], nullptr);
                 if (!part_reduce<1>(a.bar, rr, sh, S.red, [&](const double* tot, double* out) {
@@ -1962,10 +2024,13 @@ __device__ void pcg_part_mixed(const KArgs& a, double* sh, unsigned char* smem) 
                     return;
                 gnew = g3[0];
                 beta = (float)sh[24];
+                refined = true;
             }
             gamma = gnew;
-            if (IC)
+            if (IC && refined)  // the overlapped sweep used the old t
                 part_bwd<2, float, LOCAL>(C, S, p0, np, beta, err, rec);
+            else if (IC)
+                part_p_after_bwd(C, S, p0, np, beta, !LOCAL);
             else
                 part_p_update(C, S, p0, np, beta);
             if (!grid_sync(a.bar, gridDim.x)) return;
