@@ -1596,26 +1596,27 @@ __device__ __forceinline__ void sweep_prefetch(const PartCg& C, int k0, int k1, 
     prefetch_l1(&f[d]);
 }
 
-// sum_k f_k v[col_k] over the dependency entries [k0, k1), in entry order; LOCAL (the
+// s - sum_k f_k v[col_k] over the dependency entries [k0, k1), in entry order, as a chain
+// of fused multiply-adds from s (one FP64 instruction a row fewer than forming the sum and
+// subtracting it; a sweep's rows are FP64-issue-bound on GB300); LOCAL (the
 // partition-local factors, zero outside the part): the part's own entries only.
 template <class V, bool LOCAL = false>
-__device__ __forceinline__ V sweep_sum(const PartCg& C, int k0, int k1, int p0, int np, const V* sv, const V* gv,
-                                       int* err, int* rec, int row) {
+__device__ __forceinline__ V sweep_rest(const PartCg& C, int k0, int k1, int p0, int np, const V* sv, const V* gv,
+                                        V s, int* err, int* rec, int row) {
     const V* f = PartVecs<V>::f(C);
-    V sum = V(0);
     for (int k = k0; k < k1; ++k) {
         const int j = __ldg(&C.col[k]);
         if (LOCAL && (unsigned)(j - p0) >= (unsigned)np) continue;
-        sum += __ldg(&f[k]) * part_dep(j, p0, np, sv, gv, err, rec, row);
+        s = fma_rn(-__ldg(&f[k]), part_dep(j, p0, np, sv, gv, err, rec, row), s);
     }
-    return sum;
+    return s;
 }
 
 // Forward sweep over the part's groups (csr_fwd): first: t = L^{-1} r; else the updates
-// r -= alpha q and x += alpha p (MIXED: the inner update d += alpha p) with it.  Returns
-// the r.r terms (want_rr) and the t.t terms, in FP64.  LOCAL: partition-local factors, no
-// boundary copies.
-template <bool IC, class V = double, bool MIXED = false, bool LOCAL = false>
+// r -= alpha q and (XUPD) x += alpha p (MIXED: the inner update d += alpha p) with it.
+// Returns the r.r terms (want_rr) and the t.t terms, in FP64.  LOCAL: partition-local
+// factors, no boundary copies.
+template <bool IC, class V = double, bool MIXED = false, bool LOCAL = false, bool XUPD = true>
 __device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np, bool first, V alpha, bool want_rr,
                             int* err, int* rec) {
     V* gt = PartVecs<V>::gt(C);
@@ -1637,13 +1638,13 @@ __device__ double2 part_fwd(const PartCg& C, const PartSm<V>& S, int p0, int np,
                 S.r[l] = ra;
             }
             if (want_rr) rr += (double)ra * (double)ra;
-            const V sum = sweep_sum<V, LOCAL>(C, S.rp[l], d, p0, np, S.t, gt, err, rec, p0 + l);
-            const V v = IC ? (ra - sum) * __ldg(&f[d]) : ra - sum;
+            const V rest = sweep_rest<V, LOCAL>(C, S.rp[l], d, p0, np, S.t, gt, ra, err, rec, p0 + l);
+            const V v = IC ? rest * __ldg(&f[d]) : rest;
             S.t[l] = v;
             if (!LOCAL && S.bnd[l]) __stcg(&gt[p0 + l], v);
             tt += (double)v * (double)v;
             // x += alpha p last: its global load is off the sweep's dependency chain
-            if (!first) {
+            if (XUPD && !first) {
                 if (MIXED)
                     S.d[l] = S.d[l] + alpha * S.p[l];
                 else
@@ -1677,8 +1678,8 @@ __device__ double part_bwd(const PartCg& C, const PartSm<V>& S, int p0, int np, 
         for (int l = g0 + threadIdx.x; l < g1; l += kPartThreads) {
             const int d = S.dg[l];
             const V in = S.t[l];
-            const V sum = sweep_sum<V, LOCAL>(C, d + 1, S.rp[l + 1], p0, np, S.z, gz, err, rec, p0 + l);
-            const V v = (in - sum) * __ldg(&f[d]);
+            const V v = sweep_rest<V, LOCAL>(C, d + 1, S.rp[l + 1], p0, np, S.z, gz, in, err, rec, p0 + l) *
+                        __ldg(&f[d]);
             S.z[l] = v;
             V pn = V(0);
             if (PMODE == 1) pn = v;
@@ -1827,13 +1828,19 @@ __device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
             // z = L^{-T} t does not depend on beta: the backward sweep runs between this
             // block's arrival at the t.t (and r.r) reduction and the wait for the others,
             // and the direction update p = z + beta p follows the wait
-            const double2 f = part_fwd<true>(C, S, p0, np, false, alpha, rel, err, rec);
+            // x += alpha p also waits for the arrival: the FP64 pipe is otherwise idle there
+            const double2 f = part_fwd<true, double, false, false, false>(C, S, p0, np, false, alpha, rel, err, rec);
             bool done = false, ok;
             double beta = 0.0;
+            auto x_update = [&]() {
+                for (int l = tid; l < np; l += kPartThreads)
+                    __stcg(&C.x[p0 + l], __ldcg(&C.x[p0 + l]) + alpha * S.p[l]);
+            };
             if (rel) {
                 double g[2] = { f.y, f.x };
                 const unsigned tk = grid_reduce_tree_arrive<kPartThreads, 2>(a.bar, g, sh, S.red);
                 part_bwd<3>(C, S, p0, np, 0.0, err, rec);
+                x_update();
                 ok = grid_reduce_tree_wait<kPartThreads, 2>(a.bar, tk, g, sh, [&](const double* tot, double* out) {
                     out[0] = sqrt(tot[1]) <= a.tol * bnorm;
                     out[1] = tot[0] / gamma;
@@ -1844,6 +1851,7 @@ __device__ void pcg_part(const KArgs& a, double* sh, unsigned char* smem) {
                 double g[1] = { f.y };
                 const unsigned tk = grid_reduce_tree_arrive<kPartThreads, 1>(a.bar, g, sh, S.red);
                 part_bwd<3>(C, S, p0, np, 0.0, err, rec);
+                x_update();
                 ok = grid_reduce_tree_wait<kPartThreads, 1>(a.bar, tk, g, sh, [&](const double* tot, double* out) {
                     out[0] = tot[0] < a.tol * a.tol;
                     out[1] = tot[0] / gamma;
