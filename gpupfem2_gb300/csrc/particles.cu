@@ -14,6 +14,7 @@
 // projectVelocityOntoGrid then only gathers the partial sums of the cells around each
 // node (k_project_nodes): no atomics, and the result does not depend on timing.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -69,15 +70,40 @@ struct MeshRefs {
     int nc;
 };
 
+// Per-warp scratch of the warp-cooperative cell location in k_advect.
+constexpr int kSearchCap = 64;  // candidate cells a warp tests together per substep
+struct SearchBuf {
+    double x[32], y[32];          // the searching lanes' positions
+    double l[kSearchCap][3];      // a candidate's barycentric coordinates, when it holds the point
+    int nb[kSearchCap];           // candidate cell
+    int k[kSearchCap];            // its position in its lane's neighbour list
+    int owner[kSearchCap];        // the lane searching it
+    int best[32];                 // per lane: the lowest position that holds the point
+    int win[32];                  // per lane: the candidate at that position
+    int count;
+};
+
 // kAdvectParticles (:54-70) for every substep, the location of sortParticlesInCells
 // (:363-395, kernels :117-162) after each, and kCountParticlesInSubcells (:173-181).
 // Warps stride over the particles together so that the ranks of particles that land in
 // the same cell come from one atomic per cell and warp (the order of ranks is free: the
-// gather restores the old order).
+// gather restores the old order).  The lanes of a warp take the substeps together: after
+// each, the particles that left their cell are located by the whole warp.  Each such lane
+// walks its cell's neighbours in order through the FP32 pre-filter (FP32 pipe) and
+// appends the survivors to the warp's list; then every lane tests one candidate with the
+// FP64 transform, so one pass of FP64 instructions serves up to 32 candidates of any
+// lanes (a lane searching alone through its neighbours would issue the FP64 transform for
+// each of its candidates with the other 31 lanes idle: GB300 issues an FP64 warp
+// instruction at the same cost whatever its active lanes).  A lane's cell is its
+// lowest-positioned candidate that holds the point: the first one the reference's
+// sequential search finds, with the same FP64 arithmetic, so the result is bit-identical.
+// A lane whose candidates do not fit the list searches sequentially.
 __global__ void __launch_bounds__(256) k_advect(const int* __restrict__ np_ptr, int substeps, double dts, Centers C,
                                                 MeshRefs M, const double* __restrict__ ux,
                                                 const double* __restrict__ uy, PState P, int* count, int* mask,
                                                 int* rank, int level, double step) {
+    __shared__ SearchBuf sbuf[8];
+    SearchBuf& B = sbuf[threadIdx.x >> 5];
     const int np = *np_ptr;
     const int ppc = level * level;
     const int lane = threadIdx.x & 31;
@@ -86,24 +112,81 @@ __global__ void __launch_bounds__(256) k_advect(const int* __restrict__ np_ptr, 
         const int p = (int)(wb + lane);
         int key = -1;  // cell the particle ends in, -1 if none
         int sub = 0;
-        if (p < np) {
-            const int cw = P.cw[p];
-            if (cw >= 0) {
-                int c = cw & kCellMask;
-                double l0 = P.l0[p], l1 = P.l1[p];
-                double l2 = third_coord(cw, l0, l1, C);
-                double x = P.x[p], y = P.y[p];
-                bool lost = false;
-                for (int s = 0; s < substeps; ++s) {
-                    const int4 t = M.tri[c];
-                    const double vx = interp3(l0, l1, l2, __ldg(&ux[t.x]), __ldg(&ux[t.y]), __ldg(&ux[t.z]));
-                    const double vy = interp3(l0, l1, l2, __ldg(&uy[t.x]), __ldg(&uy[t.y]), __ldg(&uy[t.z]));
-                    x = __fma_rn(vx, dts, x);
-                    y = __fma_rn(vy, dts, y);
-                    double n0, n1, n2;
-                    global_to_local(x, y, M.invJ[c], M.v3[c], n0, n1, n2);
-                    if (!inside_unit(n0, n1, n2)) {
-                        const int o = M.nb_off[c], e = M.nb_off[c + 1];
+        const int cw = p < np ? P.cw[p] : -1;
+        const bool valid = cw >= 0;
+        int c = cw & kCellMask;
+        double l0 = 0.0, l1 = 0.0, l2 = 0.0, x = 0.0, y = 0.0;
+        if (valid) {
+            l0 = P.l0[p];
+            l1 = P.l1[p];
+            l2 = third_coord(cw, l0, l1, C);
+            x = P.x[p];
+            y = P.y[p];
+        }
+        bool lost = false;
+        for (int s = 0; s < substeps; ++s) {
+            const bool act = valid && !lost;
+            double n0 = 0.0, n1 = 0.0, n2 = 0.0;
+            bool need = false;
+            if (act) {
+                const int4 t = M.tri[c];
+                const double vx = interp3(l0, l1, l2, __ldg(&ux[t.x]), __ldg(&ux[t.y]), __ldg(&ux[t.z]));
+                const double vy = interp3(l0, l1, l2, __ldg(&uy[t.x]), __ldg(&uy[t.y]), __ldg(&uy[t.z]));
+                x = __fma_rn(vx, dts, x);
+                y = __fma_rn(vy, dts, y);
+                global_to_local(x, y, M.invJ[c], M.v3[c], n0, n1, n2);
+                need = !inside_unit(n0, n1, n2);
+            }
+            if (__ballot_sync(0xffffffffu, need)) {
+                if (lane == 0) B.count = 0;
+                B.best[lane] = INT_MAX;
+                __syncwarp();
+                bool overflow = false;
+                int o = 0, e = 0;
+                if (need) {
+                    B.x[lane] = x;
+                    B.y[lane] = y;
+                    o = M.nb_off[c];
+                    e = M.nb_off[c + 1];
+                    const float xf = (float)x, yf = (float)y;
+                    for (int k = o; k < e; ++k) {
+                        const int nb = M.nb_idx[k];
+                        if (!maybe_inside_f32(xf, yf, M.invJf[nb], M.v3f[nb])) continue;
+                        const int slot = atomicAdd(&B.count, 1);
+                        if (slot < kSearchCap) {
+                            B.nb[slot] = nb;
+                            B.k[slot] = k;
+                            B.owner[slot] = lane;
+                        } else {
+                            overflow = true;
+                        }
+                    }
+                }
+                __syncwarp();
+                const int total = min(B.count, kSearchCap);
+                for (int base = 0; base < total; base += 32) {
+                    const int i = base + lane;
+                    if (i < total) {
+                        const int ow = B.owner[i], nb = B.nb[i];
+                        double m0, m1, m2;
+                        global_to_local(B.x[ow], B.y[ow], M.invJ[nb], M.v3[nb], m0, m1, m2);
+                        if (inside_unit(m0, m1, m2)) {
+                            B.l[i][0] = m0;
+                            B.l[i][1] = m1;
+                            B.l[i][2] = m2;
+                            atomicMin(&B.best[ow], B.k[i]);
+                        }
+                    }
+                }
+                __syncwarp();
+                for (int base = 0; base < total; base += 32) {
+                    const int i = base + lane;
+                    if (i < total && B.k[i] == B.best[B.owner[i]]) B.win[B.owner[i]] = i;
+                }
+                __syncwarp();
+                if (need) {
+                    if (overflow) {
+                        // more candidates than the list holds: this lane's own search, in order
                         const float xf = (float)x, yf = (float)y;
                         int found = -1;
                         for (int k = o; k < e; ++k) {
@@ -112,25 +195,38 @@ __global__ void __launch_bounds__(256) k_advect(const int* __restrict__ np_ptr, 
                             global_to_local(x, y, M.invJ[nb], M.v3[nb], n0, n1, n2);
                             if (inside_unit(n0, n1, n2)) { found = nb; break; }
                         }
-                        if (found < 0) { lost = true; break; }
-                        c = found;
+                        if (found < 0) lost = true;
+                        else c = found;
+                    } else if (B.best[lane] == INT_MAX) {
+                        lost = true;
+                    } else {
+                        const int i = B.win[lane];
+                        c = B.nb[i];
+                        n0 = B.l[i][0];
+                        n1 = B.l[i][1];
+                        n2 = B.l[i][2];
                     }
-                    l0 = n0;
-                    l1 = n1;
-                    l2 = n2;
                 }
-                P.x[p] = x;
-                P.y[p] = y;
-                P.l0[p] = l0;
-                P.l1[p] = l1;
-                if (lost) {
-                    P.cw[p] = -1;
-                } else {
-                    // a located particle loses its centroid flag; with no substeps it keeps it
-                    P.cw[p] = substeps > 0 ? c : cw;
-                    key = c;
-                    sub = determine_subcell(level, step, l0, l1, l2);
-                }
+                __syncwarp();  // the list is rebuilt at the next substep
+            }
+            if (act && !lost) {
+                l0 = n0;
+                l1 = n1;
+                l2 = n2;
+            }
+        }
+        if (valid) {
+            P.x[p] = x;
+            P.y[p] = y;
+            P.l0[p] = l0;
+            P.l1[p] = l1;
+            if (lost) {
+                P.cw[p] = -1;
+            } else {
+                // a located particle loses its centroid flag; with no substeps it keeps it
+                P.cw[p] = substeps > 0 ? c : cw;
+                key = c;
+                sub = determine_subcell(level, step, l0, l1, l2);
             }
         }
         // one atomic per (warp, cell); each lane's rank = group base + lanes below it
