@@ -286,138 +286,185 @@ struct Partials {
     int nc;
 };
 
-__device__ __forceinline__ void add_partials(double acc[9], double l0, double l1, double l2, double u, double v) {
-    acc[0] = __dadd_rn(acc[0], __dmul_rn(l0, u));
-    acc[1] = __dadd_rn(acc[1], __dmul_rn(l0, v));
-    acc[2] = __dadd_rn(acc[2], l0);
-    acc[3] = __dadd_rn(acc[3], __dmul_rn(l1, u));
-    acc[4] = __dadd_rn(acc[4], __dmul_rn(l1, v));
-    acc[5] = __dadd_rn(acc[5], l1);
-    acc[6] = __dadd_rn(acc[6], __dmul_rn(l2, u));
-    acc[7] = __dadd_rn(acc[7], __dmul_rn(l2, v));
-    acc[8] = __dadd_rn(acc[8], l2);
-}
+// The nine projection partial sums of a block's eight cells c0 .. c0 + 7, cell i holding
+// slots [bs[i], bs[i] + bn[i]) of S (bn[i] < 0: the cell is skipped, no sums written):
+// for each cell (sum L0 u, sum L0 v, sum L0, the same for L1 and L2), the sums of
+// kProjectParticleVelocityOntoGrid (particle_handler_2d.cu:90-107) gathered per cell.  Thread
+// t < 216 forms one value over one third of one cell's slots, in slot order, one fused
+// multiply-add per slot (by 1.0 for the coordinate alone), and the three thirds are
+// added in order: all lanes of seven warps stay busy however many particles a cell has
+// (a warp per cell with lane j taking slots j, j + 32, ... idles most lanes of its
+// second pass at ~36 particles per cell, and every FP64 instruction costs the same
+// issue slot whatever its active lanes).  The cells' slots are contiguous; when they
+// fit kStageSlots they are first staged in shared memory by coalesced loads, L2 formed
+// once per slot, else the threads read them from S (same arithmetic, same bits).  Every
+// thread of the block calls it; S must be written before the call by this block or an
+// earlier kernel.  k_gather and k_partials both go through here, so a projection gives
+// the same bits whichever formed its sums.
+constexpr int kStageSlots = 512;
+struct PartialStage {
+    double l[3][kStageSlots];
+    double u[kStageSlots], v[kStageSlots];
+    double third[216];
+    int bs[8], bn[8];
+};
 
-// The nine partial sums of one cell from its warp's per-lane sums (lane j holding the
-// cell's slots j, j + 32, ...), through shared memory R[9][33] of the warp: lane 3v + q
-// adds value v of lanes 11q .. 11q + 10, then the three parts are combined.  Fixed order
-// (about a quarter of the FP64 additions of nine butterfly reductions); every kernel
-// that forms partial sums goes through here, so they agree bit for bit.
-__device__ __forceinline__ void warp_partials_store(const double acc[9], int lane, double (*R)[33], Partials part,
-                                                    int c) {
+__device__ __forceinline__ void block_partials(PartialStage& G, int c0, int nc, PState S, const Centers& C,
+                                               Partials part) {
+    const int t = threadIdx.x;
+    __syncthreads();  // bs, bn and the block's slots are in place
+    const int S0 = G.bs[0];
+    int total = 0;
+    bool contiguous = true;
 #pragma unroll
-    for (int k = 0; k < 9; ++k) R[k][lane] = acc[k];
-    __syncwarp();
-    double sum = 0.0;
-    if (lane < 27) {
-        const int v = lane / 3, q0 = 11 * (lane % 3), q1 = min(32, q0 + 11);
-        for (int j = q0; j < q1; ++j) sum += R[v][j];
+    for (int i = 0; i < 8; ++i) {
+        if (c0 + i >= nc) break;
+        if (G.bn[i] < 0 || G.bs[i] != S0 + total) contiguous = false;
+        total += max(G.bn[i], 0);
     }
-    const double s1 = __shfl_down_sync(0xffffffffu, sum, 1);
-    const double s2 = __shfl_down_sync(0xffffffffu, sum, 2);
-    if (lane < 27 && lane % 3 == 0) part.s[(size_t)(lane / 3) * part.nc + c] = (sum + s1) + s2;
+    const bool staged = contiguous && total <= kStageSlots;  // uniform over the block
+    if (staged) {
+        for (int k = t; k < total; k += blockDim.x) {
+            const int o = S0 + k;
+            const int w = S.cw[o];
+            const double l0 = S.l0[o], l1 = S.l1[o];
+            G.l[0][k] = l0;
+            G.l[1][k] = l1;
+            G.l[2][k] = third_coord(w, l0, l1, C);
+            G.u[k] = S.u[o];
+            G.v[k] = S.v[o];
+        }
+    }
+    __syncthreads();
+    // thread t: coordinate a (grouped so that the L2 threads of the unstaged path share
+    // warps), cell i, factor j (u, v, 1), third q
+    const int a = t / 72, rem = t % 72, i = rem / 9, j = (rem % 9) / 3, q = rem % 3;
+    double acc = 0.0;
+    if (t < 216) {
+        const int n = G.bn[i];
+        if (c0 + i < nc && n > 0) {
+            const int lo = q * n / 3, hi = (q + 1) * n / 3;
+            if (staged) {
+                const int base = G.bs[i] - S0;
+                const double* L = G.l[a] + base;
+                const double* W = (j == 0 ? G.u : G.v) + base;
+                for (int k = lo; k < hi; ++k) acc = __fma_rn(L[k], j < 2 ? W[k] : 1.0, acc);
+            } else {
+                const int base = G.bs[i];
+                const double* W = j == 0 ? S.u : S.v;
+                for (int k = lo; k < hi; ++k) {
+                    const int o = base + k;
+                    const double l0 = S.l0[o], l1 = S.l1[o];
+                    const double lv = a == 0 ? l0 : (a == 1 ? l1 : third_coord(S.cw[o], l0, l1, C));
+                    acc = __fma_rn(lv, j < 2 ? W[o] : 1.0, acc);
+                }
+            }
+        }
+        G.third[t] = acc;
+    }
+    __syncthreads();
+    if (t < 216 && q == 0 && c0 + i < nc && G.bn[i] >= 0)
+        part.s[(size_t)(3 * a + j) * part.nc + c0 + i] = __dadd_rn(__dadd_rn(G.third[t], G.third[t + 1]), G.third[t + 2]);
 }
 
-// Per cell, one warp: stable order, move, reseed (kAddParticlesToCell :197-236), partial
-// sums.  The cell's particles arrive in perm[s, s + n) in the order the atomics handed
-// out ranks; each lane ranks its particle by old index against all n (the old order is
-// the order the cell keeps), moves it to slot s + rank, then lanes fill the missing
-// sub-cells after them.  The nine partial sums are formed over the slots in a fixed
-// lane order after the moves, so they do not depend on the atomics' order.
+// Per cell, one warp: stable order, move, reseed (kAddParticlesToCell :197-236); then the
+// block's partial sums.  The cell's particles arrive in perm[s, s + n) in the order the
+// atomics handed out ranks; each lane ranks its particle by old index against all n (the
+// old order is the order the cell keeps), moves it to slot s + rank, then lanes fill the
+// missing sub-cells after them.  The partial sums are formed over the slots after the
+// moves, so they do not depend on the atomics' order.
 __global__ void __launch_bounds__(256) k_gather(int nc, const int* __restrict__ seg, int* count, int* mask,
                                                 const int* __restrict__ perm, PState S, PState D, Centers C,
                                                 int level, int reseed, const double2* __restrict__ xy,
                                                 const int4* __restrict__ tri, const double* __restrict__ ux,
                                                 const double* __restrict__ uy, Partials part, long long cap,
                                                 int* cnt) {
-    const int lane = threadIdx.x & 31;
-    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    __shared__ PartialStage G;
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const int c0 = blockIdx.x * 8;
+    const int c = c0 + wi;
     if (blockIdx.x == 0 && threadIdx.x == 0) cnt[0] = cnt[1];
-    if (c >= nc) return;  // uniform over the warp
     const int ppc = level * level;
-    const int s = seg[c], n = count[c];
-    const unsigned m = (unsigned)mask[c];
-    __syncwarp();
+    int s = 0, n = 0, nadd = 0;
+    unsigned m = 0;
+    bool fits = false;
+    if (c < nc) {  // uniform over the warp
+        s = seg[c];
+        n = count[c];
+        m = (unsigned)mask[c];
+        __syncwarp();
+        if (lane == 0) {
+            count[c] = 0;
+            mask[c] = 0;
+        }
+        const unsigned full = (1u << ppc) - 1u;
+        nadd = reseed ? ppc - __popc(m & full) : 0;
+        fits = (long long)s + n + nadd <= cap;
+    }
     if (lane == 0) {
-        count[c] = 0;
-        mask[c] = 0;
+        G.bs[wi] = s;
+        G.bn[wi] = fits ? n + nadd : -1;
     }
-    const unsigned full = (1u << ppc) - 1u;
-    const int nadd = reseed ? ppc - __popc(m & full) : 0;
-    if ((long long)s + n + nadd > cap) return;
-    // existing particles: lane handles entries base + lane of perm[s, s + n)
-    for (int base = 0; base < n; base += 32) {
-        const int i = base + lane;
-        const int v = i < n ? perm[s + i] : 0x7fffffff;
-        int r = 0;
-        for (int cb = 0; cb < n; cb += 32) {
-            const int w = cb + lane < n ? perm[s + cb + lane] : 0x7fffffff;
-            const int lim = min(32, n - cb);
-            for (int j = 0; j < lim; ++j) r += (__shfl_sync(0xffffffffu, w, j) < v) ? 1 : 0;
+    if (fits) {
+        // existing particles: lane handles entries base + lane of perm[s, s + n)
+        for (int base = 0; base < n; base += 32) {
+            const int i = base + lane;
+            const int v = i < n ? perm[s + i] : 0x7fffffff;
+            int r = 0;
+            for (int cb = 0; cb < n; cb += 32) {
+                const int w = cb + lane < n ? perm[s + cb + lane] : 0x7fffffff;
+                const int lim = min(32, n - cb);
+                for (int j = 0; j < lim; ++j) r += (__shfl_sync(0xffffffffu, w, j) < v) ? 1 : 0;
+            }
+            if (i < n) {
+                const int o = s + r;
+                D.x[o] = S.x[v];
+                D.y[o] = S.y[v];
+                D.l0[o] = S.l0[v];
+                D.l1[o] = S.l1[v];
+                D.u[o] = S.u[v];
+                D.v[o] = S.v[v];
+                D.cw[o] = S.cw[v];
+            }
         }
-        if (i < n) {
-            const int o = s + r;
-            D.x[o] = S.x[v];
-            D.y[o] = S.y[v];
-            D.l0[o] = S.l0[v];
-            D.l1[o] = S.l1[v];
-            D.u[o] = S.u[v];
-            D.v[o] = S.v[v];
-            D.cw[o] = S.cw[v];
+        // reseed: the q-th missing sub-cell goes to slot s + n + q
+        if (nadd) {
+            const int4 t = tri[c];
+            const double2 A = xy[t.x], B = xy[t.y], E = xy[t.z];
+            const double u0 = ux[t.x], u1 = ux[t.y], u2 = ux[t.z];
+            const double w0 = uy[t.x], w1 = uy[t.y], w2 = uy[t.z];
+            const unsigned missing = ~m & ((1u << ppc) - 1u);
+            for (int q = lane; q < nadd; q += 32) {
+                const int k = (int)__fns(missing, 0, q + 1);
+                const int o = s + n + q;
+                const double L0 = C.c[k][0], L1 = C.c[k][1], L2 = C.c[k][2];
+                D.x[o] = local_to_global(L0, L1, L2, A.x, B.x, E.x);
+                D.y[o] = local_to_global(L0, L1, L2, A.y, B.y, E.y);
+                D.l0[o] = L0;
+                D.l1[o] = L1;
+                D.u[o] = interp3(L0, L1, L2, u0, u1, u2);
+                D.v[o] = interp3(L0, L1, L2, w0, w1, w2);
+                D.cw[o] = c | ((k + 1) << kCellBits);
+            }
         }
     }
-    // reseed: the q-th missing sub-cell goes to slot s + n + q
-    if (nadd) {
-        const int4 t = tri[c];
-        const double2 A = xy[t.x], B = xy[t.y], E = xy[t.z];
-        const double u0 = ux[t.x], u1 = ux[t.y], u2 = ux[t.z];
-        const double w0 = uy[t.x], w1 = uy[t.y], w2 = uy[t.z];
-        const unsigned missing = ~m & full;
-        for (int q = lane; q < nadd; q += 32) {
-            const int k = (int)__fns(missing, 0, q + 1);
-            const int o = s + n + q;
-            const double L0 = C.c[k][0], L1 = C.c[k][1], L2 = C.c[k][2];
-            D.x[o] = local_to_global(L0, L1, L2, A.x, B.x, E.x);
-            D.y[o] = local_to_global(L0, L1, L2, A.y, B.y, E.y);
-            D.l0[o] = L0;
-            D.l1[o] = L1;
-            D.u[o] = interp3(L0, L1, L2, u0, u1, u2);
-            D.v[o] = interp3(L0, L1, L2, w0, w1, w2);
-            D.cw[o] = c | ((k + 1) << kCellBits);
-        }
-    }
-    __syncwarp();
-    // partial sums over the cell's slots, lane j taking slots j, j + 32, ...
-    double acc[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-    const int tot = n + nadd;
-    for (int k = lane; k < tot; k += 32) {
-        const int o = s + k;
-        const int w = D.cw[o];
-        const double l0 = D.l0[o], l1 = D.l1[o];
-        add_partials(acc, l0, l1, third_coord(w, l0, l1, C), D.u[o], D.v[o]);
-    }
-    __shared__ double red[8][9][33];
-    warp_partials_store(acc, lane, red[threadIdx.x >> 5], part, c);
+    block_partials(G, c0, nc, D, C, part);
 }
 
-// Partial sums of every cell from the current (cell-ordered) particles: one warp per
-// cell with k_gather's lane assignment and reduction, so a projection gives the same bits
-// whether its partial sums came from the sort or from here.
+// Partial sums of every cell from the current (cell-ordered) particles, eight cells per
+// block as in k_gather, so a projection gives the same bits whether its partial sums
+// came from the sort or from here.
 __global__ void __launch_bounds__(256) k_partials(int nc, const int* __restrict__ seg, PState S, Centers C,
                                                   Partials part) {
-    const int lane = threadIdx.x & 31;
-    const int c = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-    if (c >= nc) return;  // uniform over the warp
-    double acc[9] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
-    const int s = seg[c], tot = seg[c + 1] - s;
-    for (int k = lane; k < tot; k += 32) {
-        const int p = s + k;
-        const int w = S.cw[p];
-        const double l0 = S.l0[p], l1 = S.l1[p];
-        add_partials(acc, l0, l1, third_coord(w, l0, l1, C), S.u[p], S.v[p]);
+    __shared__ PartialStage G;
+    const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+    const int c0 = blockIdx.x * 8;
+    const int c = c0 + wi;
+    if (lane == 0) {
+        G.bs[wi] = c < nc ? seg[c] : 0;
+        G.bn[wi] = c < nc ? seg[c + 1] - seg[c] : -1;
     }
-    __shared__ double red[8][9][33];
-    warp_partials_store(acc, lane, red[threadIdx.x >> 5], part, c);
+    block_partials(G, c0, nc, S, C, part);
 }
 
 // kFinalizeVelocityProjection (:109-115): u_i = sum L v / sum L over the cells around
