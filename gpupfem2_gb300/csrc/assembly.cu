@@ -371,15 +371,24 @@ __global__ void k_prediction_bc(int nbc, const int* __restrict__ node, const dou
 }
 
 // kCountBodyEdges + kCalculateBodyForces + reduceVector (Cylinder2D/main.cu:299-376,
-// :414-428): one block, each thread strides over the cells and takes the first body
-// edge of each cell; a fixed-order block reduction gives the totals.
-__global__ void k_body_loads(int nc, RowMesh M, FlowCoef P, int body_id, double thickness, double umean, double cx,
-                             double cy, const double* __restrict__ ux, const double* __restrict__ uy,
-                             const double* __restrict__ pres, double* out) {
-    __shared__ double sh[33];
+// :414-428): kLoadBlocks blocks, block b over the cells [b * chunk, (b + 1) * chunk), its
+// threads striding over them and taking the first body edge of each cell (the scan of
+// the cells' edge ids is the kernel's work: a million cells hold a few hundred body
+// edges).  Each block's fixed-order sums go to out[2 ...]; the last block to finish
+// (a ticket after out's partials) adds the blocks' sums in block order, writes the two
+// coefficients and rewinds the ticket.  No block waits for another.
+__global__ void __launch_bounds__(256) k_body_loads(int nc, RowMesh M, FlowCoef P, int body_id, double thickness,
+                                                    double umean, double cx, double cy,
+                                                    const double* __restrict__ ux, const double* __restrict__ uy,
+                                                    const double* __restrict__ pres, double* out) {
+    __shared__ double sh[33 * 4];
+    __shared__ int last;
     const double gq[2] = { -0.577350269189626, 0.577350269189626 };  // quadrature_formula_1d.cu:15-18
     double F[4] = { 0, 0, 0, 0 };
-    for (int c = threadIdx.x; c < nc; c += blockDim.x) {
+    const int chunk = (nc + kLoadBlocks - 1) / kLoadBlocks;
+    const long long lo = (long long)blockIdx.x * chunk;
+    const int c1 = (int)std::min<long long>(nc, lo + chunk);
+    for (int c = (int)std::min<long long>(lo, nc) + threadIdx.x; c < c1; c += blockDim.x) {
         int e = -1;
         for (int k = 0; k < 3; ++k)
             if (M.edge_ids[3 * c + k] == body_id) { e = k; break; }
@@ -412,12 +421,26 @@ __global__ void k_body_loads(int nc, RowMesh M, FlowCoef P, int body_id, double 
             F[3] += P.mu * dvt * ty * w;
         }
     }
-    double tot[4];
-    for (int k = 0; k < 4; ++k) tot[k] = block_sum(F[k], sh);
+    block_sum_n<4>(F, sh);
+    double* part = out + 2;
+    unsigned* ticket = reinterpret_cast<unsigned*>(out + 2 + 4 * kLoadBlocks);
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < 4; ++k) __stcg(&part[k * kLoadBlocks + blockIdx.x], F[k]);
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == kLoadBlocks - 1;
+    }
+    __syncthreads();
+    if (!last) return;  // uniform over the block
+    __threadfence();
+    double tot[4] = { 0, 0, 0, 0 };
+    for (int b = threadIdx.x; b < kLoadBlocks; b += blockDim.x)
+        for (int k = 0; k < 4; ++k) tot[k] += __ldcg(&part[k * kLoadBlocks + b]);
+    block_sum_n<4>(tot, sh);
     if (threadIdx.x == 0) {
         const double coeff = 2.0 / (P.rho * umean * umean * thickness);
         out[0] = (tot[0] + tot[2]) * coeff;
         out[1] = (tot[1] + tot[3]) * coeff;
+        *ticket = 0u;
     }
 }
 
@@ -460,8 +483,8 @@ pf2_status launch_prediction_bc(const pf2_mesh* m, const FlowCoef& P, const pf2_
 pf2_status launch_body_loads(const pf2_mesh* m, const FlowCoef& P, int body_id, double thickness, double umean,
                              double cx, double cy, const double* ux, const double* uy, const double* pres,
                              double* out_dev, cudaStream_t st) {
-    k_body_loads<<<1, 1024, 0, st>>>(m->nc, row_mesh(m), P, body_id, thickness, umean, cx, cy, ux, uy, pres,
-                                     out_dev);
+    k_body_loads<<<kLoadBlocks, 256, 0, st>>>(m->nc, row_mesh(m), P, body_id, thickness, umean, cx, cy, ux, uy,
+                                              pres, out_dev);
     PF2_LAUNCH_CHECK();
     return PF2_OK;
 }
@@ -577,7 +600,8 @@ pf2_status pf2_body_loads(const pf2_mesh* m, const pf2_params* p, double cx, dou
     PF2_REQUIRE(m && p && ux && uy && pres && cxcy, PF2_BAD_INPUT, "null argument");
     cudaStream_t st = as_stream(stream);
     DevBuf<double> out;
-    PF2_TRY(out.alloc(2));
+    PF2_TRY(out.alloc(kBodyLoadsDoubles));
+    PF2_CUDA(cudaMemsetAsync(out.p, 0, sizeof(double) * kBodyLoadsDoubles, st));
     PF2_TRY(launch_body_loads(m, FlowCoef{ p->rho, p->mu, p->dt }, p->body_boundary_id, p->thickness,
                               p->mean_velocity, cx, cy, ux, uy, pres, out.p, st));
     PF2_CUDA(cudaMemcpyAsync(cxcy, out.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -147,11 +147,11 @@ pf2_status pf2_flow_create(const pf2_mesh* mesh, const pf2_params* p, int nbx, c
     o.ordering = PF2_ORDERING_NATURAL;
     o.precond = PF2_PRECOND_JACOBI;
     if ((s = pf2_solver_create(F->A[3], &o, &F->cg_c))) return fail(s);
-    if ((s = F->rec.alloc(kRecords)) || (s = F->h_rec.alloc(kRecords)) || (s = F->loads.alloc(2)) ||
-        (s = F->h_loads.alloc(2)) || (s = F->h_np.alloc(2)))
+    if ((s = F->rec.alloc(kRecords)) || (s = F->h_rec.alloc(kRecords)) ||
+        (s = F->loads.alloc(kBodyLoadsDoubles)) || (s = F->h_loads.alloc(2)) || (s = F->h_np.alloc(2)))
         return fail(s);
     if (cudaMemset(F->rec.p, 0, sizeof(SolveRecord) * kRecords) != cudaSuccess ||
-        cudaMemset(F->loads.p, 0, sizeof(double) * 2) != cudaSuccess)
+        cudaMemset(F->loads.p, 0, sizeof(double) * kBodyLoadsDoubles) != cudaSuccess)
         return fail(PF2_CUDA_ERROR);
     if (cudaEventCreateWithFlags(&F->done, cudaEventDisableTiming) != cudaSuccess) return fail(PF2_CUDA_ERROR);
     if ((s = F->guess_res.alloc(2)) || (s = F->guess_used.alloc(1)) || (s = F->h_guess_res.alloc(2)) ||

@@ -19,6 +19,10 @@ pf2_status launch_correction(const pf2_mesh* m, const FlowCoef& P, bool matrix, 
                              double* rhsy, const pf2_bc* bcx, const pf2_bc* bcy, cudaStream_t st);
 pf2_status launch_prediction_bc(const pf2_mesh* m, const FlowCoef& P, const pf2_bc* src, pf2_bc* dst,
                                 const double* pres, const double* pold, int comp, cudaStream_t st);
+// Drag and lift coefficients into out_dev[0..1]; out_dev holds kBodyLoadsDoubles doubles
+// (the blocks' partial sums and a ticket after the two results), zeroed before first use.
+constexpr int kLoadBlocks = 1024;
+constexpr int kBodyLoadsDoubles = 2 + 4 * kLoadBlocks + 1;
 pf2_status launch_body_loads(const pf2_mesh* m, const FlowCoef& P, int body_id, double thickness, double umean,
                              double cx, double cy, const double* ux, const double* uy, const double* pres,
                              double* out_dev, cudaStream_t st);

@@ -364,7 +364,8 @@ __device__ __forceinline__ void block_partials(PartialStage& G, int c0, int nc, 
     }
     __syncthreads();
     if (t < 216 && q == 0 && c0 + i < nc && G.bn[i] >= 0)
-        part.s[(size_t)(3 * a + j) * part.nc + c0 + i] = __dadd_rn(__dadd_rn(G.third[t], G.third[t + 1]), G.third[t + 2]);
+        part.s[(size_t)(3 * a + j) * part.nc + c0 + i] =
+            __dadd_rn(__dadd_rn(G.third[t], G.third[t + 1]), G.third[t + 2]);
 }
 
 // Per cell, one warp: stable order, move, reseed (kAddParticlesToCell :197-236); then the
