@@ -26,6 +26,7 @@ SOLVER_CG, SOLVER_GMRES, SOLVER_BICGSTAB = 0, 1, 2
 PRECOND = {"none": -1, "jacobi": 0, "ilu": 1, "ic": 2}
 CRITERION_ABS, CRITERION_REL = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
+X0_GIVEN, X0_LEARNED = 0, 1  # pf2_params.pressure_x0
 RHS_GAUSSIAN, RHS_SINSIN = 0, 1
 RHS3D_GAUSSIAN, RHS3D_SINSINSIN = 0, 1
 CG_STANDARD, CG_ONE_REDUCTION, CG_PIPELINED = 0, 1, 2
