@@ -30,8 +30,8 @@ constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 do
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
 constexpr double kMixedInnerEta = 0.1;  // mixed CG refines when the iterated residual drops by this factor
 constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
-constexpr int kBandMinLevels = 128;
-constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)  // dependency chains at least this long use the banded solve
+constexpr int kBandMinLevels = 128;  // dependency chains at least this long use the banded solve
+constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)
 
 struct Csr {
     int n;
