@@ -374,7 +374,7 @@ __device__ __forceinline__ void block_partials(PartialStage& G, int c0, int nc, 
 // old order is the order the cell keeps), moves it to slot s + rank, then lanes fill the
 // missing sub-cells after them.  The partial sums are formed over the slots after the
 // moves, so they do not depend on the atomics' order.
-__global__ void __launch_bounds__(256) k_gather(int nc, const int* __restrict__ seg, int* count, int* mask,
+__global__ void __launch_bounds__(256, 5) k_gather(int nc, const int* __restrict__ seg, int* count, int* mask,
                                                 const int* __restrict__ perm, PState S, PState D, Centers C,
                                                 int level, int reseed, const double2* __restrict__ xy,
                                                 const int4* __restrict__ tri, const double* __restrict__ ux,
