@@ -28,7 +28,7 @@ constexpr int kSolverThreads = 512;
 constexpr int kMaxGmresSmem = 1024;
 constexpr int kShDoubles = 136;  // block_sum_n / grid_reduce scratch (33 x 4 doubles)
 constexpr int kMaxOuter = 40;    // refinements of the mixed-precision solver
-constexpr double kMixedInnerEta = 0.1;  // mixed CG refines when the iterated residual drops by this factor
+constexpr double kMixedInnerEta = 0.3;  // mixed CG refines when the iterated residual drops by this factor
 constexpr int kBandRows = 12288;  // rows per range of the banded triangular solve (96 KB FP64 window)
 constexpr int kBandMinLevels = 128;  // dependency chains at least this long use the banded solve
 constexpr int kSolverBlocksPerSm = 2;  // cooperative solver blocks per SM (grid-barrier cost vs parallelism)

@@ -276,7 +276,8 @@ enum { PF2_CRITERION_ABS = 0,   /* CG: r^T z < tol^2; GMRES: |beta_k| < tol (the
 enum { PF2_PRECISION_FP64 = 0,    /* the reference's FP64 PCG */
        PF2_PRECISION_MIXED = 1 };  /* CG iteration in FP32 (FP64 sums across threads) with reliable
                                       updates: x += d, r = b - A x and the test in FP64 whenever
-                                      the iterated residual drops tenfold; CG only */
+                                      the iterated residual drops to 0.3 of the last true
+                                      residual; CG only */
 enum { PF2_X0_GIVEN = 0, PF2_X0_LEARNED = 1 };
 enum { PF2_ORDERING_NATURAL = 0,    /* ILU(0)/IC(0) on A as numbered (the reference's)     */
        PF2_ORDERING_MULTICOLOR = 1 }; /* on P A P^T, P a greedy colouring whose thin tail of
